@@ -1,0 +1,158 @@
+/*
+ * openph.h — C ABI of the GB300-native OpenPH reduction library
+ * (libopenph_gb300.so).  Plain pointers and sizes only.
+ *
+ * The reduction is over Z/2 on a filtered complex's boundary matrix: columns
+ * are added left to right until every nonzero column has a distinct low (the
+ * row of its last nonzero).  Every algorithm below yields the same low array
+ * (the lows of a reduced matrix are unique).  All algorithms run on the GPU;
+ * there is no CPU fallback: without a usable CUDA device the calls fail with
+ * OPH_ERR_CUDA.
+ */
+#ifndef OPENPH_GB300_H
+#define OPENPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+enum {
+    OPH_OK = 0,
+    OPH_ERR_BAD_INPUT = 1,  /* malformed matrix or argument; nothing ran       */
+    OPH_ERR_OOM = 2,        /* device memory (or the caller's budget) exhausted */
+    OPH_ERR_OVERFLOW = 3,   /* column store could not grow any further          */
+    OPH_ERR_TIMEOUT = 4,    /* sweep/iteration cap reached before convergence   */
+    OPH_ERR_CUDA = 5,       /* CUDA runtime error (no device, launch failure)   */
+    OPH_ERR_ALGO = 6        /* algorithm string not recognised                  */
+};
+
+/* algorithm ids; the strings of the reference's dispatch
+ * (src/cuda/algorithms/algorithm_factory.cu:10-12, 54-78, 103-148) map to
+ * these: "standard", "twist", "ph_row", "standard_parallel", "twist_parallel",
+ * "ph_row_parallel", "pms". */
+enum {
+    OPH_ALGO_STANDARD = 0,
+    OPH_ALGO_TWIST = 1,
+    OPH_ALGO_PH_ROW = 2,
+    OPH_ALGO_STANDARD_PARALLEL = 3,
+    OPH_ALGO_TWIST_PARALLEL = 4,
+    OPH_ALGO_PH_ROW_PARALLEL = 5,
+    OPH_ALGO_PMS = 6
+};
+
+/* Returns the algorithm id for a reference algorithm string, or -1. */
+int oph_algo_from_string(const char *algstr);
+const char *oph_status_string(int status);
+
+/* --------------------------------------------------------- drop-in entry */
+/*
+ * openph — the reference's C function behind the `ph` MATLAB MEX call,
+ * same name, arguments and meaning (replaces src/cuda/openph.cu:29-35, called
+ * from src/matlab/ph/ph.cu:71-74).
+ *
+ *   algstr      one of the seven reference algorithm strings
+ *   h_rows_in   int32[nnz], 1-based row of each nonzero
+ *   h_cols_in   int32[nnz], 1-based column of each nonzero, non-decreasing;
+ *               rows ascending inside a column
+ *   m           number of columns (= rows)
+ *   col_width   accepted and ignored: column capacity is adaptive, no fixed
+ *               slot count is needed
+ *   h_low_true  int32[m] 1-based true lows (0 = none) used only by the
+ *               progress trackers; may be all zeros or NULL
+ *   nnz         number of nonzeros
+ *   h_low       out int32[m]: 1-based low of each reduced column, 0 if zero
+ *   h_ess       out int32[m]: 1 if the column is estimated essential
+ *   err_linf, err_lone, err_redu, err_ess, time_track
+ *               out float[m+1] progress trackers (index 0 = initial state,
+ *               1..num_iters-1 = after each iteration); each may be NULL
+ *   num_iters   out int32[1]
+ *   gpu_number  CUDA device ordinal (the reference hard-codes 0 in the MEX)
+ *
+ * Like the reference, this returns nothing; errors are reported on stderr
+ * and leave h_low all zeros.  Use oph_openph for a status code.
+ */
+void openph(char *algstr, int *h_rows_in, int *h_cols_in, int m, int col_width, int *h_low_true, int nnz,
+            int *h_low, int *h_ess, float *err_linf, float *err_lone, float *err_redu, float *err_ess,
+            float *time_track, int *num_iters, int gpu_number);
+
+/* openph with a status code (OPH_OK on success). */
+int oph_openph(const char *algstr, const int *h_rows_in, const int *h_cols_in, int m, int col_width,
+               const int *h_low_true, int nnz, int *h_low, int *h_ess, float *err_linf, float *err_lone,
+               float *err_redu, float *err_ess, float *time_track, int *num_iters, int gpu_number);
+
+/* ------------------------------------------------------- context-based API */
+typedef struct oph_context oph_context;
+
+typedef struct {
+    int32_t num_iters;       /* iterations as the reference counts them        */
+    int32_t sweeps;          /* pms sweeps (0 for the sequential variants)     */
+    int64_t additions;       /* column additions performed on the device       */
+    int64_t slots_moved;     /* sum over additions of |P| + |T| + |T xor P|    */
+    int64_t pool_bytes;      /* column-store bytes in use at the end           */
+    int32_t regrows;         /* times the column store had to grow             */
+    float device_ms;         /* device time of the reduction (CUDA events)     */
+} oph_info;
+
+/* A context owns one CUDA stream on one device plus cached device buffers;
+ * calls on one context are serialised on its stream, distinct contexts may be
+ * used from distinct host threads.  No global device symbols are used. */
+int oph_context_create(int device, oph_context **out);
+int oph_context_destroy(oph_context *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order work. */
+void *oph_context_stream(oph_context *ctx);
+/* Cap on device bytes the context may hold (0 = no cap). */
+int oph_context_set_budget(oph_context *ctx, int64_t bytes);
+
+/*
+ * oph_reduce — reduce one boundary matrix given as host 0-based CSC.
+ *   colptr int64[m+1], rows int32[colptr[m]] (ascending inside each column)
+ *   low    out int32[m], 0-based, -1 = zero or cleared column
+ *   ess    out int32[m] (may be NULL)
+ *   arglow out int32[m], arglow[i] = column whose low is i, or -1 (may be NULL)
+ */
+int oph_reduce(oph_context *ctx, int algo, int64_t m, const int64_t *colptr, const int32_t *rows, int32_t *low,
+               int32_t *ess, int32_t *arglow, oph_info *info);
+
+/*
+ * oph_reduce_device — the same on device-resident buffers, asynchronously on
+ * the context's stream except for the host reads of the convergence flag.
+ * d_colptr/d_rows/d_low/d_ess/d_arglow are device pointers (d_ess and
+ * d_arglow may be NULL).
+ */
+int oph_reduce_device(oph_context *ctx, int algo, int64_t m, const int64_t *d_colptr, const int32_t *d_rows,
+                      int32_t *d_low, int32_t *d_ess, int32_t *d_arglow, oph_info *info);
+
+/*
+ * oph_reduce_batch — reduce `count` independent matrices in one pass over a
+ * segmented store.  Instance b owns columns [col_off[b], col_off[b+1]) of the
+ * concatenation; colptr (int64[col_off[count]+1]) indexes the concatenated
+ * rows, and each instance's row indices are LOCAL (0-based within the
+ * instance).  low/ess are concatenated per-instance local outputs.
+ * Host buffers; ess may be NULL.
+ */
+int oph_reduce_batch(oph_context *ctx, int algo, int32_t count, const int64_t *col_off, const int64_t *colptr,
+                     const int32_t *rows, int32_t *low, int32_t *ess, oph_info *info);
+
+/* the same on device buffers (asynchronous on the context's stream) */
+int oph_reduce_batch_device(oph_context *ctx, int algo, int32_t count, const int64_t *d_col_off,
+                            const int64_t *d_colptr, const int32_t *d_rows, int64_t total_m, int64_t total_nnz,
+                            int32_t *d_low, int32_t *d_ess, oph_info *info);
+
+/* ------------------------------------------------------------ diagnostics */
+/* Kernel-level timing of the last reduction on this context: per-kernel
+ * cumulative device milliseconds for the pms phases (Phase II first). */
+int oph_last_phase_ms(oph_context *ctx, float *phase2_ms, float *phase1_ms, float *setup_ms, int32_t *phase2_launches);
+
+/* Testing hooks: cap the sweep count (0 = default) and the initial column
+ * store size in bytes (0 = default), to exercise the timeout and regrow
+ * paths without faulting anything. */
+int oph_context_set_limits(oph_context *ctx, int32_t max_sweeps, int64_t initial_pool_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPENPH_GB300_H */

@@ -1,0 +1,584 @@
+// C ABI of libopenph_gb300 (include/openph.h): contexts, device workspace,
+// input conversion, algorithm dispatch and output finalisation.
+//
+// Reference counterparts: openph() (src/cuda/openph.cu:29-237) and
+// algorithm_factory() (src/cuda/algorithms/algorithm_factory.cu:1-151).
+// Unlike the reference, device buffers are cached per context instead of
+// ~17 cudaMalloc/cudaFree pairs per call, every call runs on the context's
+// own stream, and nothing uses global __device__ symbols, so distinct
+// contexts are independent.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "oph_host.h"
+
+using namespace oph;
+
+struct oph_context : public oph::Context {};
+
+namespace oph {
+
+void *ctx_alloc(Context *ctx, int slot, size_t bytes) {
+    DevBuf &b = ctx->bufs[slot];
+    if (bytes == 0) bytes = 16;
+    bytes = (bytes + 255) & ~(size_t)255;
+    if (b.bytes >= bytes) return b.ptr;
+    if (ctx->budget > 0) {
+        size_t total = 0;
+        for (int i = 0; i < S_NSLOTS; i++) total += (i == slot) ? 0 : ctx->bufs[i].bytes;
+        if ((int64_t)(total + bytes) > ctx->budget) return nullptr;
+    }
+    if (b.ptr) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(b.ptr);
+        b.ptr = nullptr;
+        b.bytes = 0;
+    }
+    if (cudaMalloc(&b.ptr, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        b.ptr = nullptr;
+        return nullptr;
+    }
+    b.bytes = bytes;
+    return b.ptr;
+}
+
+// --------------------------------------------------------------- kernels
+// Batch input: shift each instance's local rows into its column range.
+__global__ void k_shift_rows(const int64_t *__restrict__ colptr, const int64_t *__restrict__ inst_off, int count,
+                             int64_t m, const int32_t *__restrict__ rows_local, int32_t *__restrict__ rows_global) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = count;  // last b with inst_off[b] <= j
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (inst_off[mid] <= j) lo = mid; else hi = mid;
+        }
+        const int64_t base = inst_off[lo];
+        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) rows_global[k] = rows_local[k] + (int32_t)base;
+    }
+}
+
+enum EssMode { ESS_PAIRS = 0, ESS_ROW_PARALLEL = 1, ESS_RUNNING = 2 };
+
+// Output pass 1: low (0- or 1-based, optionally local to its batch instance),
+// ess initial values, arglow cleared.
+__global__ void k_finalize1(const int32_t *__restrict__ low, int64_t m, int one_based, int ess_mode,
+                            const int64_t *__restrict__ inst_off, int count, int32_t *__restrict__ out_low,
+                            int32_t *__restrict__ ess, int32_t *__restrict__ arglow) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        int l = low[j];
+        int64_t base = 0;
+        if (inst_off) {
+            int lo = 0, hi = count;
+            while (hi - lo > 1) {
+                int mid = (lo + hi) >> 1;
+                if (inst_off[mid] <= j) lo = mid; else hi = mid;
+            }
+            base = inst_off[lo];
+        }
+        if (out_low) out_low[j] = l >= 0 ? (int32_t)(l - base) + one_based : (one_based ? 0 : -1);
+        if (ess) {
+            if (ess_mode == ESS_PAIRS) ess[j] = l >= 0 ? 0 : 1;
+            else if (ess_mode == ESS_ROW_PARALLEL) ess[j] = 1;
+            else if (l >= 0) ess[j] = 0;
+        }
+        if (arglow) arglow[j] = -1;
+    }
+}
+
+// Output pass 2: the row of every nonzero low is paired (ess 0), arglow.
+__global__ void k_finalize2(const int32_t *__restrict__ low, int64_t m, const int64_t *__restrict__ inst_off,
+                            int count, int32_t *__restrict__ ess, int32_t *__restrict__ arglow) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        int l = low[j];
+        if (l < 0) continue;
+        if (ess) ess[l] = 0;
+        if (arglow) {
+            int64_t base = 0;
+            if (inst_off) {
+                int lo = 0, hi = count;
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (inst_off[mid] <= j) lo = mid; else hi = mid;
+                }
+                base = inst_off[lo];
+            }
+            arglow[l] = (int32_t)(j - base);
+        }
+    }
+}
+
+__global__ void k_fill_i32(int32_t *p, int64_t n, int32_t v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// Tracker sums for the reference's progress outputs (tracker.cu:92-134):
+// acc[0] = sum |low - low_true|, acc[1] = max |.|, acc[2] = sum ess,
+// acc[3] = sum ess_true, acc[4] = sum |low_true + 1| (1-based norm),
+// acc[5] = max |low_true + 1|.  Lows 0-based; low_true 0-based (-1 = none).
+__global__ void k_tracker(const int32_t *__restrict__ low, const int32_t *__restrict__ low_true,
+                          const int32_t *__restrict__ ess, const int32_t *__restrict__ ess_true, int64_t m,
+                          double *acc) {
+    double s = 0, mx = 0, se = 0, st = 0, nt = 0, mt = 0;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        double d = fabs((double)low[j] - (double)low_true[j]);
+        s += d;
+        mx = fmax(mx, d);
+        se += ess[j];
+        st += ess_true[j];
+        double t = fabs((double)low_true[j] + 1.0);
+        nt += t;
+        mt = fmax(mt, t);
+    }
+    atomicAdd(&acc[0], s);
+    atomicAdd(&acc[2], se);
+    atomicAdd(&acc[3], st);
+    atomicAdd(&acc[4], nt);
+    // maxima of non-negative doubles compare as their bit patterns
+    atomicMax((unsigned long long *)&acc[1], (unsigned long long)__double_as_longlong(mx));
+    atomicMax((unsigned long long *)&acc[5], (unsigned long long)__double_as_longlong(mt));
+}
+
+// ess_true from low_true (compute_ess_true, src/cuda/kernels.cu:54-62).
+__global__ void k_ess_true(const int32_t *__restrict__ low_true, int64_t m, int32_t *__restrict__ ess_true, int pass) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        int l = low_true[j];
+        if (pass == 0) ess_true[j] = l >= 0 ? 0 : 1;
+        else if (l >= 0 && l < m) ess_true[l] = 0;
+    }
+}
+
+__global__ void k_shift_down(const int *__restrict__ in, int64_t m, int32_t *__restrict__ out) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
+        out[j] = in[j] - 1;
+}
+
+int ctx_sync_status(Context *ctx, Work &w, DevStatus *out) {
+    OPH_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, w.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, ctx->stream));
+    OPH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (out) *out = *ctx->h_status;
+    return OPH_OK;
+}
+
+static int grid_for(Context *ctx, int64_t n) {
+    int64_t g = (n + 255) / 256;
+    int64_t cap = (int64_t)ctx->sm_count * 16;
+    if (g > cap) g = cap;
+    return g < 1 ? 1 : (int)g;
+}
+
+// Allocates the per-column working arrays of a reduction of m columns.
+static int alloc_work(Context *ctx, Work &w, int64_t m) {
+    const int64_t mm = m > 0 ? m : 1;
+    w.m = m;
+    w.low = (int32_t *)ctx_alloc(ctx, S_LOW, sizeof(int32_t) * mm);
+    w.classes = (int8_t *)ctx_alloc(ctx, S_CLASSES, mm);
+    w.clear = (uint8_t *)ctx_alloc(ctx, S_CLEAR, mm);
+    w.dim = (int8_t *)ctx_alloc(ctx, S_DIM, mm);
+    w.first = (int32_t *)ctx_alloc(ctx, S_FIRST, sizeof(int32_t) * mm);
+    w.left = (int32_t *)ctx_alloc(ctx, S_LEFT, sizeof(int32_t) * mm);
+    w.beta = (int32_t *)ctx_alloc(ctx, S_BETA, sizeof(int32_t) * mm);
+    w.worklist = (int32_t *)ctx_alloc(ctx, S_WORK, sizeof(int32_t) * mm);
+    w.widelist = (int32_t *)ctx_alloc(ctx, S_WIDE, sizeof(int32_t) * mm);
+    w.seg = (int64_t *)ctx_alloc(ctx, S_SEG, sizeof(int64_t) * mm);
+    w.rowpiv = (unsigned long long *)ctx_alloc(ctx, S_ROWPIV, sizeof(unsigned long long) * mm);
+    w.ntiles = (m + 2047) / 2048;
+    w.agg = (int32_t *)ctx_alloc(ctx, S_AGG, sizeof(int32_t) * MAXC * (w.ntiles + 1) + 64);
+    w.st = (DevStatus *)ctx_alloc(ctx, S_STATUS, sizeof(DevStatus));
+    if (!w.low || !w.classes || !w.clear || !w.dim || !w.first || !w.left || !w.beta || !w.worklist ||
+        !w.widelist || !w.seg || !w.rowpiv || !w.agg || !w.st)
+        return OPH_ERR_OOM;
+    return OPH_OK;
+}
+
+struct Outputs {
+    int32_t *low = nullptr;     // device, m
+    int one_based = 0;
+    int32_t *ess = nullptr;     // device, m (may be null)
+    int32_t *arglow = nullptr;  // device, m (may be null)
+    const int64_t *inst_off = nullptr;
+    int count = 0;
+};
+
+// Runs `algo` on the CSC already in w.colptr / w.rows and writes outputs.
+static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_info *info) {
+    cudaStream_t s = ctx->stream;
+    const int64_t m = w.m;
+    const bool pms = algo == OPH_ALGO_PMS;
+    int rc = setup_store(ctx, w, pms);
+    if (rc) return rc;
+    DevStatus hs;
+    if ((rc = ctx_sync_status(ctx, w, &hs))) return rc;
+    if (hs.error) return OPH_ERR_BAD_INPUT;
+    // the Phase I scan keeps one running maximum per dimension bucket -1 .. MAXC-2
+    if (pms && hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;
+    const int row_quirk = algo == OPH_ALGO_PH_ROW;
+    if (row_quirk && o.ess) k_fill_i32<<<grid_for(ctx, m), 256, 0, s>>>(o.ess, m, 1);
+    oph_info local{};
+    if (m > 0) {
+        if (pms) {
+            rc = run_pms(ctx, w, &local);
+        } else {
+            rc = run_sequential(ctx, w, algo, row_quirk ? o.ess : nullptr, &local);
+        }
+        if (rc) return rc;
+    } else {
+        local.num_iters = 1;
+    }
+    const int ess_mode = algo == OPH_ALGO_PH_ROW_PARALLEL ? ESS_ROW_PARALLEL : (row_quirk ? ESS_RUNNING : ESS_PAIRS);
+    if (m > 0) {
+        k_finalize1<<<grid_for(ctx, m), 256, 0, s>>>(w.low, m, o.one_based, ess_mode, o.inst_off, o.count, o.low,
+                                                     o.ess, o.arglow);
+        k_finalize2<<<grid_for(ctx, m), 256, 0, s>>>(w.low, m, o.inst_off, o.count, o.ess, o.arglow);
+        OPH_CUDA_TRY(cudaGetLastError());
+    }
+    if (info) *info = local;
+    return OPH_OK;
+}
+
+static int check_algo(int algo) { return algo >= OPH_ALGO_STANDARD && algo <= OPH_ALGO_PMS ? OPH_OK : OPH_ERR_ALGO; }
+
+}  // namespace oph
+
+// =================================================================== C ABI
+extern "C" {
+
+__attribute__((visibility("default"))) int oph_algo_from_string(const char *algstr) {
+    if (!algstr) return -1;
+    static const char *names[] = {"standard", "twist", "ph_row", "standard_parallel", "twist_parallel",
+                                  "ph_row_parallel", "pms"};
+    for (int i = 0; i < 7; i++)
+        if (strcmp(algstr, names[i]) == 0) return i;
+    return -1;
+}
+
+__attribute__((visibility("default"))) const char *oph_status_string(int status) {
+    switch (status) {
+        case OPH_OK: return "ok";
+        case OPH_ERR_BAD_INPUT: return "malformed boundary matrix or argument";
+        case OPH_ERR_OOM: return "out of device memory (or over the context budget)";
+        case OPH_ERR_OVERFLOW: return "column store cannot grow any further";
+        case OPH_ERR_TIMEOUT: return "iteration cap reached before convergence";
+        case OPH_ERR_CUDA: return "CUDA runtime error";
+        case OPH_ERR_ALGO: return "algorithm not recognised";
+        default: return "unknown status";
+    }
+}
+
+__attribute__((visibility("default"))) int oph_context_create(int device, oph_context **out) {
+    if (!out) return OPH_ERR_BAD_INPUT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return OPH_ERR_CUDA;
+    }
+    if (device < 0 || device >= n) return OPH_ERR_BAD_INPUT;
+    OPH_CUDA_TRY(cudaSetDevice(device));
+    oph_context *ctx = new oph_context();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost((void **)&ctx->h_status, sizeof(DevStatus)) != cudaSuccess) {
+        delete ctx;
+        return OPH_ERR_CUDA;
+    }
+    for (auto &e : ctx->ev) cudaEventCreate(&e);
+    *out = ctx;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_context_destroy(oph_context *ctx) {
+    if (!ctx) return OPH_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto &b : ctx->bufs)
+        if (b.ptr) cudaFree(b.ptr);
+    for (auto &e : ctx->ev) cudaEventDestroy(e);
+    if (ctx->h_status) cudaFreeHost(ctx->h_status);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) void *oph_context_stream(oph_context *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+__attribute__((visibility("default"))) int oph_context_set_budget(oph_context *ctx, int64_t bytes) {
+    if (!ctx || bytes < 0) return OPH_ERR_BAD_INPUT;
+    ctx->budget = bytes;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_context_set_limits(oph_context *ctx, int32_t max_sweeps,
+                                                                  int64_t initial_pool_bytes) {
+    if (!ctx || max_sweeps < 0 || initial_pool_bytes < 0) return OPH_ERR_BAD_INPUT;
+    ctx->max_sweeps = max_sweeps;
+    ctx->initial_pool_bytes = initial_pool_bytes;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_last_phase_ms(oph_context *ctx, float *p2, float *p1, float *setup,
+                                                             int32_t *p2_launches) {
+    if (!ctx) return OPH_ERR_BAD_INPUT;
+    if (p2) *p2 = ctx->phase2_ms;
+    if (p1) *p1 = ctx->phase1_ms;
+    if (setup) *setup = ctx->setup_ms;
+    if (p2_launches) *p2_launches = ctx->phase2_launches;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_reduce_device(oph_context *ctx, int algo, int64_t m,
+                                                             const int64_t *d_colptr, const int32_t *d_rows,
+                                                             int32_t *d_low, int32_t *d_ess, int32_t *d_arglow,
+                                                             oph_info *info) {
+    if (!ctx || m < 0 || m >= (1ll << 29) || !d_colptr || (m > 0 && !d_low)) return OPH_ERR_BAD_INPUT;
+    if (check_algo(algo)) return OPH_ERR_ALGO;
+    OPH_CUDA_TRY(cudaSetDevice(ctx->device));
+    int64_t nnz = 0;
+    OPH_CUDA_TRY(cudaMemcpyAsync(&nnz, d_colptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    OPH_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    if (nnz < 0 || (nnz > 0 && !d_rows)) return OPH_ERR_BAD_INPUT;
+    Work w;
+    int rc = alloc_work(ctx, w, m);
+    if (rc) return rc;
+    w.nnz = nnz;
+    w.colptr = d_colptr;
+    w.rows = d_rows;
+    Outputs o;
+    o.low = d_low;
+    o.ess = d_ess;
+    o.arglow = d_arglow;
+    rc = reduce_core(ctx, algo, w, o, info);
+    if (rc) return rc;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_reduce(oph_context *ctx, int algo, int64_t m, const int64_t *colptr,
+                                                      const int32_t *rows, int32_t *low, int32_t *ess,
+                                                      int32_t *arglow, oph_info *info) {
+    if (!ctx || m < 0 || m >= (1ll << 29) || !colptr || (m > 0 && !low)) return OPH_ERR_BAD_INPUT;
+    if (check_algo(algo)) return OPH_ERR_ALGO;
+    const int64_t nnz = colptr[m];
+    if (nnz < 0 || colptr[0] != 0 || (nnz > 0 && !rows)) return OPH_ERR_BAD_INPUT;
+    OPH_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    int64_t *d_colptr = (int64_t *)ctx_alloc(ctx, S_COLPTR, sizeof(int64_t) * (m + 1));
+    int32_t *d_rows = (int32_t *)ctx_alloc(ctx, S_ROWS, sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+    int32_t *d_out = (int32_t *)ctx_alloc(ctx, S_ESS, sizeof(int32_t) * 3 * (m > 0 ? m : 1));
+    if (!d_colptr || !d_rows || !d_out) return OPH_ERR_OOM;
+    OPH_CUDA_TRY(cudaMemcpyAsync(d_colptr, colptr, sizeof(int64_t) * (m + 1), cudaMemcpyHostToDevice, s));
+    if (nnz > 0) OPH_CUDA_TRY(cudaMemcpyAsync(d_rows, rows, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice, s));
+    Work w;
+    int rc = alloc_work(ctx, w, m);
+    if (rc) return rc;
+    w.nnz = nnz;
+    w.colptr = d_colptr;
+    w.rows = d_rows;
+    Outputs o;
+    o.low = d_out;
+    o.ess = ess ? d_out + m : nullptr;
+    o.arglow = arglow ? d_out + 2 * m : nullptr;
+    rc = reduce_core(ctx, algo, w, o, info);
+    if (rc) return rc;
+    if (m > 0) {
+        OPH_CUDA_TRY(cudaMemcpyAsync(low, d_out, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+        if (ess) OPH_CUDA_TRY(cudaMemcpyAsync(ess, d_out + m, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+        if (arglow) OPH_CUDA_TRY(cudaMemcpyAsync(arglow, d_out + 2 * m, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+    }
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    return OPH_OK;
+}
+
+static int batch_core(oph_context *ctx, int algo, int32_t count, const int64_t *d_col_off, const int64_t *d_colptr,
+                      const int32_t *d_rows_local, int64_t total_m, int64_t total_nnz, int32_t *d_low, int32_t *d_ess,
+                      oph_info *info) {
+    cudaStream_t s = ctx->stream;
+    int32_t *d_rows_g = (int32_t *)ctx_alloc(ctx, S_COO_R, sizeof(int32_t) * (total_nnz > 0 ? total_nnz : 1));
+    if (!d_rows_g) return OPH_ERR_OOM;
+    if (total_m > 0)
+        k_shift_rows<<<grid_for(ctx, total_m), 256, 0, s>>>(d_colptr, d_col_off, count, total_m, d_rows_local,
+                                                            d_rows_g);
+    OPH_CUDA_TRY(cudaGetLastError());
+    Work w;
+    int rc = alloc_work(ctx, w, total_m);
+    if (rc) return rc;
+    w.nnz = total_nnz;
+    w.colptr = d_colptr;
+    w.rows = d_rows_g;
+    Outputs o;
+    o.low = d_low;
+    o.ess = d_ess;
+    o.inst_off = d_col_off;
+    o.count = count;
+    return reduce_core(ctx, algo, w, o, info);
+}
+
+__attribute__((visibility("default"))) int oph_reduce_batch_device(oph_context *ctx, int algo, int32_t count,
+                                                                   const int64_t *d_col_off, const int64_t *d_colptr,
+                                                                   const int32_t *d_rows, int64_t total_m,
+                                                                   int64_t total_nnz, int32_t *d_low, int32_t *d_ess,
+                                                                   oph_info *info) {
+    if (!ctx || count < 1 || total_m < 0 || total_m >= (1ll << 29) || total_nnz < 0 || !d_col_off || !d_colptr ||
+        (total_m > 0 && !d_low))
+        return OPH_ERR_BAD_INPUT;
+    if (check_algo(algo)) return OPH_ERR_ALGO;
+    OPH_CUDA_TRY(cudaSetDevice(ctx->device));
+    return batch_core(ctx, algo, count, d_col_off, d_colptr, d_rows, total_m, total_nnz, d_low, d_ess, info);
+}
+
+__attribute__((visibility("default"))) int oph_reduce_batch(oph_context *ctx, int algo, int32_t count,
+                                                            const int64_t *col_off, const int64_t *colptr,
+                                                            const int32_t *rows, int32_t *low, int32_t *ess,
+                                                            oph_info *info) {
+    if (!ctx || count < 1 || !col_off || !colptr) return OPH_ERR_BAD_INPUT;
+    if (check_algo(algo)) return OPH_ERR_ALGO;
+    const int64_t total_m = col_off[count];
+    if (total_m < 0 || total_m >= (1ll << 29) || col_off[0] != 0 || (total_m > 0 && !low)) return OPH_ERR_BAD_INPUT;
+    for (int b = 0; b < count; b++)
+        if (col_off[b + 1] < col_off[b]) return OPH_ERR_BAD_INPUT;
+    const int64_t total_nnz = colptr[total_m];
+    if (total_nnz < 0 || (total_nnz > 0 && !rows)) return OPH_ERR_BAD_INPUT;
+    OPH_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    int64_t *d_off = (int64_t *)ctx_alloc(ctx, S_INSTOFF, sizeof(int64_t) * (count + 1));
+    int64_t *d_colptr = (int64_t *)ctx_alloc(ctx, S_COLPTR, sizeof(int64_t) * (total_m + 1));
+    int32_t *d_rows = (int32_t *)ctx_alloc(ctx, S_ROWS, sizeof(int32_t) * (total_nnz > 0 ? total_nnz : 1));
+    int32_t *d_out = (int32_t *)ctx_alloc(ctx, S_ESS, sizeof(int32_t) * 2 * (total_m > 0 ? total_m : 1));
+    if (!d_off || !d_colptr || !d_rows || !d_out) return OPH_ERR_OOM;
+    OPH_CUDA_TRY(cudaMemcpyAsync(d_off, col_off, sizeof(int64_t) * (count + 1), cudaMemcpyHostToDevice, s));
+    OPH_CUDA_TRY(cudaMemcpyAsync(d_colptr, colptr, sizeof(int64_t) * (total_m + 1), cudaMemcpyHostToDevice, s));
+    if (total_nnz > 0)
+        OPH_CUDA_TRY(cudaMemcpyAsync(d_rows, rows, sizeof(int32_t) * total_nnz, cudaMemcpyHostToDevice, s));
+    int rc = batch_core(ctx, algo, count, d_off, d_colptr, d_rows, total_m, total_nnz, d_out,
+                        ess ? d_out + total_m : nullptr, info);
+    if (rc) return rc;
+    if (total_m > 0) {
+        OPH_CUDA_TRY(cudaMemcpyAsync(low, d_out, sizeof(int32_t) * total_m, cudaMemcpyDeviceToHost, s));
+        if (ess) OPH_CUDA_TRY(cudaMemcpyAsync(ess, d_out + total_m, sizeof(int32_t) * total_m, cudaMemcpyDeviceToHost, s));
+    }
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    return OPH_OK;
+}
+
+// ----------------------------------------------------------- drop-in path
+static std::mutex g_ctx_mu;
+static oph_context *g_ctx[64];
+
+static oph_context *default_context(int device, int *rc) {
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    if (device < 0 || device >= 64) { *rc = OPH_ERR_BAD_INPUT; return nullptr; }
+    if (!g_ctx[device]) {
+        *rc = oph_context_create(device, &g_ctx[device]);
+        if (*rc) return nullptr;
+    }
+    *rc = OPH_OK;
+    return g_ctx[device];
+}
+
+__attribute__((visibility("default"))) int oph_openph(const char *algstr, const int *h_rows_in, const int *h_cols_in,
+                                                      int m, int col_width, const int *h_low_true, int nnz, int *h_low,
+                                                      int *h_ess, float *err_linf, float *err_lone, float *err_redu,
+                                                      float *err_ess, float *time_track, int *num_iters,
+                                                      int gpu_number) {
+    (void)col_width;  // capacity is adaptive
+    const int algo = oph_algo_from_string(algstr);
+    if (algo < 0) return OPH_ERR_ALGO;
+    if (m < 0 || nnz < 0 || (nnz > 0 && (!h_rows_in || !h_cols_in)) || (m > 0 && !h_low)) return OPH_ERR_BAD_INPUT;
+    // the reference clamps an out-of-range ordinal to 0 (functions.cu:49-56)
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return OPH_ERR_CUDA;
+    }
+    if (gpu_number < 0 || gpu_number >= ndev) gpu_number = 0;
+    int rc = OPH_OK;
+    oph_context *ctx = default_context(gpu_number, &rc);
+    if (!ctx) return rc;
+    OPH_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int64_t mm = m > 0 ? m : 1;
+    int *d_r1 = (int *)ctx_alloc(ctx, S_COO_R, sizeof(int) * (nnz > 0 ? nnz : 1));
+    int *d_c1 = (int *)ctx_alloc(ctx, S_COO_C, sizeof(int) * (nnz > 0 ? nnz : 1));
+    int64_t *d_colptr = (int64_t *)ctx_alloc(ctx, S_COLPTR, sizeof(int64_t) * (m + 1));
+    int32_t *d_rows = (int32_t *)ctx_alloc(ctx, S_ROWS, sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+    int32_t *d_out = (int32_t *)ctx_alloc(ctx, S_ESS, sizeof(int32_t) * 2 * mm);
+    int32_t *d_lt = (int32_t *)ctx_alloc(ctx, S_LOWTRUE, sizeof(int32_t) * 2 * mm);
+    double *d_acc = (double *)ctx_alloc(ctx, S_TRACK, sizeof(double) * 16);
+    if (!d_r1 || !d_c1 || !d_colptr || !d_rows || !d_out || !d_lt || !d_acc) return OPH_ERR_OOM;
+    if (nnz > 0) {
+        OPH_CUDA_TRY(cudaMemcpyAsync(d_r1, h_rows_in, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+        OPH_CUDA_TRY(cudaMemcpyAsync(d_c1, h_cols_in, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
+    }
+    Work w;
+    rc = alloc_work(ctx, w, m);
+    if (rc) return rc;
+    // the status block must be clean before the conversion kernel reports into it
+    OPH_CUDA_TRY(cudaMemsetAsync(w.st, 0, sizeof(DevStatus), s));
+    rc = coo1_to_csc(ctx, d_r1, d_c1, nnz, m, d_colptr, d_rows);
+    if (rc) return rc;
+    DevStatus hs;
+    if ((rc = ctx_sync_status(ctx, w, &hs))) return rc;
+    if (hs.error) return OPH_ERR_BAD_INPUT;
+    w.nnz = nnz;
+    w.colptr = d_colptr;
+    w.rows = d_rows;
+    const bool track = h_low_true && (err_linf || err_lone || err_redu || err_ess);
+    Outputs o;
+    o.low = d_out;
+    o.one_based = 1;
+    o.ess = d_out + mm;
+    oph_info info{};
+    rc = reduce_core(ctx, algo, w, o, &info);
+    if (rc) return rc;
+    if (m > 0) {
+        OPH_CUDA_TRY(cudaMemcpyAsync(h_low, d_out, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+        if (h_ess) OPH_CUDA_TRY(cudaMemcpyAsync(h_ess, d_out + mm, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
+    }
+    double acc[16] = {0};
+    if (track && m > 0) {
+        // progress trackers for the final state (tracker.cu:92-134); low_true
+        // arrives 1-based and is compared 0-based like the reference
+        int32_t *lt0 = d_lt, *esst = d_lt + mm;
+        OPH_CUDA_TRY(cudaMemcpyAsync(lt0, h_low_true, sizeof(int) * m, cudaMemcpyHostToDevice, s));
+        k_shift_down<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, lt0);
+        k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 0);
+        k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 1);
+        OPH_CUDA_TRY(cudaMemsetAsync(d_acc, 0, sizeof(double) * 16, s));
+        k_tracker<<<grid_for(ctx, m), 256, 0, s>>>(w.low, lt0, d_out + mm, esst, m, d_acc);
+        OPH_CUDA_TRY(cudaMemcpyAsync(acc, d_acc, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
+    }
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    const int it = info.num_iters > 0 ? info.num_iters : 1;
+    if (num_iters) *num_iters = it;
+    if (time_track && m >= 1) {
+        time_track[0] = 0.0f;
+        time_track[it - 1 < m ? it - 1 : m] = info.device_ms;
+    }
+    if (track && m > 0) {
+        const int last = it - 1 < m ? it - 1 : m;
+        if (err_lone) err_lone[last] = (float)(acc[0] / acc[4]);
+        if (err_linf) err_linf[last] = (float)(acc[1] / acc[5]);
+        if (err_redu) err_redu[last] = 0.0f;
+        if (err_ess) err_ess[last] = acc[2] == acc[3] ? 1.0f : (float)(acc[3] / acc[2]);
+    }
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) void openph(char *algstr, int *h_rows_in, int *h_cols_in, int m,
+                                                   int col_width, int *h_low_true, int nnz, int *h_low, int *h_ess,
+                                                   float *err_linf, float *err_lone, float *err_redu, float *err_ess,
+                                                   float *time_track, int *num_iters, int gpu_number) {
+    int rc = oph_openph(algstr, h_rows_in, h_cols_in, m, col_width, h_low_true, nnz, h_low, h_ess, err_linf,
+                        err_lone, err_redu, err_ess, time_track, num_iters, gpu_number);
+    if (rc != OPH_OK) {
+        if (rc == OPH_ERR_ALGO) printf("Not recognised");
+        else fprintf(stderr, "openph: %s\n", oph_status_string(rc));
+        if (h_low)
+            for (int i = 0; i < m; i++) h_low[i] = 0;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// Host-side internals shared by the translation units of libopenph_gb300.
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <cuda_runtime.h>
+
+#include "openph.h"
+#include "oph_device.cuh"
+
+#define OPH_CUDA_TRY(expr)                                                                         \
+    do {                                                                                           \
+        cudaError_t _e = (expr);                                                                   \
+        if (_e != cudaSuccess) {                                                                   \
+            fprintf(stderr, "openph_gb300: %s failed: %s (%s:%d)\n", #expr, cudaGetErrorString(_e), \
+                    __FILE__, __LINE__);                                                           \
+            return OPH_ERR_CUDA;                                                                   \
+        }                                                                                          \
+    } while (0)
+
+namespace oph {
+
+// A grow-only device buffer owned by a context.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// Device views of one reduction's working state (single matrix or a
+// block-diagonal batch).  All indices are global column ids; a batch instance
+// b owns columns [inst_off[b], inst_off[b+1]) and its rows are shifted into
+// that range, so the batch is one block-diagonal boundary matrix.
+struct Work {
+    int64_t m = 0, nnz = 0;
+    const int64_t *colptr = nullptr;  // m+1
+    const int32_t *rows = nullptr;    // nnz (global row ids)
+    int32_t *low = nullptr;           // m
+    int8_t *classes = nullptr;        // m: 0 unknown, -1 pivot (negative), 1 cleared (positive)
+    uint8_t *clear = nullptr;         // m: row marked for clearing
+    int8_t *dim = nullptr;            // m: nnz(col) - 1, the reference's "dimension"
+    int32_t *first = nullptr;         // m: first column (in order) holding each low
+    int32_t *left = nullptr;          // m: first column holding each row in the input
+    int32_t *beta = nullptr;          // m
+    int32_t *worklist = nullptr;      // m
+    int32_t *widelist = nullptr;      // m
+    int64_t *seg = nullptr;           // m: segment of each column
+    unsigned long long *rowpiv = nullptr;  // m
+    int32_t *agg = nullptr;           // tiles * MAXC (tile maxima, then exclusive prefixes)
+    int64_t ntiles = 0;
+    int *pool = nullptr;              // column store
+    DevStatus *st = nullptr;
+};
+
+struct Context;
+
+// setup.cu
+int setup_store(Context *ctx, Work &w, bool need_beta);
+int coo1_to_csc(Context *ctx, const int *d_rows1, const int *d_cols1, int64_t nnz, int64_t m, int64_t *d_colptr,
+                int32_t *d_rows0);
+int grow_pool(Context *ctx, Work &w);
+
+// pms.cu
+int run_pms(Context *ctx, Work &w, oph_info *info);
+
+// variants.cu
+int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *info);
+
+// capi.cu
+void *ctx_alloc(Context *ctx, int slot, size_t bytes);
+int ctx_sync_status(Context *ctx, Work &w, DevStatus *out);
+
+struct Context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[8] = {};
+    DevBuf bufs[32];
+    DevStatus *h_status = nullptr;  // pinned mirror
+    int max_sweeps = 0;             // 0 = default
+    int64_t initial_pool_bytes = 0; // 0 = default
+    int64_t budget = 0;
+    int64_t pool_ints = 0;          // current pool capacity
+    float phase2_ms = 0, phase1_ms = 0, setup_ms = 0;
+    int phase2_launches = 0;
+};
+
+// buffer slots of Context::bufs
+enum Slot {
+    S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
+    S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
+    S_NSLOTS
+};
+
+}  // namespace oph

@@ -1,0 +1,189 @@
+"""ORACLE — test infrastructure only.
+
+The checker for the GPU reduction: a C restatement of the reference's CPU
+algorithms (``oracle.c``), a dense NumPy reduction restating the reference's
+own test oracle (src/test/std_test.m:10-31), and a driver for the reference's
+own CPU code compiled from its sources (``_ref/ref_ph``, built where the
+reference checkout exists).  Only tests, the smoke check and the bench's CPU
+baseline leg may import this package; the product path never does.
+
+All functions take a 0-based CSC boundary matrix (``colptr`` int64[m+1],
+``rows`` int32) and return 0-based ``low`` (-1 = zero or cleared column) and
+``ess`` (1 = estimated essential), both int32[m].
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboph_oracle.so"
+REF_BIN = HERE / "_ref" / "ref_ph"
+REFERENCE_SRC = Path("/root/reference/src/cuda")
+
+
+class Stats(C.Structure):
+    _fields_ = [("additions", C.c_int64), ("slots_read", C.c_int64), ("slots_written", C.c_int64),
+                ("max_len", C.c_int64), ("iters", C.c_int64), ("columns_done", C.c_int64),
+                ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def build(force: bool = False) -> None:
+    """Compile the restatement, and the reference's CPU code where it exists."""
+    src = HERE / "oracle.c"
+    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), "liboph_oracle.so"], check=True)
+    if REFERENCE_SRC.exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        L = C.CDLL(str(LIB))
+        i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+        i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+        for name in ("oracle_twist", "oracle_standard", "oracle_ph_row", "oracle_pms"):
+            f = getattr(L, name)
+            f.argtypes = [C.c_int64, i64p, i32p, i32p, i32p, C.POINTER(Stats)]
+            f.restype = C.c_int
+        L.oracle_twist_fixed_p.argtypes = [C.c_int64, i64p, i32p, C.c_int, C.c_int64, C.c_double, i32p, i32p,
+                                           C.POINTER(Stats)]
+        L.oracle_twist_fixed_p.restype = C.c_int
+        L.oracle_transverse.argtypes = [C.c_int64, C.c_int32] + [i32p] * 10
+        L.oracle_setup.argtypes = [C.c_int64, i64p, i32p, i32p, i32p, i32p, i32p, C.POINTER(C.c_int32)]
+        _lib = L
+    return _lib
+
+
+def _run(name, bm):
+    m = bm.m
+    low = np.empty(max(m, 1), np.int32)
+    ess = np.empty(max(m, 1), np.int32)
+    st = Stats()
+    rc = getattr(lib(), name)(m, bm.colptr, bm.rows, low, ess, C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"{name} failed with status {rc}")
+    return low[:m], ess[:m], st.as_dict()
+
+
+def twist(bm):
+    """CPU twist (src/cuda/algorithms/twist/twist.cu:10-87)."""
+    return _run("oracle_twist", bm)
+
+
+def standard(bm):
+    """CPU standard (src/cuda/algorithms/standard/standard.cu:1-57)."""
+    return _run("oracle_standard", bm)
+
+
+def ph_row(bm):
+    """CPU row algorithm (src/cuda/algorithms/ph_row/ph_row.cu:2-121)."""
+    return _run("oracle_ph_row", bm)
+
+
+def pms(bm):
+    """pms sweeps, one thread at a time (src/cuda/algorithms/pms/pms.cu:1-118)."""
+    return _run("oracle_pms", bm)
+
+
+def twist_fixed_p(bm, col_width: int, max_columns: int = 0, max_seconds: float = 0.0):
+    """Twist on the reference's m x p slot layout: the timed CPU baseline."""
+    m = bm.m
+    low = np.empty(max(m, 1), np.int32)
+    ess = np.empty(max(m, 1), np.int32)
+    st = Stats()
+    rc = lib().oracle_twist_fixed_p(m, bm.colptr, bm.rows, col_width, max_columns, max_seconds, low, ess,
+                                    C.byref(st))
+    return rc, low[:m], ess[:m], st.as_dict()
+
+
+def setup(bm):
+    """low, beta, left, dim, complex_dim as the reference's set-up computes them."""
+    m = bm.m
+    arrs = [np.empty(max(m, 1), np.int32) for _ in range(4)]
+    cd = C.c_int32()
+    lib().oracle_setup(m, bm.colptr, bm.rows, *arrs, C.byref(cd))
+    low, beta, left, dim = (a[:m] for a in arrs)
+    return low, beta, left, dim, int(cd.value)
+
+
+def transverse(dim, start, next_, low, arglow, classes, ess, cdim):
+    """One serial Phase I walk (pms_functions.cu:55-85) on copies of the state."""
+    m = len(low)
+    low, arglow, classes, ess = (np.array(a, np.int32) for a in (low, arglow, classes, ess))
+    clear = np.zeros(max(m, 1), np.int32)
+    visited = np.zeros(max(m, 1), np.int32)
+    ceil = np.full(cdim + 1, -1, np.int32)
+    lib().oracle_transverse(m, cdim, np.ascontiguousarray(dim, np.int32), np.ascontiguousarray(start, np.int32),
+                            np.ascontiguousarray(next_, np.int32), low, arglow, classes, clear, visited, ess, ceil)
+    return low, arglow, classes, clear[:m], ess
+
+
+def dense_standard(bm):
+    """Dense Z/2 standard reduction (src/test/std_test.m:10-31), for m <= ~3000.
+
+    Returns 0-based low; zero columns get -1."""
+    m = bm.m
+    R = np.zeros((m, m), np.uint8)
+    for j in range(m):
+        R[bm.column(j), j] = 1
+    low = np.full(m, -1, np.int64)
+    nz = R.any(axis=0)
+    low[nz] = m - 1 - np.argmax(R[::-1, nz], axis=0)
+    for j in range(m):
+        while low[j] >= 0:
+            prev = np.nonzero(low[:j] == low[j])[0]
+            if prev.size == 0:
+                break
+            R[:, j] ^= R[:, prev[0]]
+            col = np.nonzero(R[:, j])[0]
+            low[j] = col[-1] if col.size else -1
+    return low.astype(np.int32)
+
+
+def essential_from_low(low):
+    """ess implied by a reduced low array: unpaired columns are essential."""
+    low = np.asarray(low)
+    ess = np.ones(len(low), np.int32)
+    neg = low >= 0
+    ess[neg] = 0
+    ess[low[neg]] = 0
+    return ess
+
+
+def ref_available() -> bool:
+    return REF_BIN.exists() and os.access(REF_BIN, os.X_OK)
+
+
+def ref_run(bm, alg: str = "twist", col_width: int = 10, timeout: float = 600.0):
+    """Run the reference's own CPU code on bm; None when it overflowed its slots."""
+    with tempfile.TemporaryDirectory() as td:
+        inp, out = Path(td) / "in.csc", Path(td) / "out.bin"
+        bm.save(inp)
+        r = subprocess.run([str(REF_BIN), alg, str(col_width), str(inp), str(out)], capture_output=True,
+                           timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_ph exited {r.returncode}: {r.stderr.decode()}")
+        if not out.exists():
+            return None  # the reference hit its fixed slot limit and exited
+        m = bm.m
+        raw = out.read_bytes()
+        low = np.frombuffer(raw, np.int32, m, 0).copy()
+        ess = np.frombuffer(raw, np.int32, m, 4 * m).copy()
+        iters = int(np.frombuffer(raw, np.int32, 1, 8 * m)[0])
+        secs = float(np.frombuffer(raw, np.float64, 1, 8 * m + 4)[0])
+        return low, ess, iters, secs

@@ -1,0 +1,57 @@
+"""Shared test matrices (small, seeded)."""
+from __future__ import annotations
+
+import numpy as np
+
+from openph_gb300 import complexes as cx
+from openph_gb300.complexes import BoundaryMatrix
+
+
+def triangle():
+    """The filled triangle: v1 v2 v3, e12 e13 e23, t (1-based low 0 0 0 2 3 0 6)."""
+    return BoundaryMatrix.from_columns([[], [], [], [0, 1], [0, 2], [1, 2], [3, 4, 5]])
+
+
+def empty_columns(m=5):
+    return BoundaryMatrix.from_columns([[] for _ in range(m)])
+
+
+def random_complex(n_vertices, p_edge, p_tri, seed):
+    """A random filtered 2-complex (flag-free): random edges, random triangles
+    whose three edges exist, in a random valid filtration order."""
+    rng = np.random.default_rng(seed)
+    V = list(range(n_vertices))
+    edges = [(a, b) for a in V for b in V if a < b and rng.random() < p_edge]
+    es = set(edges)
+    tris = [(a, b, c) for a in V for b in V for c in V if a < b < c and (a, b) in es and (a, c) in es
+            and (b, c) in es and rng.random() < p_tri]
+    # filtration value: random for vertices/edges, then cofaces after faces
+    val = {}
+    for v in V:
+        val[(v,)] = rng.random() * 0.1
+    for e in edges:
+        val[e] = max(val[(e[0],)], val[(e[1],)]) + rng.random()
+    for t in tris:
+        val[t] = max(val[(t[0], t[1])], val[(t[0], t[2])], val[(t[1], t[2])]) + rng.random()
+    simplices = sorted(val, key=lambda s: (val[s], len(s), s))
+    pos = {s: i for i, s in enumerate(simplices)}
+    cols = []
+    for s in simplices:
+        if len(s) == 1:
+            cols.append([])
+        else:
+            cols.append(sorted(pos[f] for f in (tuple(x for x in s if x != y) for y in s)))
+    return BoundaryMatrix.from_columns(cols)
+
+
+def small_cases():
+    out = {
+        "triangle": triangle(),
+        "empty5": empty_columns(5),
+        "rips_cube_12": cx.rips_cube(12, seed=3),
+        "rips_circle_16": cx.rips_mixed(16, seed=7),
+        "lower_star_8x8": cx.lower_star_image(8, 8, seed=4, sigma=1.0),
+    }
+    for s in range(3):
+        out[f"random_{s}"] = random_complex(14, 0.5, 0.6, seed=100 + s)
+    return out

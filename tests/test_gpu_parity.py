@@ -1,0 +1,155 @@
+"""GPU parity: every algorithm, through the C ABI, against the oracle.
+
+The lows of a reduced matrix are unique, so every algorithm must reproduce the
+oracle's low bit for bit; ess must match the reference's per-algorithm
+estimate (see the oracle's restatements)."""
+import numpy as np
+import pytest
+
+import oracle
+from openph_gb300 import complexes as cx
+from openph_gb300.api import ALGORITHMS, OphError, ph
+
+from cases import small_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+
+
+def expected(bm, algo):
+    low, ess, _ = oracle.twist(bm)
+    if algo == "ph_row":
+        _, ess, _ = oracle.ph_row(bm)
+    elif algo == "ph_row_parallel":
+        # the reference's GPU row variant never fills arglow, so its estimate
+        # only clears rows that are some column's low (ph_row_parallel.cu:20-89)
+        ess = np.ones(bm.m, np.int32)
+        ess[low[low >= 0]] = 0
+    return low, ess
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("algo", ALGORITHMS)
+def test_small_cases_all_algorithms(cuda_lib, name, algo):
+    bm = CASES[name]
+    r, c = bm.to_coo1()
+    low, ess, *_ = ph(algo, r, c, bm.m, 3, np.zeros(bm.m, np.int32))
+    want_low, want_ess = expected(bm, algo)
+    np.testing.assert_array_equal(low, want_low + 1)
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+@pytest.mark.parametrize("algo", ALGORITHMS)
+def test_rips_cube_50(cuda_lib, algo):
+    bm = cx.rips_cube(50, seed=1)
+    r, c = bm.to_coo1()
+    low, ess, *_ = ph(algo, r, c, bm.m, 3, np.zeros(bm.m, np.int32))
+    want_low, want_ess = expected(bm, algo)
+    np.testing.assert_array_equal(low, want_low + 1)
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_context_reduce_arglow(ctx):
+    bm = cx.rips_cube(30, seed=9)
+    low, ess, arglow, info = ctx.reduce(bm, "pms", with_arglow=True)
+    want, want_ess, _ = oracle.twist(bm)
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+    want_arg = np.full(bm.m, -1, np.int32)
+    j = np.nonzero(want >= 0)[0]
+    want_arg[want[j]] = j
+    np.testing.assert_array_equal(arglow, want_arg)
+    assert info["sweeps"] >= 1
+
+
+def test_lower_star_64(ctx):
+    bm = cx.lower_star_image(64, 64, seed=11, sigma=4.0)
+    want, want_ess, _ = oracle.twist(bm)
+    for algo in ("pms", "twist", "standard", "ph_row"):
+        low, ess, _ = ctx.reduce(bm, algo)
+        np.testing.assert_array_equal(low, want, err_msg=algo)
+    low, ess, _ = ctx.reduce(bm, "pms")
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_batch_mixed(ctx):
+    mats = [cx.rips_mixed(n, seed=s) for s, n in enumerate([12, 20, 7, 25, 16, 9])]
+    lows, esss, info = ctx.reduce_batch(mats, "pms")
+    for bm, low, ess in zip(mats, lows, esss):
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_batch_equals_alone(ctx):
+    mats = [cx.rips_mixed(n, seed=40 + s) for s, n in enumerate([30, 22, 26])]
+    lows, _, _ = ctx.reduce_batch(mats, "pms")
+    for bm, low in zip(mats, lows):
+        alone, _, _ = ctx.reduce(bm, "pms")
+        np.testing.assert_array_equal(low, alone)
+
+
+def test_regrow_from_tiny_pool(cuda_lib):
+    from openph_gb300.api import Context
+    bm = cx.lower_star_image(48, 48, seed=2, sigma=3.0)
+    want, _, _ = oracle.twist(bm)
+    with Context(0) as c:
+        c.set_limits(initial_pool_bytes=1)  # the packed input only: any growth must regrow
+        for algo in ("pms", "twist", "ph_row"):
+            low, _, info = c.reduce(bm, algo)
+            np.testing.assert_array_equal(low, want, err_msg=algo)
+            assert info["regrows"] >= 1, algo
+
+
+def test_sweep_cap_times_out(cuda_lib):
+    from openph_gb300.api import Context, OPH_ERR_TIMEOUT
+    bm = cx.rips_cube(40, seed=1)
+    with Context(0) as c:
+        c.set_limits(max_sweeps=1)
+        with pytest.raises(OphError) as e:
+            c.reduce(bm, "pms")
+        assert e.value.status == OPH_ERR_TIMEOUT
+        c.set_limits(max_sweeps=0)
+        low, _, _ = c.reduce(bm, "pms")  # the context stays usable
+        np.testing.assert_array_equal(low, oracle.twist(bm)[0])
+
+
+def test_budget_oom(cuda_lib):
+    from openph_gb300.api import Context, OPH_ERR_OOM
+    bm = cx.rips_cube(40, seed=1)
+    with Context(0) as c:
+        c.set_budget(4096)
+        with pytest.raises(OphError) as e:
+            c.reduce(bm, "pms")
+        assert e.value.status == OPH_ERR_OOM
+
+
+@pytest.mark.parametrize("bad", ["row_out_of_range", "unsorted_rows", "cols_decreasing"])
+def test_malformed_input_rejected(cuda_lib, bad):
+    from openph_gb300.api import OPH_ERR_BAD_INPUT
+    bm = cases_triangle = CASES["triangle"]
+    r, c = bm.to_coo1()
+    r, c = r.copy(), c.copy()
+    if bad == "row_out_of_range":
+        r[-1] = bm.m + 1
+    elif bad == "unsorted_rows":
+        r[-1], r[-2] = r[-2], r[-1]
+    else:
+        c[0], c[-1] = c[-1], c[0]
+    with pytest.raises(OphError) as e:
+        ph("pms", r, c, bm.m, 3)
+    assert e.value.status == OPH_ERR_BAD_INPUT
+
+
+def test_unknown_algorithm(cuda_lib):
+    r, c = CASES["triangle"].to_coo1()
+    with pytest.raises(OphError):
+        ph("spectral", r, c, 7, 3)
+
+
+def test_zero_columns(cuda_lib):
+    for algo in ALGORITHMS:
+        low, ess, *_ = ph(algo, np.zeros(0, np.int32), np.zeros(0, np.int32), 4, 3)
+        np.testing.assert_array_equal(low, np.zeros(4, np.int32))
+        np.testing.assert_array_equal(ess, np.ones(4, np.int32))
