@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark: plain pms on one Rips complex of a noisy torus (~5M columns).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one full pms reduction of the complex (set-up, sweeps, outputs).
+``value`` is columns/s with the boundary matrix already resident in HBM;
+``e2e`` is the same metric through the drop-in ``openph()`` C call with host
+(pinned) COO input and host outputs, copies included.  The roofline is the
+Phase II narrow-tier kernel (the additions), timed with CUDA events on the
+library's stream during the timed steps.  ``cpu_baseline`` is the fixed-slot
+port of the reference's CPU twist on a bounded prefix of the same reduction.
+
+``--impl reference`` times the reference's CPU twist (its port; the
+reference's own build needs its source tree) on the host cores, on the same
+matrix and metric.  For N > 1 every rank reduces its own replica (no
+collective on the data path); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {"name": "rips_torus", "points": 400, "target_m": 5_000_000, "seed": 2,
+            "torus": {"R": 2.0, "r": 1.0, "sigma": 0.05}}
+CPU_SAMPLE_SECONDS = 15.0
+REF_STEP_SECONDS = 3.0
+L2_FLUSH_BYTES = 512 << 20
+COL_WIDTH = 80  # slot width factor for the fixed-slot CPU port (p = 240 >= widest column)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws, backend):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def max_over_ranks(x: float, dist, device=None) -> float:
+    """Max of a float over all ranks (identity without a process group)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None:
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+def make_workload():
+    from openph_gb300 import complexes as cx
+    w = WORKLOAD
+    pts = cx.points_torus(w["points"], seed=w["seed"], **w["torus"])
+    thr = cx.rips_threshold(pts, w["target_m"])
+    bm = cx.rips(pts, thr)
+    bm.meta.update(threshold=thr)
+    return bm
+
+
+def algorithmic_bytes(bm, st) -> dict:
+    """Bytes per reduction by the reference's layout: the CSC read once, low
+    written, and for every twist addition |P| + |T| read and |T xor P| written
+    (int32 slots)."""
+    base = 4 * (bm.nnz + bm.m + 1) + 4 * bm.m
+    adds = 4 * (st["slots_read"] + st["slots_written"])
+    return {"total": base + adds, "additions": adds, "twist_additions": st["additions"]}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"oph_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_port_sample(bm, seconds: float):
+    """The fixed-slot twist port on a bounded prefix of the reduction order."""
+    import oracle
+    rc, _, _, st = oracle.twist_fixed_p(bm, COL_WIDTH, max_columns=0, max_seconds=seconds)
+    if rc != 0:
+        raise RuntimeError(f"CPU port failed with status {rc}")
+    return st["columns_done"] / st["seconds"], st
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    bm = make_workload()
+    for _ in range(args.warmup):
+        cpu_port_sample(bm, 0.5)
+    rates, cols, secs = [], 0, 0.0
+    for _ in range(args.steps):
+        r, st = cpu_port_sample(bm, REF_STEP_SECONDS)
+        rates.append(r)
+        cols += st["columns_done"]
+        secs += st["seconds"]
+    value = cols / secs
+    line = {
+        "metric": "cols/s", "value": value, "unit": "cols/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
+        "impl": "reference",
+        "config": {"workload": f"rips_torus_{WORKLOAD['points']}pts_{bm.m}cols", "m": bm.m, "nnz": bm.nnz,
+                   "algorithm": "twist (reference CPU reduction, fixed-slot layout)", "col_width": COL_WIDTH,
+                   "seed": WORKLOAD["seed"]},
+        "cpu_baseline": {"value": value, "unit": "cols/s", "cores": 1, "kind": "port",
+                         "sample": f"first columns of the twist order of the same matrix, {REF_STEP_SECONDS:.0f} s "
+                                   f"per step ({cols} columns over {args.steps} steps); the reference's twist is "
+                                   "single-threaded"},
+        "e2e": {"value": value, "unit": "cols/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_traffic():
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+
+    from openph_gb300 import api
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    dist = init_dist(ws, "nccl")
+    api.lib()
+    bm = make_workload()
+    m, nnz = bm.m, bm.nnz
+
+    # the oracle: full CPU twist in the background (algorithmic bytes and a
+    # bit-exact check of the GPU result at full size); rank 0 only
+    oracle_out = {}
+
+    def oracle_job():
+        import oracle
+        low, ess, st = oracle.twist(bm)
+        oracle_out.update(low=low, ess=ess, st=st)
+
+    th = None
+    if rank == 0:
+        import oracle
+        oracle.build()
+        th = threading.Thread(target=oracle_job, daemon=True)
+        th.start()
+
+    ctx = api.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=device)
+    d_colptr = torch.from_numpy(bm.colptr).to(device)
+    d_rows = torch.from_numpy(bm.rows).to(device)
+    d_low = torch.empty(m, dtype=torch.int32, device=device)
+    d_ess = torch.empty(m, dtype=torch.int32, device=device)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=device)
+    torch.cuda.synchronize()
+
+    def step():
+        return ctx.reduce_device(m, d_colptr.data_ptr(), d_rows.data_ptr(), d_low.data_ptr(), d_ess.data_ptr(),
+                                 None, "pms")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    ctx.set_profile(True)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    narrow_ms, wide_ms, p1_ms, launches, p2_launches, infos = 0.0, 0.0, 0.0, 0, 0, []
+    barrier(dist, device)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.fill_(k)  # evict L2 between steps (512 MB write)
+            torch.cuda.synchronize()
+            ev[k][0].record(stream)
+            infos.append(step())
+            ev[k][1].record(stream)
+            prof = ctx.last_profile()
+            narrow_ms += prof["phase2_narrow_ms"]
+            wide_ms += prof["phase2_wide_ms"]
+            p1_ms += prof["phase1_ms"]
+            launches += prof["kernel_launches"]
+            p2_launches += prof["phase2_launches"]
+        torch.cuda.synchronize()
+    ctx.set_profile(False)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = max_over_ranks(sum(step_ms) / 1e3, dist, device)
+    barrier(dist, device)
+
+    # end to end through the drop-in C call: pinned host COO in, host low/ess out
+    r1, c1 = bm.to_coo1()
+    h_r = torch.from_numpy(r1).pin_memory()
+    h_c = torch.from_numpy(c1).pin_memory()
+    h_low = torch.empty(m, dtype=torch.int32).pin_memory()
+    h_ess = torch.empty(m, dtype=torch.int32).pin_memory()
+    it = np.zeros(1, np.int32)
+    L = api.lib()
+    L.oph_openph.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_void_p, C.c_int]
+
+    def e2e_step():
+        rc = L.oph_openph(b"pms", h_r.data_ptr(), h_c.data_ptr(), m, 0, None, nnz, h_low.data_ptr(),
+                          h_ess.data_ptr(), None, None, None, None, None, it.ctypes.data, local)
+        if rc != 0:
+            raise api.OphError(rc, "openph")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_times = []
+    for k in range(args.steps):
+        flush.fill_(k)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(sum(e2e_times), dist, device)
+
+    if rank != 0:
+        barrier(dist, device)
+        return 0
+
+    th.join()
+    st = oracle_out["st"]
+    low_gpu = d_low.cpu().numpy()
+    parity = bool(np.array_equal(low_gpu, oracle_out["low"]) and np.array_equal(d_ess.cpu().numpy(),
+                                                                               oracle_out["ess"]))
+    parity_e2e = bool(np.array_equal(h_low.numpy(), oracle_out["low"] + 1))
+    cpu_rate, cpu_st = cpu_port_sample(bm, CPU_SAMPLE_SECONDS)
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    peak = peaks.get("hbm_gbs", 6800.0)
+    ab = algorithmic_bytes(bm, st)
+    # dominant kernel: Phase II narrow tier; algorithmic bytes per launch /
+    # mean launch time == addition bytes per reduction / narrow time per reduction
+    per_red_narrow_s = narrow_ms / 1e3 / args.steps
+    achieved = ab["additions"] / per_red_narrow_s / 1e9 if per_red_narrow_s > 0 else None
+    traffic = load_traffic()
+    launches_per_red = p2_launches / args.steps
+    line = {
+        "metric": "cols/s", "value": ws * m * args.steps / total_s, "unit": "cols/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic (seeded generator; replicas on every rank)",
+        "config": {"workload": f"rips_torus_{WORKLOAD['points']}pts_{m}cols", "m": m, "nnz": nnz,
+                   "algorithm": "pms", "seed": WORKLOAD["seed"], "threshold": bm.meta["threshold"],
+                   "l2": "flushed between steps (512 MB write)", "parallelism": f"replicas x{ws}"},
+        "complexes_per_s": ws * args.steps / total_s,
+        "e2e": {"value": ws * m * args.steps / e2e_s, "unit": "cols/s", "h2d_bytes_per_step": 8 * nnz,
+                "d2h_bytes_per_step": 8 * m, "ms_per_step": 1e3 * e2e_s / args.steps, "api": "openph() C ABI"},
+        "roofline": {"bound": "hbm", "kernel": "k_p2_narrow (Phase II additions)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if achieved else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback",
+                     "algorithmic_bytes_per_launch": ab["additions"] / launches_per_red if launches_per_red else None,
+                     "mean_launch_ms": narrow_ms / max(1, p2_launches),
+                     "traffic": (traffic or {}).get("bytes_per_launch"),
+                     "traffic_source": (traffic or {}).get("source")},
+        "phases_ms_per_step": {"phase2_narrow": narrow_ms / args.steps, "phase2_wide_global": wide_ms / args.steps,
+                               "phase1": p1_ms / args.steps},
+        "sweeps": infos[-1]["sweeps"], "device_additions": infos[-1]["additions"],
+        "twist_additions": st["additions"],
+        "cpu_baseline": {"value": cpu_rate, "unit": "cols/s", "cores": 1, "kind": "port",
+                         "sample": f"fixed-slot twist port, first {cpu_st['columns_done']} columns of the twist "
+                                   f"order of the same matrix ({cpu_st['seconds']:.1f} s)"},
+        "parity": {"low_ess_equal_oracle": parity, "e2e_low_equal_oracle": parity_e2e},
+        "clocks": clocks.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        barrier(dist, device)
+    return 0 if (parity and parity_e2e) else 3
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    return run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -142,9 +142,20 @@ int oph_reduce_batch_device(oph_context *ctx, int algo, int32_t count, const int
                             int32_t *d_low, int32_t *d_ess, oph_info *info);
 
 /* ------------------------------------------------------------ diagnostics */
-/* Kernel-level timing of the last reduction on this context: per-kernel
- * cumulative device milliseconds for the pms phases (Phase II first). */
-int oph_last_phase_ms(oph_context *ctx, float *phase2_ms, float *phase1_ms, float *setup_ms, int32_t *phase2_launches);
+typedef struct {
+    float phase2_narrow_ms;   /* Phase II narrow-tier kernel, summed over launches */
+    float phase2_wide_ms;     /* Phase II wide + global tiers                      */
+    float phase1_ms;          /* Phase I kernels                                   */
+    float setup_ms;           /* store set-up, alpha/beta, Phase 0                 */
+    int32_t phase2_launches;  /* narrow-tier launches that did work                */
+    int32_t kernel_launches;  /* every kernel launched by the last reduction       */
+} oph_profile;
+
+/* Turn per-phase CUDA-event timing on or off for later reductions on ctx
+ * (off by default; on adds event records between the phase kernels). */
+int oph_context_set_profile(oph_context *ctx, int on);
+/* Per-phase device times and launch counts of the last reduction on ctx. */
+int oph_last_profile(oph_context *ctx, oph_profile *out);
 
 /* Testing hooks: cap the sweep count (0 = default) and the initial column
  * store size in bytes (0 = default), to exercise the timeout and regrow

@@ -56,7 +56,7 @@ def build_gen(force: bool = False) -> Path:
     src = GEN / "ophgen.c"
     if force or _stale(GENLIB, [src]):
         _run(["gcc", "-O2", "-fPIC", "-shared", "-std=c11", "-ffp-contract=off", "-fvisibility=hidden",
-              "-Wall", "-o", str(GENLIB), str(src), "-lm"])
+              "-Wall", "-pthread", "-o", str(GENLIB), str(src), "-lm"])
     return GENLIB
 
 

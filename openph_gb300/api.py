@@ -40,6 +40,14 @@ class Info(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Profile(C.Structure):
+    _fields_ = [("phase2_narrow_ms", C.c_float), ("phase2_wide_ms", C.c_float), ("phase1_ms", C.c_float),
+                ("setup_ms", C.c_float), ("phase2_launches", C.c_int32), ("kernel_launches", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -79,8 +87,8 @@ def lib():
         L.oph_reduce_batch.argtypes = [vp, C.c_int, C.c_int32, i64, i64, vp, i32, vp, C.POINTER(Info)]
         L.oph_reduce_batch_device.argtypes = [vp, C.c_int, C.c_int32, vp, vp, vp, C.c_int64, C.c_int64, vp, vp,
                                               C.POINTER(Info)]
-        L.oph_last_phase_ms.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
-                                        C.POINTER(C.c_int32)]
+        L.oph_context_set_profile.argtypes = [vp, C.c_int]
+        L.oph_last_profile.argtypes = [vp, C.POINTER(Profile)]
         _lib = L
     return _lib
 
@@ -258,8 +266,10 @@ class Context:
             raise OphError(rc, f"oph_reduce_batch_device({algo!r})")
         return info.as_dict()
 
-    def phase_ms(self):
-        p2, p1, su = C.c_float(), C.c_float(), C.c_float()
-        n = C.c_int32()
-        lib().oph_last_phase_ms(self._h, C.byref(p2), C.byref(p1), C.byref(su), C.byref(n))
-        return {"phase2_ms": p2.value, "phase1_ms": p1.value, "setup_ms": su.value, "phase2_launches": n.value}
+    def set_profile(self, on: bool = True):
+        lib().oph_context_set_profile(self._h, 1 if on else 0)
+
+    def last_profile(self):
+        p = Profile()
+        lib().oph_last_profile(self._h, C.byref(p))
+        return p.as_dict()

@@ -51,6 +51,10 @@ def _lib():
         lib.oph_rips_threshold.restype = C.c_double
         lib.oph_lower_star.argtypes = [fp, C.c_int, C.c_int, C.POINTER(_Complex)]
         lib.oph_complex_free.argtypes = [C.POINTER(_Complex)]
+        lib.oph_rips_mixed_batch.argtypes = [C.c_int, np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS"),
+                                             np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS"), C.c_int,
+                                             np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS"),
+                                             C.POINTER(_Complex)]
         _gen = lib
     return _gen
 
@@ -219,3 +223,37 @@ def rips_mixed(n_points: int, seed: int) -> BoundaryMatrix:
     bm = rips(pts)
     bm.meta.update(workload="rips_mixed", seed=seed)
     return bm
+
+
+def mixed_batch_sizes(count: int, seed: int, lo: int = 20, hi: int = 120):
+    """Point counts ~ U[lo, hi] and per-instance seeds of the batched mix."""
+    rng = np.random.default_rng(seed)
+    n = rng.integers(lo, hi + 1, size=count).astype(np.int32)
+    seeds = (np.arange(count, dtype=np.uint64) * np.uint64(2654435761) + np.uint64(seed) * np.uint64(1000003))
+    return n, seeds
+
+
+def rips_mixed_batch(count: int = 4096, seed: int = 4, threads: int | None = None, lo: int = 20, hi: int = 120):
+    """The batched workload: `count` full 2-skeleton Rips complexes, point
+    counts uniform in [lo, hi], half uniform in the cube and half on a noisy
+    circle (by instance seed parity).  Returns (col_off, colptr, rows_local,
+    n_points, seeds) ready for Context.reduce_batch_packed."""
+    import os
+    n, seeds = mixed_batch_sizes(count, seed, lo, hi)
+    col_off = np.zeros(count + 1, np.int64)
+    cx = _Complex()
+    nt = threads or os.cpu_count() or 1
+    if _lib().oph_rips_mixed_batch(count, n, seeds, nt, col_off, C.byref(cx)) != 0:
+        raise MemoryError("batch generation failed")
+    m, nnz = cx.m, cx.nnz
+    colptr = np.ctypeslib.as_array(cx.colptr, shape=(m + 1,)).copy()
+    rows = np.ctypeslib.as_array(cx.rows, shape=(max(nnz, 1),))[:nnz].copy()
+    _lib().oph_complex_free(C.byref(cx))
+    return col_off, colptr, rows, n, seeds
+
+
+def batch_instance(col_off, colptr, rows, b: int) -> BoundaryMatrix:
+    """Instance b of a packed batch as its own matrix (local rows)."""
+    c0, c1 = int(col_off[b]), int(col_off[b + 1])
+    cp = colptr[c0:c1 + 1] - colptr[c0]
+    return BoundaryMatrix(cp, rows[colptr[c0]:colptr[c1]])

@@ -208,8 +208,17 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
     cudaStream_t s = ctx->stream;
     const int64_t m = w.m;
     const bool pms = algo == OPH_ALGO_PMS;
+    ctx->launches = 0;
+    ctx->prof = oph_profile{};
+    if (ctx->profile) cudaEventRecord(ctx->ev[2], s);
     int rc = setup_store(ctx, w, pms);
     if (rc) return rc;
+    ctx->launches += pms ? 3 : 1;
+    if (ctx->profile) {
+        cudaEventRecord(ctx->ev[3], s);
+        cudaEventSynchronize(ctx->ev[3]);
+        cudaEventElapsedTime(&ctx->prof.setup_ms, ctx->ev[2], ctx->ev[3]);
+    }
     DevStatus hs;
     if ((rc = ctx_sync_status(ctx, w, &hs))) return rc;
     if (hs.error) return OPH_ERR_BAD_INPUT;
@@ -233,8 +242,10 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
         k_finalize1<<<grid_for(ctx, m), 256, 0, s>>>(w.low, m, o.one_based, ess_mode, o.inst_off, o.count, o.low,
                                                      o.ess, o.arglow);
         k_finalize2<<<grid_for(ctx, m), 256, 0, s>>>(w.low, m, o.inst_off, o.count, o.ess, o.arglow);
+        ctx->launches += 2;
         OPH_CUDA_TRY(cudaGetLastError());
     }
+    ctx->prof.kernel_launches = ctx->launches;
     if (info) *info = local;
     return OPH_OK;
 }
@@ -298,6 +309,8 @@ __attribute__((visibility("default"))) int oph_context_destroy(oph_context *ctx)
     for (auto &b : ctx->bufs)
         if (b.ptr) cudaFree(b.ptr);
     for (auto &e : ctx->ev) cudaEventDestroy(e);
+    for (int i = 0; i < ctx->pev_n; i++) cudaEventDestroy(ctx->pev[i]);
+    free(ctx->pev);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -320,13 +333,15 @@ __attribute__((visibility("default"))) int oph_context_set_limits(oph_context *c
     return OPH_OK;
 }
 
-__attribute__((visibility("default"))) int oph_last_phase_ms(oph_context *ctx, float *p2, float *p1, float *setup,
-                                                             int32_t *p2_launches) {
+__attribute__((visibility("default"))) int oph_context_set_profile(oph_context *ctx, int on) {
     if (!ctx) return OPH_ERR_BAD_INPUT;
-    if (p2) *p2 = ctx->phase2_ms;
-    if (p1) *p1 = ctx->phase1_ms;
-    if (setup) *setup = ctx->setup_ms;
-    if (p2_launches) *p2_launches = ctx->phase2_launches;
+    ctx->profile = on ? 1 : 0;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_last_profile(oph_context *ctx, oph_profile *out) {
+    if (!ctx || !out) return OPH_ERR_BAD_INPUT;
+    *out = ctx->prof;
     return OPH_OK;
 }
 

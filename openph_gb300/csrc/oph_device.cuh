@@ -32,6 +32,7 @@ constexpr int PIV_SHIFT = 35;
 constexpr unsigned long long PIV_OFF_MASK = (1ull << PIV_SHIFT) - 1;
 constexpr int FIRST_NONE = 0x7f7f7f7f;  // byte pattern 0x7f: "no column yet"
 constexpr int MAXC = 8;                 // dimension buckets handled by the Phase I scan (-1 .. 6)
+constexpr int POOL_PAD = 1024;          // ints of readable padding past the pool's end
 
 // Device-resident status block of one reduction.
 struct DevStatus {
@@ -129,6 +130,42 @@ __device__ __forceinline__ int merge_xor(const Tile &tile, const int *A, int nA,
     }
     tile.sync();
     return nA + nP - 2 * common;
+}
+
+// The same symmetric difference when the pivot P has at most G entries and is
+// held one element per lane (lane k < nP holds P[k] in `pv`).  Lane k ranks
+// P[k] in A by binary search; every element x of A is then shifted by
+//   sum over k of [P[k] < x] * (P[k] common ? -1 : +1)
+// (the pivot broadcast by shuffles), and dropped if it equals some P[k].
+// No staging of P and no second pass over it.  Returns |A xor P|.
+template <int G, class Tile>
+__device__ __forceinline__ int merge_xor_small(const Tile &tile, const int *A, int nA, int pv, int nP, int *B) {
+    const int lane = tile.thread_rank();
+    const unsigned lt = (1u << lane) - 1u;
+    int r = 0;
+    bool pdup = false;
+    if (lane < nP) {
+        r = lower_bound(A, nA, pv);
+        pdup = r < nA && A[r] == pv;
+    }
+    const unsigned dmask = tile.ballot(pdup);
+    if (lane < nP && !pdup) B[lane + r - 2 * __popc(dmask & lt)] = pv;
+    for (int base = 0; base < nA; base += G) {
+        const int i = base + lane;
+        const bool v = i < nA;
+        const int x = v ? A[i] : 0;
+        int shift = 0;
+        bool drop = false;
+        for (int k = 0; k < nP; k++) {
+            const int pk = tile.shfl(pv, k);
+            const int s = ((dmask >> k) & 1u) ? -1 : 1;
+            shift += pk < x ? s : 0;
+            drop |= pk == x;
+        }
+        if (v && !drop) B[i + shift] = x;
+    }
+    tile.sync();
+    return nA + nP - 2 * __popc(dmask);
 }
 
 // Group copy of n ints; 128-bit moves when both ends are 16-byte aligned.

@@ -79,8 +79,11 @@ struct Context {
     int64_t initial_pool_bytes = 0; // 0 = default
     int64_t budget = 0;
     int64_t pool_ints = 0;          // current pool capacity
-    float phase2_ms = 0, phase1_ms = 0, setup_ms = 0;
-    int phase2_launches = 0;
+    int profile = 0;                // record per-phase events
+    cudaEvent_t *pev = nullptr;     // profiling events (pairs)
+    int pev_n = 0;
+    oph_profile prof{};             // last reduction
+    int launches = 0;               // kernels launched by the current reduction
 };
 
 // buffer slots of Context::bufs

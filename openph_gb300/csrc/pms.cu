@@ -88,7 +88,12 @@ __global__ void k_p1_first(PmsArgs a) {
             if (lj >= 0) a.low[j] = -1;
             lj = -1;
         }
-        if (lj >= 0) atomicMin(&a.first[lj], (int)j);
+        if (lj >= 0) {
+            // a column whose low already has a pivot to its left is a repeat:
+            // the pivot itself records first[low], so only the others race
+            const unsigned long long w = a.rowpiv[lj];
+            if (w == NO_PIVOT || pivot_col(w) >= (int)j) atomicMin(&a.first[lj], (int)j);
+        }
     }
 }
 
@@ -251,7 +256,8 @@ __global__ void k_p1_worklist(PmsArgs a) {
         bool want = false;
         if (j < a.m) {
             int lj = a.low[j];
-            if (lj >= 0) a.first[lj] = FIRST_NONE;
+            // reset first[] for the next sweep: once per row, by its winner
+            if (lj >= 0 && a.first[lj] == (int)j) a.first[lj] = FIRST_NONE;
             if (a.clear[j]) {
                 a.clear[j] = 0;
                 a.classes[j] = 1;
@@ -335,13 +341,86 @@ __device__ void reduce_column(const Tile &tile, const PmsArgs &a, int j, int *A,
     tile.sync();
 }
 
+// Narrow tier: G lanes per column, the column in shared memory (A/B, CAP
+// ints each), the pivot in registers when it has at most G entries (the
+// common case: most pivots are apparent pairs with 3 entries) and read from
+// the store otherwise.  Each addition is two dependent round trips: the pivot
+// word (with left[] alongside) and the pivot's header + rows in one go.
+// Reads up to G ints past a segment's start, which the pool's tail padding
+// keeps in bounds.
+template <int G, class Tile>
+__device__ void reduce_column_narrow(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int cap,
+                                     long long &adds, long long &slots) {
+    const int lane = tile.thread_rank();
+    int lj = a.low[j];
+    unsigned long long w = ld_acquire(&a.rowpiv[lj]);
+    if (w == NO_PIVOT || pivot_col(w) >= j) return;
+    const long long sj = a.seg[j];
+    int n = a.pool[sj];
+    const int capj = a.pool[sj + 1];
+    if (n > cap) {
+        if (lane == 0) a.widelist[atomicAdd(&a.st->wide_count, 1)] = j;
+        return;
+    }
+    group_copy<G>(tile, A, a.pool + sj + SEG_HDR, n);
+    bool made_pivot = false, handed = false;
+    for (;;) {
+        const long long sp = pivot_seg(w);
+        const int np = a.pool[sp];
+        const int pv = a.pool[sp + SEG_HDR + lane];
+        if (n + np > cap) { handed = true; break; }
+        int nn;
+        if (np <= G) nn = merge_xor_small<G>(tile, A, n, pv, np, B);
+        else nn = merge_xor<G>(tile, A, n, a.pool + sp + SEG_HDR, np, B);
+        slots += n + np + nn;
+        adds++;
+        n = nn;
+        int *t = A; A = B; B = t;
+        lj = n ? A[n - 1] : -1;
+        if (lj < 0) break;
+        const int lf = a.left[lj];
+        w = ld_acquire(&a.rowpiv[lj]);
+        if (lane == 0) a.clear[lj] = 1;
+        if (lf == j) { made_pivot = true; break; }
+        if (w == NO_PIVOT || pivot_col(w) >= j) break;
+    }
+    long long dst = sj;
+    int dcap = capj;
+    if (n > capj) {
+        dcap = round4(max(2 * n, 16));
+        long long off = 0;
+        if (lane == 0) off = pool_alloc(a.st, SEG_HDR + dcap);
+        off = tile.shfl(off, 0);
+        if (off < 0) return;  // pool exhausted: j keeps its pre-sweep state
+        dst = off;
+    }
+    group_copy<G>(tile, a.pool + dst + SEG_HDR, A, n);
+    if (lane == 0) {
+        a.pool[dst] = n;
+        a.pool[dst + 1] = dcap;
+        a.seg[j] = dst;
+        a.low[j] = lj;
+    }
+    if (made_pivot) {
+        fence_acq_rel();
+        tile.sync();
+        if (lane == 0) {
+            a.classes[j] = -1;
+            st_release(&a.rowpiv[lj], pack_pivot(j, dst));
+        }
+    } else if (handed) {
+        if (lane == 0) a.widelist[atomicAdd(&a.st->wide_count, 1)] = j;
+    }
+    tile.sync();
+}
+
 template <int G, int CAP>
 __global__ void __launch_bounds__(256) k_p2_narrow(PmsArgs a) {
     if (a.st->converged) return;
     extern __shared__ int smem[];
     auto tile = cg::tiled_partition<G>(cg::this_thread_block());
     const int gid = threadIdx.x / G;
-    int *buf = smem + (size_t)gid * 3 * CAP;
+    int *buf = smem + (size_t)gid * 2 * CAP;
     const int count = a.st->wl_count;
     long long adds = 0, slots = 0;
     for (;;) {
@@ -349,8 +428,7 @@ __global__ void __launch_bounds__(256) k_p2_narrow(PmsArgs a) {
         if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->wl_cursor, 1);
         idx = tile.shfl(idx, 0);
         if (idx >= count) break;
-        reduce_column<G>(tile, a, a.worklist[idx], buf, buf + CAP, buf + 2 * CAP, CAP, a.widelist, &a.st->wide_count,
-                         adds, slots);
+        reduce_column_narrow<G>(tile, a, a.worklist[idx], buf, buf + CAP, CAP, adds, slots);
     }
     if (tile.thread_rank() == 0 && adds) {
         atomicAdd(&a.st->additions, (unsigned long long)adds);
@@ -472,8 +550,14 @@ __global__ void k_count_sweep(DevStatus *st) {
 }
 
 // ------------------------------------------------------------------ driver
-constexpr int NARROW_G = 32;
-constexpr int NARROW_CAP = 256;
+#ifndef OPH_NARROW_G
+#define OPH_NARROW_G 8
+#endif
+#ifndef OPH_NARROW_CAP
+#define OPH_NARROW_CAP 128
+#endif
+constexpr int NARROW_G = OPH_NARROW_G;
+constexpr int NARROW_CAP = OPH_NARROW_CAP;
 constexpr int WIDE_CAP = 8192;
 
 int run_pms(Context *ctx, Work &w, oph_info *info) {
@@ -485,7 +569,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     cudaStream_t s = ctx->stream;
 
     static bool attr_done[64] = {};
-    const size_t narrow_smem = (size_t)(256 / NARROW_G) * 3 * NARROW_CAP * sizeof(int);
+    const size_t narrow_smem = (size_t)(256 / NARROW_G) * 2 * NARROW_CAP * sizeof(int);
     const size_t wide_smem = (size_t)3 * WIDE_CAP * sizeof(int);
     if (!attr_done[ctx->device & 63]) {
         OPH_CUDA_TRY(cudaFuncSetAttribute(k_p2_narrow<NARROW_G, NARROW_CAP>,
@@ -513,34 +597,65 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
 
     cudaEventRecord(ctx->ev[0], s);
     k_phase0<<<grid_m, 256, 0, s>>>(a);
+    ctx->launches++;
     OPH_CUDA_TRY(cudaGetLastError());
+
+    // profiling: 4 events per sweep (before Phase I, before/after the narrow
+    // tier, after the wide and global tiers), reused batch after batch
+    constexpr int MAX_BATCH = 16;
+    if (ctx->profile && ctx->pev_n < 4 * MAX_BATCH + 2) {
+        ctx->pev = (cudaEvent_t *)realloc(ctx->pev, sizeof(cudaEvent_t) * (4 * MAX_BATCH + 2));
+        for (int i = ctx->pev_n; i < 4 * MAX_BATCH + 2; i++) cudaEventCreate(&ctx->pev[i]);
+        ctx->pev_n = 4 * MAX_BATCH + 2;
+    }
+    if (ctx->profile) cudaEventRecord(ctx->pev[4 * MAX_BATCH], s);  // end of Phase 0
 
     const int max_sweeps = ctx->max_sweeps > 0 ? ctx->max_sweeps : 1 << 20;
     int sweeps_launched = 0;
     int batch = 2;
     DevStatus hs{};
     int rc = OPH_OK;
-    float p2_ms = 0, p1_ms = 0;
+    float p2_ms = 0, p2w_ms = 0, p1_ms = 0;
+    int p2_launches = 0;
     int regrows = 0;
     for (;;) {
         const int nb = std::min(batch, max_sweeps - sweeps_launched);
         for (int b = 0; b < nb; b++) {
+            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b], s);
             k_p1_first<<<grid_m, 256, 0, s>>>(a);
             k_p1_tiles<<<grid_t, P1_THREADS, 0, s>>>(a);
             k_p1_scan<<<1, 32 * MAXC, 0, s>>>(a);
             k_p1_mark<<<grid_t, P1_THREADS, 0, s>>>(a);
             k_p1_worklist<<<grid_m, 256, 0, s>>>(a);
+            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b + 1], s);
             k_p2_narrow<NARROW_G, NARROW_CAP><<<grid_narrow, 256, narrow_smem, s>>>(a);
+            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b + 2], s);
             k_reset_global_queue<<<1, 1, 0, s>>>(w.st);
             k_p2_wide<WIDE_CAP><<<grid_wide, 32, wide_smem, s>>>(a);
             k_p2_global<<<ctx->sm_count * 4, 32, 0, s>>>(a);
             k_count_sweep<<<1, 1, 0, s>>>(w.st);
+            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b + 3], s);
+            ctx->launches += 10;
         }
         sweeps_launched += nb;
         OPH_CUDA_TRY(cudaGetLastError());
         OPH_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, w.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
         OPH_CUDA_TRY(cudaStreamSynchronize(s));
         hs = *ctx->h_status;
+        if (ctx->profile) {
+            // sweeps past convergence return at once; count only working ones
+            const int worked = std::max(0, std::min(nb, hs.sweeps - (sweeps_launched - nb)));
+            for (int b = 0; b < nb; b++) {
+                float t1 = 0, t2 = 0, t3 = 0;
+                cudaEventElapsedTime(&t1, ctx->pev[4 * b], ctx->pev[4 * b + 1]);
+                cudaEventElapsedTime(&t2, ctx->pev[4 * b + 1], ctx->pev[4 * b + 2]);
+                cudaEventElapsedTime(&t3, ctx->pev[4 * b + 2], ctx->pev[4 * b + 3]);
+                p1_ms += t1;
+                p2_ms += t2;
+                p2w_ms += t3;
+            }
+            p2_launches += worked;
+        }
         if (hs.error) { rc = OPH_ERR_BAD_INPUT; break; }
         if (hs.overflow) {
             // a column could not be written back: grow the store and run the
@@ -554,16 +669,24 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         }
         if (hs.converged) break;
         if (sweeps_launched >= max_sweeps) { rc = OPH_ERR_TIMEOUT; break; }
-        batch = std::min(batch * 2, 16);
+        batch = std::min(batch * 2, MAX_BATCH);
     }
     cudaEventRecord(ctx->ev[1], s);
     OPH_CUDA_TRY(cudaEventSynchronize(ctx->ev[1]));
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-    (void)p2_ms; (void)p1_ms;
+    if (ctx->profile) {
+        float p0 = 0;
+        cudaEventElapsedTime(&p0, ctx->ev[0], ctx->pev[4 * MAX_BATCH]);
+        ctx->prof.phase2_narrow_ms = p2_ms;
+        ctx->prof.phase2_wide_ms = p2w_ms;
+        ctx->prof.phase1_ms = p1_ms;
+        ctx->prof.setup_ms += p0;
+        ctx->prof.phase2_launches = p2_launches;
+    }
     if (info) {
         info->sweeps = hs.sweeps;
-        info->num_iters = hs.sweeps + 1;
+        info->num_iters = std::max(hs.sweeps, 1) + 1;
         info->additions = (int64_t)hs.additions;
         info->slots_moved = (int64_t)hs.slots;
         info->pool_bytes = (int64_t)hs.pool_used * 4;

@@ -113,7 +113,9 @@ static int64_t initial_pool_ints(Context *ctx, int64_t m, int64_t nnz) {
 int setup_store(Context *ctx, Work &w, bool need_beta) {
     const int64_t m = w.m;
     int64_t pool_ints = initial_pool_ints(ctx, m, w.nnz);
-    w.pool = (int *)ctx_alloc(ctx, S_POOL, sizeof(int) * pool_ints);
+    // tail padding: narrow-tier kernels read up to a group's width past a
+    // segment start
+    w.pool = (int *)ctx_alloc(ctx, S_POOL, sizeof(int) * (pool_ints + POOL_PAD));
     if (!w.pool) return OPH_ERR_OOM;
     ctx->pool_ints = pool_ints;
     const int64_t used = 8 * (m + 1) + 4 * ((w.nnz + 3) / 4) + 64;
@@ -147,7 +149,7 @@ int grow_pool(Context *ctx, Work &w) {
     int64_t want = ctx->pool_ints * 2;
     if (want < used + (16 << 20)) want = used + (16 << 20);
     if (want >= (int64_t)(PIV_OFF_MASK << 2)) return OPH_ERR_OVERFLOW;
-    int *np = (int *)ctx_alloc(ctx, S_POOL2, sizeof(int) * want);
+    int *np = (int *)ctx_alloc(ctx, S_POOL2, sizeof(int) * (want + POOL_PAD));
     if (!np) return OPH_ERR_OOM;
     OPH_CUDA_TRY(cudaMemcpyAsync(np, w.pool, sizeof(int) * used, cudaMemcpyDeviceToDevice, ctx->stream));
     // swap the two pool slots so the larger one becomes the pool

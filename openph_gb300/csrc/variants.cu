@@ -329,6 +329,7 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
         int hstats[2] = {-1, 0};
         OPH_CUDA_TRY(cudaMemcpyAsync(d_stats, hstats, sizeof(hstats), cudaMemcpyHostToDevice, s));
         k_dim_stats<<<grid_m, 256, 0, s>>>(w.dim, m, d_stats);
+        ctx->launches++;
         OPH_CUDA_TRY(cudaMemcpyAsync(hstats, d_stats, sizeof(hstats), cudaMemcpyDeviceToHost, s));
         OPH_CUDA_TRY(cudaMemsetAsync(a.arglow, 0xff, sizeof(int32_t) * m, s));
         OPH_CUDA_TRY(cudaStreamSynchronize(s));
@@ -346,6 +347,7 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
         if (!(a.twist && maxdim < 1)) {
             for (;;) {
                 k_seq_walk<<<1, 32, smem, s>>>(a);
+                ctx->launches++;
                 OPH_CUDA_TRY(cudaGetLastError());
                 OPH_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, w.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
                 OPH_CUDA_TRY(cudaStreamSynchronize(s));
@@ -381,6 +383,7 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
             k_row_buckets<<<grid_m, 256, 0, s>>>(a);
             a.start_pos = m - 1;
             k_row_walk<<<1, ROW_THREADS, smem, s>>>(a);
+            ctx->launches += 2;
             OPH_CUDA_TRY(cudaGetLastError());
             OPH_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, w.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
             OPH_CUDA_TRY(cudaStreamSynchronize(s));

@@ -390,3 +390,99 @@ OPHGEN_API int oph_lower_star(const float *img, int h, int w, oph_complex_t *out
     free(recs); free(fac); free(val); free(dims);
     return rc;
 }
+
+/* ------------------------------------------------------------- batches */
+/* One instance of the mixed batch: n points uniform in [0,1]^3 (even seed) or
+ * on a noisy unit circle in R^3 (odd seed, sigma = 0.05), full 2-skeleton. */
+static int mixed_instance(int n, uint64_t seed, oph_complex_t *out) {
+    double *pts = (double *)malloc(sizeof(double) * 3 * n);
+    if (!pts) return -1;
+    if (seed % 2 == 0) oph_points_cube(n, 3, seed, pts);
+    else oph_points_circle(n, 0.05, seed, pts);
+    int rc = oph_rips(pts, n, 3, INFINITY, out);
+    free(pts);
+    return rc;
+}
+
+#include <pthread.h>
+
+typedef struct {
+    int count, nthreads, tid;
+    const int *npts;
+    const uint64_t *seeds;
+    oph_complex_t *inst;
+    int rc;
+} batch_job_t;
+
+static void *batch_worker(void *p) {
+    batch_job_t *j = (batch_job_t *)p;
+    for (int b = j->tid; b < j->count; b += j->nthreads)
+        if (mixed_instance(j->npts[b], j->seeds[b], &j->inst[b]) != 0) j->rc = -1;
+    return NULL;
+}
+
+typedef struct {
+    int count, nthreads, tid;
+    oph_complex_t *inst;
+    const int64_t *col_off, *nnz_off;
+    int64_t *colptr;
+    int32_t *rows;
+} cat_job_t;
+
+static void *cat_worker(void *p) {
+    cat_job_t *j = (cat_job_t *)p;
+    for (int b = j->tid; b < j->count; b += j->nthreads) {
+        oph_complex_t *c = &j->inst[b];
+        for (int64_t k = 0; k < c->m; k++) j->colptr[j->col_off[b] + k] = j->nnz_off[b] + c->colptr[k];
+        memcpy(j->rows + j->nnz_off[b], c->rows, sizeof(int32_t) * c->nnz);
+        oph_complex_free(c);
+    }
+    return NULL;
+}
+
+/* `count` instances of the mixed batch generated on `nthreads` threads and
+ * concatenated: col_off[count+1] column offsets, out->colptr (global, m+1)
+ * and out->rows holding each instance's LOCAL row ids.  out->value and
+ * out->dim are not filled (NULL). */
+OPHGEN_API int oph_rips_mixed_batch(int count, const int *npts, const uint64_t *seeds, int nthreads,
+                                    int64_t *col_off, oph_complex_t *out) {
+    memset(out, 0, sizeof(*out));
+    if (count <= 0) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    oph_complex_t *inst = (oph_complex_t *)calloc(count, sizeof(oph_complex_t));
+    int64_t *nnz_off = (int64_t *)malloc(sizeof(int64_t) * (count + 1));
+    pthread_t th[256];
+    batch_job_t bj[256];
+    if (!inst || !nnz_off) { free(inst); free(nnz_off); return -1; }
+    for (int t = 0; t < nthreads; t++) {
+        bj[t] = (batch_job_t){count, nthreads, t, npts, seeds, inst, 0};
+        pthread_create(&th[t], NULL, batch_worker, &bj[t]);
+    }
+    int rc = 0;
+    for (int t = 0; t < nthreads; t++) { pthread_join(th[t], NULL); rc |= bj[t].rc; }
+    if (rc) {
+        for (int b = 0; b < count; b++) oph_complex_free(&inst[b]);
+        free(inst); free(nnz_off);
+        return -1;
+    }
+    col_off[0] = 0; nnz_off[0] = 0;
+    for (int b = 0; b < count; b++) { col_off[b + 1] = col_off[b] + inst[b].m; nnz_off[b + 1] = nnz_off[b] + inst[b].nnz; }
+    out->m = col_off[count]; out->nnz = nnz_off[count];
+    out->colptr = (int64_t *)malloc(sizeof(int64_t) * (out->m + 1));
+    out->rows = (int32_t *)malloc(sizeof(int32_t) * (out->nnz ? out->nnz : 1));
+    if (!out->colptr || !out->rows) {
+        for (int b = 0; b < count; b++) oph_complex_free(&inst[b]);
+        free(inst); free(nnz_off); oph_complex_free(out);
+        return -1;
+    }
+    cat_job_t cj[256];
+    for (int t = 0; t < nthreads; t++) {
+        cj[t] = (cat_job_t){count, nthreads, t, inst, col_off, nnz_off, out->colptr, out->rows};
+        pthread_create(&th[t], NULL, cat_worker, &cj[t]);
+    }
+    for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+    out->colptr[out->m] = out->nnz;
+    free(inst); free(nnz_off);
+    return 0;
+}

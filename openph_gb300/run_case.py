@@ -1,0 +1,59 @@
+"""Reduce one generated workload a few times on the GPU (for profiler runs).
+
+    python -m openph_gb300.run_case [--workload rips_torus|lower_star|rips_cube]
+                                    [--target-m M] [--algo pms] [--steps K]
+
+Prints one JSON line with the device time per reduction and the library's
+counters.  The matrix is device-resident before the first reduction.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import numpy as np
+
+
+def make(workload: str, target_m: int, seed: int):
+    from . import complexes as cx
+    if workload == "rips_torus":
+        return cx.rips_torus(400, target_m, seed=seed)
+    if workload == "lower_star":
+        side = int(round((target_m / 6) ** 0.5)) if target_m else 512
+        return cx.lower_star_image(side, side, seed=seed)
+    if workload == "rips_cube":
+        return cx.rips_cube(50, seed=seed)
+    raise SystemExit(f"unknown workload {workload}")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="rips_torus")
+    ap.add_argument("--target-m", type=int, default=1_000_000)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--algo", default="pms")
+    ap.add_argument("--steps", type=int, default=2)
+    args = ap.parse_args()
+
+    import torch
+
+    from . import api
+    bm = make(args.workload, args.target_m, args.seed)
+    dev = torch.device("cuda", 0)
+    ctx = api.Context(0)
+    d_colptr = torch.from_numpy(bm.colptr).to(dev)
+    d_rows = torch.from_numpy(bm.rows).to(dev)
+    d_low = torch.empty(max(bm.m, 1), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(args.steps):
+        out.append(ctx.reduce_device(bm.m, d_colptr.data_ptr(), d_rows.data_ptr(), d_low.data_ptr(), None, None,
+                                     args.algo))
+    print(json.dumps({"workload": args.workload, "m": bm.m, "nnz": bm.nnz, "algo": args.algo,
+                      "device_ms": [o["device_ms"] for o in out], "sweeps": out[-1]["sweeps"],
+                      "additions": out[-1]["additions"], "pivots": int((d_low.cpu().numpy() >= 0).sum())}))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
