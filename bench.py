@@ -250,6 +250,7 @@ def run_ours(args, ws, rank, local):
     ctx.set_profile(True)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     narrow_ms, wide_ms, p1_ms, launches, p2_launches, infos = 0.0, 0.0, 0.0, 0, 0, []
+    tier0_slots = 0
     barrier(dist, device)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
@@ -265,6 +266,7 @@ def run_ours(args, ws, rank, local):
             p1_ms += prof["phase1_ms"]
             launches += prof["kernel_launches"]
             p2_launches += prof["phase2_launches"]
+            tier0_slots += prof["tier_slots"][0]
         torch.cuda.synchronize()
     ctx.set_profile(False)
     step_ms = [a.elapsed_time(b) for a, b in ev]
@@ -318,10 +320,13 @@ def run_ours(args, ws, rank, local):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     ab = algorithmic_bytes(bm, st)
-    # dominant kernel: Phase II narrow tier; algorithmic bytes per launch /
-    # mean launch time == addition bytes per reduction / narrow time per reduction
+    # dominant kernel: Phase II tier 0.  Its algorithmic bytes are the
+    # per-addition figure 4 (|P| + |T| + |T xor P|) summed over the additions
+    # it performed (counted on the device), per launch; divided by its mean
+    # launch time (CUDA events around each launch on the library's stream)
     per_red_narrow_s = narrow_ms / 1e3 / args.steps
-    achieved = ab["additions"] / per_red_narrow_s / 1e9 if per_red_narrow_s > 0 else None
+    t0_bytes = 4 * tier0_slots / args.steps
+    achieved = t0_bytes / per_red_narrow_s / 1e9 if per_red_narrow_s > 0 else None
     traffic = load_traffic()
     launches_per_red = p2_launches / args.steps
     line = {
@@ -335,11 +340,12 @@ def run_ours(args, ws, rank, local):
         "complexes_per_s": ws * args.steps / total_s,
         "e2e": {"value": ws * m * args.steps / e2e_s, "unit": "cols/s", "h2d_bytes_per_step": 8 * nnz,
                 "d2h_bytes_per_step": 8 * m, "ms_per_step": 1e3 * e2e_s / args.steps, "api": "openph() C ABI"},
-        "roofline": {"bound": "hbm", "kernel": "k_p2_narrow (Phase II additions)",
+        "roofline": {"bound": "hbm", "kernel": "k_p2_tier<8,128,256> (Phase II tier 0: column additions)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback",
-                     "algorithmic_bytes_per_launch": ab["additions"] / launches_per_red if launches_per_red else None,
+                     "algorithmic_bytes_per_launch": t0_bytes / launches_per_red if launches_per_red else None,
+                     "algorithmic_bytes_per_reduction_all_tiers_twist": ab["additions"],
                      "mean_launch_ms": narrow_ms / max(1, p2_launches),
                      "traffic": (traffic or {}).get("bytes_per_launch"),
                      "traffic_source": (traffic or {}).get("source")},
@@ -361,16 +367,263 @@ def run_ours(args, ws, rank, local):
     return 0 if (parity and parity_e2e) else 3
 
 
+BATCH = {"count": 4096, "seed": 4, "lo": 20, "hi": 120}
+
+
+def run_batch(args, ws, rank, local):
+    """The batched workload: 4096 Rips complexes (n ~ U[20,120], half cube,
+    half noisy circle) reduced in one segmented pass, against plain pms one
+    complex at a time on the same GPU.  Bit-exactness: every instance of the
+    batched result equals the one-at-a-time result, and a seeded sample of
+    instances equals the oracle."""
+    import torch
+
+    import oracle
+    from openph_gb300 import api
+    from openph_gb300 import complexes as cx
+
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    dist = init_dist(ws, "nccl")
+    t0 = time.perf_counter()
+    col_off, colptr, rows, npts, seeds = cx.rips_mixed_batch(args.count or BATCH["count"], BATCH["seed"],
+                                                             lo=BATCH["lo"], hi=BATCH["hi"])
+    gen_s = time.perf_counter() - t0
+    count = len(col_off) - 1
+    total_m, total_nnz = int(col_off[-1]), int(colptr[-1])
+    ctx = api.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=device)
+    d_off = torch.from_numpy(col_off).to(device)
+    d_colptr = torch.from_numpy(colptr).to(device)
+    d_rows = torch.from_numpy(rows).to(device)
+    d_low = torch.empty(total_m, dtype=torch.int32, device=device)
+    torch.cuda.synchronize()
+
+    def batched():
+        return ctx.reduce_batch_device(count, d_off.data_ptr(), d_colptr.data_ptr(), d_rows.data_ptr(), total_m,
+                                       total_nnz, d_low.data_ptr(), None, "pms")
+
+    for _ in range(args.warmup):
+        batched()
+    ctx.set_profile(True)
+    launches = 0
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(dist, device)
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            torch.cuda.synchronize()
+            ev[k][0].record(stream)
+            info = batched()
+            ev[k][1].record(stream)
+            launches += ctx.last_profile()["kernel_launches"]
+        torch.cuda.synchronize()
+    ctx.set_profile(False)
+    batch_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / 1e3, dist, device)
+    low_batch = d_low.cpu().numpy()
+
+    # plain pms, one complex at a time, device-resident inputs
+    d_low1 = torch.empty(int(np.diff(col_off).max()), dtype=torch.int32, device=device)
+    colptr_d = [None] * count
+    for b in range(count):
+        c0, c1 = int(col_off[b]), int(col_off[b + 1])
+        colptr_d[b] = torch.from_numpy(colptr[c0:c1 + 1] - colptr[c0]).to(device)
+    rows_d = [d_rows[int(colptr[col_off[b]]):int(colptr[col_off[b + 1]])] for b in range(count)]
+    for b in range(min(count, 8)):
+        ctx.reduce_device(int(col_off[b + 1] - col_off[b]), colptr_d[b].data_ptr(), rows_d[b].data_ptr(),
+                          d_low1.data_ptr(), None, None, "pms")
+    torch.cuda.synchronize()
+    mismatches = 0
+    seq_ms = 0.0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for b in range(count):
+        mb = int(col_off[b + 1] - col_off[b])
+        e0.record(stream)
+        ctx.reduce_device(mb, colptr_d[b].data_ptr(), rows_d[b].data_ptr(), d_low1.data_ptr(), None, None, "pms")
+        e1.record(stream)
+        e1.synchronize()
+        seq_ms += e0.elapsed_time(e1)
+        if not np.array_equal(d_low1[:mb].cpu().numpy(), low_batch[col_off[b]:col_off[b + 1]]):
+            mismatches += 1
+    seq_s = max_over_ranks(seq_ms / 1e3, dist, device)
+
+    # oracle on a seeded sample of instances
+    rng = np.random.default_rng(7)
+    sample = sorted(rng.choice(count, size=min(count, 24), replace=False).tolist())
+    oracle_ok = True
+    for b in sample:
+        bm = cx.batch_instance(col_off, colptr, rows, b)
+        want, _, _ = oracle.twist(bm)
+        oracle_ok &= bool(np.array_equal(want, low_batch[col_off[b]:col_off[b + 1]]))
+    if rank == 0:
+        line = {
+            "metric": "complexes/s", "value": ws * count * args.steps / batch_s, "unit": "complexes/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * batch_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": f"rips_mixed_batch_{count}", "total_m": total_m, "total_nnz": total_nnz,
+                       "points": [BATCH["lo"], BATCH["hi"]], "seed": BATCH["seed"], "algorithm": "pms",
+                       "l2": "inputs (%.1f GB) larger than L2" % ((total_nnz * 4 + total_m * 8) / 1e9)},
+            "plain_sequential": {"complexes_per_s": count / seq_s, "s_total": seq_s},
+            "batched_over_plain": (count * args.steps / batch_s) / (count / seq_s),
+            "cols_per_s": ws * total_m * args.steps / batch_s,
+            "sweeps": info["sweeps"], "device_additions": info["additions"], "regrows": info["regrows"],
+            "pool_bytes": info["pool_bytes"],
+            "parity": {"batched_equals_one_at_a_time": mismatches == 0, "mismatched_instances": mismatches,
+                       "oracle_sample": len(sample), "oracle_sample_equal": oracle_ok},
+            "generation_s": gen_s, "clocks": clocks.summary(), "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    return 0 if (mismatches == 0 and oracle_ok) else 3
+
+
+SERVE = {"requests": 160, "m_lo": 1_000, "m_hi": 2_000_000, "seed": 5, "budget_bytes": 150 * (1 << 30),
+         "rates_x_plain": [0.5, 1, 2, 4, 8, 16, 32]}
+
+
+def _serve_request(args):
+    """One request of the serving stream: (kind, target m, seed) -> CSC."""
+    kind, m, seed = args
+    from openph_gb300 import complexes as cx
+    if kind == "rips_cube":
+        n = max(4, int(round((6 * m) ** (1 / 3))))
+        bm = cx.rips_cube(n, seed=seed)
+    elif kind == "rips_torus":
+        bm = cx.rips_torus(400, m, seed=seed)
+    else:
+        side = max(4, int(round((m / 6) ** 0.5)))
+        bm = cx.lower_star_image(side, side, seed=seed)
+    return kind, bm.colptr, bm.rows
+
+
+def serve_stream(count, seed):
+    """Request mix: sizes log-uniform in [m_lo, m_hi], kind uniform over the
+    three generator families, fresh seeds; generated on all host cores."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    rng = np.random.default_rng(seed)
+    ms = np.exp(rng.uniform(np.log(SERVE["m_lo"]), np.log(SERVE["m_hi"]), size=count)).astype(np.int64)
+    kinds = rng.choice(["rips_cube", "rips_torus", "lower_star"], size=count)
+    seeds = rng.integers(1 << 30, size=count)
+    jobs = [(str(k), int(m), int(sd)) for k, m, sd in zip(kinds, ms, seeds)]
+    with cf.ProcessPoolExecutor(max_workers=os.cpu_count(), mp_context=mp.get_context("spawn")) as ex:
+        out = list(ex.map(_serve_request, jobs, chunksize=1))
+    from openph_gb300.complexes import BoundaryMatrix
+    return [(k, BoundaryMatrix(cp, rw)) for k, cp, rw in out]
+
+
+def run_serve(args, ws, rank, local):
+    """Serving: a Poisson stream of reduction requests through the
+    continuous-batching server (HBM budget 150 GB), rates swept to
+    saturation; against plain pms one request at a time on the same GPU
+    (host CSC in, host lows out, like the server)."""
+    reqs = serve_stream(args.count or SERVE["requests"], SERVE["seed"])  # before any CUDA use
+    import torch
+
+    import oracle
+    from openph_gb300 import api
+    torch.cuda.set_device(local)
+    n = len(reqs)
+    total_m = sum(bm.m for _, bm in reqs)
+    # plain: one at a time, service time of each
+    ctx = api.Context(local)
+    for _, bm in reqs[:3]:
+        ctx.reduce(bm, "pms")
+    service, plain_low = [], []
+    for _, bm in reqs:
+        t0 = time.perf_counter()
+        low, _, _ = ctx.reduce(bm, "pms")
+        service.append(time.perf_counter() - t0)
+        plain_low.append(low)
+    ctx.close()
+    service = np.array(service)
+    plain_rate = n / service.sum()
+
+    srv = api.Server(local, budget_bytes=SERVE["budget_bytes"], max_active=4096)
+    for _, bm in reqs[:3]:  # warm-up
+        srv.wait(srv.submit(bm))
+    rng = np.random.default_rng(SERVE["seed"] + 1)
+    results, mism = [], 0
+    for x in SERVE["rates_x_plain"]:
+        rate = x * plain_rate
+        gaps = rng.exponential(1.0 / rate, size=n)
+        arrivals = np.cumsum(gaps)
+        tickets = [None] * n
+        t_start = time.perf_counter()
+
+        def producer():
+            for k, (_, bm) in enumerate(reqs):
+                delay = arrivals[k] - (time.perf_counter() - t_start)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets[k] = srv.submit(bm)
+
+        th = threading.Thread(target=producer)
+        th.start()
+        lat, done_ms, sub_ms = [], [], []
+        for k in range(n):
+            while tickets[k] is None:
+                time.sleep(0.0002)
+            low, _, info = srv.wait(tickets[k])
+            lat.append(info["latency_ms"])
+            done_ms.append(info["done_ms"])
+            sub_ms.append(info["submit_ms"])
+            if not np.array_equal(low, plain_low[k]):
+                mism += 1
+        th.join()
+        span_s = (max(done_ms) - min(sub_ms)) / 1e3
+        # plain pms at the same arrivals: a FIFO single server with the
+        # measured service times
+        fin, plat = 0.0, []
+        for k in range(n):
+            fin = max(fin, arrivals[k]) + service[k]
+            plat.append(1e3 * (fin - arrivals[k]))
+        results.append({"offered_per_s": rate, "served_per_s": n / span_s,
+                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                        "plain_p50_ms": float(np.percentile(plat, 50)), "plain_p99_ms": float(np.percentile(plat, 99)),
+                        "plain_served_per_s": n / max(fin, arrivals[-1])})
+    counters = srv.stats()
+    srv.close()
+    # oracle on the smallest requests (the rest are checked against plain pms)
+    order = np.argsort([bm.m for _, bm in reqs])[:16]
+    oracle_ok = all(np.array_equal(oracle.twist(reqs[i][1])[0], plain_low[i]) for i in order)
+    best = max(results, key=lambda r: r["served_per_s"])
+    line = {
+        "metric": "complexes/s", "value": best["served_per_s"], "unit": "complexes/s", "n_gpus": ws,
+        "steps": len(results), "warmup": 3, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators, fresh seeds per request)",
+        "config": {"workload": "serving_poisson_stream", "requests": n, "total_m": total_m,
+                   "m_range": [SERVE["m_lo"], SERVE["m_hi"]], "budget_gb": SERVE["budget_bytes"] / (1 << 30),
+                   "kinds": sorted({k for k, _ in reqs})},
+        "plain_sequential": {"complexes_per_s": plain_rate, "mean_service_ms": 1e3 * service.mean()},
+        "served_over_plain_at_saturation": best["served_per_s"] / plain_rate,
+        "p50_ms_at_saturation": best["p50_ms"], "p99_ms_at_saturation": best["p99_ms"],
+        "rate_sweep": results, "server": counters,
+        "parity": {"served_equals_plain": mism == 0, "mismatches": mism, "oracle_checked_smallest": len(order),
+                   "oracle_equal": bool(oracle_ok)},
+    }
+    print(json.dumps(line), flush=True)
+    return 0 if (mism == 0 and oracle_ok) else 3
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["torus", "batch", "serve"], default="torus",
+                    help="torus: the ~5M-column complex (the headline); batch: 4096 complexes in one pass; "
+                         "serve: a Poisson request stream through the continuous-batching server")
+    ap.add_argument("--count", type=int, default=0, help="batch/serve: number of complexes / requests")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.workload == "batch":
+        return run_batch(args, ws, rank, local)
+    if args.workload == "serve":
+        return run_serve(args, ws, rank, local)
     return run_ours(args, ws, rank, local)
 
 

@@ -141,6 +141,45 @@ int oph_reduce_batch_device(oph_context *ctx, int algo, int32_t count, const int
                             const int64_t *d_colptr, const int32_t *d_rows, int64_t total_m, int64_t total_nnz,
                             int32_t *d_low, int32_t *d_ess, oph_info *info);
 
+/* ---------------------------------------------------------------- serving */
+/*
+ * A reduction server with continuous batching: requests are reduced by a
+ * worker thread that advances every admitted request with each pms sweep over
+ * one block-diagonal column space, admits queued requests between sweeps
+ * while they fit in the device arena (budget_bytes of HBM, allocated up
+ * front), and releases each request as soon as it has converged.  At most
+ * max_active requests are on the device at once.  Results are identical to
+ * a single-matrix pms reduction of the same matrix.
+ */
+typedef struct oph_server oph_server;
+
+typedef struct {
+    double latency_ms;   /* submit -> result on the host          */
+    double queue_ms;     /* submit -> admitted to the device        */
+    double submit_ms;    /* host monotonic clock at submit (ms)     */
+    double done_ms;      /* host monotonic clock at completion (ms) */
+    int32_t sweeps;      /* sweeps the request took part in         */
+    int32_t status;      /* OPH_OK or the failure                   */
+    int64_t m;
+} oph_request_info;
+
+typedef struct {
+    int64_t completed, pending, active, sweeps, regrows;
+    int64_t pool_bytes_in_use, columns_in_use, arena_bytes;
+} oph_server_counters;
+
+int oph_server_create(int device, int64_t budget_bytes, int32_t max_active, oph_server **out);
+/* Queue a 0-based CSC matrix (copied); returns a ticket.  OPH_ERR_OOM if it
+ * can never fit the arena, OPH_ERR_BAD_INPUT if malformed. */
+int oph_server_submit(oph_server *srv, int64_t m, const int64_t *colptr, const int32_t *rows, int64_t *ticket);
+/* Wait for a ticket (timeout_ms < 0: forever); copies low/ess (0-based,
+ * -1 = none; either may be NULL) and frees the ticket. */
+int oph_server_wait(oph_server *srv, int64_t ticket, int32_t *low, int32_t *ess, oph_request_info *info,
+                    int64_t timeout_ms);
+int oph_server_stats(oph_server *srv, oph_server_counters *out);
+/* Finishes the queued requests, stops the worker, frees the arena. */
+int oph_server_destroy(oph_server *srv);
+
 /* ------------------------------------------------------------ diagnostics */
 typedef struct {
     float phase2_narrow_ms;   /* Phase II narrow-tier kernel, summed over launches */
@@ -149,6 +188,8 @@ typedef struct {
     float setup_ms;           /* store set-up, alpha/beta, Phase 0                 */
     int32_t phase2_launches;  /* narrow-tier launches that did work                */
     int32_t kernel_launches;  /* every kernel launched by the last reduction       */
+    int64_t tier_additions[4];/* column additions done by each Phase II tier       */
+    int64_t tier_slots[4];    /* sum of |P| + |T| + |T xor P| per tier             */
 } oph_profile;
 
 /* Turn per-phase CUDA-event timing on or off for later reductions on ctx

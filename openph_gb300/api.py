@@ -40,12 +40,32 @@ class Info(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-class Profile(C.Structure):
-    _fields_ = [("phase2_narrow_ms", C.c_float), ("phase2_wide_ms", C.c_float), ("phase1_ms", C.c_float),
-                ("setup_ms", C.c_float), ("phase2_launches", C.c_int32), ("kernel_launches", C.c_int32)]
+class RequestInfo(C.Structure):
+    _fields_ = [("latency_ms", C.c_double), ("queue_ms", C.c_double), ("submit_ms", C.c_double),
+                ("done_ms", C.c_double), ("sweeps", C.c_int32), ("status", C.c_int32), ("m", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerCounters(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("completed", "pending", "active", "sweeps", "regrows", "pool_bytes_in_use",
+                                         "columns_in_use", "arena_bytes")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Profile(C.Structure):
+    _fields_ = [("phase2_narrow_ms", C.c_float), ("phase2_wide_ms", C.c_float), ("phase1_ms", C.c_float),
+                ("setup_ms", C.c_float), ("phase2_launches", C.c_int32), ("kernel_launches", C.c_int32),
+                ("tier_additions", C.c_int64 * 4), ("tier_slots", C.c_int64 * 4)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["tier_additions"] = list(self.tier_additions)
+        d["tier_slots"] = list(self.tier_slots)
+        return d
 
 
 _lib = None
@@ -87,6 +107,11 @@ def lib():
         L.oph_reduce_batch.argtypes = [vp, C.c_int, C.c_int32, i64, i64, vp, i32, vp, C.POINTER(Info)]
         L.oph_reduce_batch_device.argtypes = [vp, C.c_int, C.c_int32, vp, vp, vp, C.c_int64, C.c_int64, vp, vp,
                                               C.POINTER(Info)]
+        L.oph_server_create.argtypes = [C.c_int, C.c_int64, C.c_int32, C.POINTER(vp)]
+        L.oph_server_submit.argtypes = [vp, C.c_int64, i64, vp, C.POINTER(C.c_int64)]
+        L.oph_server_wait.argtypes = [vp, C.c_int64, vp, vp, C.POINTER(RequestInfo), C.c_int64]
+        L.oph_server_stats.argtypes = [vp, C.POINTER(ServerCounters)]
+        L.oph_server_destroy.argtypes = [vp]
         L.oph_context_set_profile.argtypes = [vp, C.c_int]
         L.oph_last_profile.argtypes = [vp, C.POINTER(Profile)]
         _lib = L
@@ -273,3 +298,58 @@ class Context:
         p = Profile()
         lib().oph_last_profile(self._h, C.byref(p))
         return p.as_dict()
+
+
+class Server:
+    """Continuous-batching reduction server (one worker thread per server).
+
+    ``submit(bm)`` queues a matrix and returns a ticket; ``wait(ticket)``
+    returns (low, ess, info).  Requests are admitted between pms sweeps while
+    they fit in the device arena of ``budget_bytes``."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 8 << 30, max_active: int = 4096):
+        self._h = C.c_void_p()
+        rc = lib().oph_server_create(device, int(budget_bytes), int(max_active), C.byref(self._h))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_server_create")
+        self._m = {}
+
+    def submit(self, bm) -> int:
+        t = C.c_int64()
+        rc = lib().oph_server_submit(self._h, bm.m, bm.colptr, _ptr(bm.rows if bm.nnz else None), C.byref(t))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_server_submit")
+        self._m[t.value] = bm.m
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        m = self._m.pop(ticket)
+        low = np.empty(max(m, 1), np.int32)
+        ess = np.empty(max(m, 1), np.int32)
+        info = RequestInfo()
+        rc = lib().oph_server_wait(self._h, ticket, _ptr(low), _ptr(ess), C.byref(info), int(timeout_ms))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_server_wait")
+        return low[:m], ess[:m], info.as_dict()
+
+    def stats(self):
+        c = ServerCounters()
+        lib().oph_server_stats(self._h, C.byref(c))
+        return c.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().oph_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -179,17 +179,16 @@ static int alloc_work(Context *ctx, Work &w, int64_t m) {
     w.clear = (uint8_t *)ctx_alloc(ctx, S_CLEAR, mm);
     w.dim = (int8_t *)ctx_alloc(ctx, S_DIM, mm);
     w.first = (int32_t *)ctx_alloc(ctx, S_FIRST, sizeof(int32_t) * mm);
-    w.left = (int32_t *)ctx_alloc(ctx, S_LEFT, sizeof(int32_t) * mm);
     w.beta = (int32_t *)ctx_alloc(ctx, S_BETA, sizeof(int32_t) * mm);
     w.worklist = (int32_t *)ctx_alloc(ctx, S_WORK, sizeof(int32_t) * mm);
     w.widelist = (int32_t *)ctx_alloc(ctx, S_WIDE, sizeof(int32_t) * mm);
     w.seg = (int64_t *)ctx_alloc(ctx, S_SEG, sizeof(int64_t) * mm);
-    w.rowpiv = (unsigned long long *)ctx_alloc(ctx, S_ROWPIV, sizeof(unsigned long long) * mm);
+    w.rec = (PivRec *)ctx_alloc(ctx, S_ROWPIV, sizeof(PivRec) * mm);
     w.ntiles = (m + 2047) / 2048;
     w.agg = (int32_t *)ctx_alloc(ctx, S_AGG, sizeof(int32_t) * MAXC * (w.ntiles + 1) + 64);
     w.st = (DevStatus *)ctx_alloc(ctx, S_STATUS, sizeof(DevStatus));
-    if (!w.low || !w.classes || !w.clear || !w.dim || !w.first || !w.left || !w.beta || !w.worklist ||
-        !w.widelist || !w.seg || !w.rowpiv || !w.agg || !w.st)
+    if (!w.low || !w.classes || !w.clear || !w.dim || !w.first || !w.beta || !w.worklist || !w.widelist ||
+        !w.seg || !w.rec || !w.agg || !w.st)
         return OPH_ERR_OOM;
     return OPH_OK;
 }

@@ -11,12 +11,20 @@
 // replaces the reference's fixed m x p slot store (src/cuda/openph.cu:41-90,
 // src/cuda/kernels.cu:25-38): no slot count is supplied.
 //
-// Pivot table.  rowpiv[i] publishes the column whose (final) low is row i,
-// packed with that column's segment so a reader reaches the pivot's rows in
-// one dependent load: (col << 35) | (segment >> 2).  ~0 = no pivot.  It is
-// written with release semantics after the column's rows are in place and
-// read with acquire semantics (the reference's arglow[] has neither,
-// src/cuda/algorithms/pms/pms_functions.cu:87-112).
+// Pivot records.  rec[i] (32 bytes, one L2 sector) describes row i:
+//   col   the column whose final low is row i (the reference's arglow[i],
+//         src/cuda/algorithms/pms/pms_functions.cu:87-112), -1 = none yet
+//   np    that column's length, seg4 its segment / 4
+//   e[4]  its first four rows
+//   left  the first input column holding row i (beta.cu:2-15)
+// so one 32-byte read per column addition yields the beta check, the pivot
+// test and, for a pivot of at most four entries (most pivots are apparent
+// pairs of three), the pivot's rows too: one dependent round trip per
+// addition instead of three.  Every field changes at most once per
+// reduction, from a marker (col -1, np 0, e -1) to its final value; the
+// publisher writes col last behind a fence.  A reader that sees col set but
+// any needed field still at its marker falls back to an acquire load of col
+// and re-reads the fields and the segment.
 #pragma once
 #include <cooperative_groups.h>
 #include <cstdint>
@@ -27,9 +35,7 @@ namespace cg = cooperative_groups;
 namespace oph {
 
 constexpr int SEG_HDR = 4;
-constexpr unsigned long long NO_PIVOT = ~0ull;
-constexpr int PIV_SHIFT = 35;
-constexpr unsigned long long PIV_OFF_MASK = (1ull << PIV_SHIFT) - 1;
+constexpr long long MAX_POOL_INTS = 4ll << 32;  // segment / 4 is held in 32 bits
 constexpr int FIRST_NONE = 0x7f7f7f7f;  // byte pattern 0x7f: "no column yet"
 constexpr int MAXC = 8;                 // dimension buckets handled by the Phase I scan (-1 .. 6)
 constexpr int POOL_PAD = 1024;          // ints of readable padding past the pool's end
@@ -44,32 +50,74 @@ struct DevStatus {
     int error;                     // malformed input (1) or internal error
     int converged;                 // pms: no repeated low left
     int sweeps;                    // pms sweeps run
-    int wl_count;                  // Phase II worklist size
-    int wl_cursor;                 // Phase II work-queue cursor
-    int wide_count;                // columns handed to the wide path
-    int wide_cursor;
+    int wl_count;                  // Phase II worklist size (tier 0 input)
+    int wl_cursor;                 // unused (tier cursors below)
+    int wide_count;                // unused
+    int wide_cursor;               // unused
+    int t_count[4];                // Phase II tier queues: columns queued per tier
+    int t_cursor[4];               //   and the work-queue cursor of each tier
     int reps;                      // repeated lows seen by the last Phase I
     int resume_dim;                // sequential walkers: where to resume after a regrow
     long long resume_pos;          //   (column or row index; -1 = finished)
     int max_dim;                   // largest nnz(col) - 1 seen by the set-up
     int pad;
+    unsigned long long tier_adds[4];   // additions performed by each Phase II tier
+    unsigned long long tier_slots[4];  // |P| + |T| + |T xor P| summed per tier
 };
 
-__device__ __forceinline__ unsigned long long pack_pivot(int col, long long seg) {
-    return ((unsigned long long)col << PIV_SHIFT) | ((unsigned long long)seg >> 2);
-}
-__device__ __forceinline__ int pivot_col(unsigned long long w) { return (int)(w >> PIV_SHIFT); }
-__device__ __forceinline__ long long pivot_seg(unsigned long long w) { return (long long)((w & PIV_OFF_MASK) << 2); }
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+struct __align__(32) PivRec {
+    int col;
+    int np;
+    int left;
+    unsigned seg4;
+    int e[4];
+};
+
+// The record of a row, read through L2 (two 16-byte loads of one sector).
+__device__ __forceinline__ void rec_load(const PivRec *r, int4 &h, int4 &e) {
+    const int4 *p = reinterpret_cast<const int4 *>(r);
+    h = __ldcg(p);
+    e = __ldcg(p + 1);
+}
+
+__device__ __forceinline__ int ld_acquire_i32(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release(unsigned long long *p, unsigned long long v) {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_release_i32(int *p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// True when a relaxed record read already holds the whole pivot (np <= 4,
+// every needed entry past its marker).
+__device__ __forceinline__ bool rec_complete(const int4 &h, const int4 &e) {
+    const int np = h.y;
+    return np >= 1 && np <= 4 && e.x >= 0 && (np < 2 || e.y >= 0) && (np < 3 || e.z >= 0) && (np < 4 || e.w >= 0);
+}
+__device__ __forceinline__ int rec_entry(const int4 &e, int k) {
+    return k == 0 ? e.x : k == 1 ? e.y : k == 2 ? e.z : e.w;
+}
+
+// Publish column `col` (length n, segment seg, first rows in `rows`) as the
+// pivot of row `row`.  Called by one thread after the column's rows are
+// visible to it (its own writes, or writes ordered before by a barrier).
+// ORDERED = false when the readers run in a later kernel (Phase 0 / I).
+template <bool ORDERED = true>
+__device__ __forceinline__ void rec_publish(PivRec *rec, int row, int col, int n, long long seg, const int *rows) {
+    PivRec *r = rec + row;
+    r->np = n;
+    r->seg4 = (unsigned)(seg >> 2);
+    for (int k = 0; k < 4; k++) r->e[k] = k < n ? rows[k] : -1;
+    if (ORDERED) {
+        fence_acq_rel();
+        st_release_i32(&r->col, col);
+    } else {
+        r->col = col;
+    }
+}
 
 __device__ __forceinline__ int round4(int n) { return (n + 3) & ~3; }
 
@@ -166,6 +214,94 @@ __device__ __forceinline__ int merge_xor_small(const Tile &tile, const int *A, i
     }
     tile.sync();
     return nA + nP - 2 * __popc(dmask);
+}
+
+// Symmetric difference for a pivot of at most G entries held one per lane,
+// by segments: the pivot's entries, ranked in A (lanes k < nP, binary
+// search), cut A into nP + 1 runs that are copied with a constant shift each;
+// a pivot entry absent from A is written between its runs, one present in A
+// removes that element and shifts the following runs down by one.  Per
+// element of A this is a load, a store and an add.  Returns |A xor P|.
+template <int G, class Tile>
+__device__ __forceinline__ int merge_xor_seg(const Tile &tile, const int *A, int nA, int pv, int nP, int *B) {
+    const int lane = tile.thread_rank();
+    int r = 0;
+    bool pdup = false;
+    if (lane < nP) {
+        r = lower_bound(A, nA, pv);
+        pdup = r < nA && A[r] == pv;
+    }
+    const unsigned dmask = tile.ballot(pdup);
+    int src = 0, shift = 0;
+    for (int k = 0; k < nP; k++) {
+        const int rk = tile.shfl(r, k);
+        const int pk = tile.shfl(pv, k);
+        for (int q = src + lane; q < rk; q += G) B[q + shift] = A[q];
+        if ((dmask >> k) & 1u) {
+            src = rk + 1;
+            shift -= 1;
+        } else {
+            if (lane == 0) B[rk + shift] = pk;
+            src = rk;
+            shift += 1;
+        }
+    }
+    for (int q = src + lane; q < nA; q += G) B[q + shift] = A[q];
+    tile.sync();
+    return nA + nP - 2 * __popc(dmask);
+}
+
+// Block-wide symmetric difference (every thread of the CTA), for wide
+// columns: the rank placement of merge_xor with the common-value counts
+// carried across the CTA by per-warp ballots and a shared-memory prefix.
+// `scratch` is 2 * (blockDim.x / 32) ints of shared memory.  A, P, B may be
+// in shared or global memory; B must not alias A or P.
+__device__ __forceinline__ int merge_xor_block(const int *A, int nA, const int *P, int nP, int *B, int *scratch) {
+    const int tid = threadIdx.x, nt = blockDim.x, wid = tid >> 5, lane = tid & 31, nw = nt >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    int *wtot = scratch;  // per-warp counts of the current chunk
+    int carry = 0, common = 0;
+    for (int pass = 0; pass < 2; pass++) {
+        const int *X = pass ? P : A, *Y = pass ? A : P;
+        const int nX = pass ? nP : nA, nY = pass ? nA : nP;
+        carry = 0;
+        for (int base = 0; base < nX; base += nt) {
+            const int i = base + tid;
+            const bool v = i < nX;
+            const int x = v ? X[i] : 0;
+            const int r = v ? lower_bound(Y, nY, x) : 0;
+            const bool dup = v && r < nY && Y[r] == x;
+            const unsigned b = __ballot_sync(0xffffffffu, dup);
+            if (lane == 0) wtot[wid] = __popc(b);
+            __syncthreads();
+            int before = carry + __popc(b & lt), total = 0;
+            for (int q = 0; q < nw; q++) {
+                const int c = wtot[q];
+                if (q < wid) before += c;
+                total += c;
+            }
+            if (v && !dup) B[i + r - 2 * before] = x;
+            carry += total;
+            __syncthreads();
+        }
+        if (pass == 0) common = carry;
+    }
+    __syncthreads();
+    return nA + nP - 2 * common;
+}
+
+// Block copy of n ints (all threads of the CTA).
+__device__ __forceinline__ void block_copy(int *dst, const int *src, int n) {
+    if ((((uintptr_t)dst | (uintptr_t)src) & 15) == 0) {
+        const int n4 = n >> 2;
+        const int4 *s4 = reinterpret_cast<const int4 *>(src);
+        int4 *d4 = reinterpret_cast<int4 *>(dst);
+        for (int q = threadIdx.x; q < n4; q += blockDim.x) d4[q] = s4[q];
+        for (int q = (n4 << 2) + threadIdx.x; q < n; q += blockDim.x) dst[q] = src[q];
+    } else {
+        for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = src[q];
+    }
+    __syncthreads();
 }
 
 // Group copy of n ints; 128-bit moves when both ends are 16-byte aligned.

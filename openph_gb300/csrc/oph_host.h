@@ -38,12 +38,11 @@ struct Work {
     uint8_t *clear = nullptr;         // m: row marked for clearing
     int8_t *dim = nullptr;            // m: nnz(col) - 1, the reference's "dimension"
     int32_t *first = nullptr;         // m: first column (in order) holding each low
-    int32_t *left = nullptr;          // m: first column holding each row in the input
     int32_t *beta = nullptr;          // m
     int32_t *worklist = nullptr;      // m
     int32_t *widelist = nullptr;      // m
     int64_t *seg = nullptr;           // m: segment of each column
-    unsigned long long *rowpiv = nullptr;  // m
+    PivRec *rec = nullptr;            // m: per-row pivot records (left[] inside)
     int32_t *agg = nullptr;           // tiles * MAXC (tile maxima, then exclusive prefixes)
     int64_t ntiles = 0;
     int *pool = nullptr;              // column store

@@ -27,6 +27,7 @@
 #include <algorithm>
 
 #include "oph_host.h"
+#include "pms.cuh"
 
 namespace oph {
 
@@ -34,35 +35,19 @@ constexpr int P1_THREADS = 256;
 constexpr int P1_ITEMS = 8;
 constexpr int P1_TILE = P1_THREADS * P1_ITEMS;
 
-struct PmsArgs {
-    int64_t m;
-    int32_t *low;
-    int8_t *classes;
-    uint8_t *clear;
-    const int8_t *dim;
-    int32_t *first;
-    const int32_t *left;
-    const int32_t *beta;
-    int32_t *worklist;
-    int32_t *widelist;
-    int64_t *seg;
-    unsigned long long *rowpiv;
-    int32_t *agg;
-    int64_t ntiles;
-    int *pool;
-    DevStatus *st;
-};
+
 
 // ---------------------------------------------------------------- Phase 0
 // mark_pivots_and_clear (pms_functions.cu:33-53): low_j == beta_j >= 0 means
 // row low_j first appears in column j, so j is a final pivot; the column of
 // row low_j is positive and is cleared (the clear is applied by Phase I).
-__global__ void k_phase0(PmsArgs a) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.m; j += (int64_t)gridDim.x * blockDim.x) {
+__global__ void k_phase0(PmsArgs a, int64_t c0, int64_t c1) {
+    for (int64_t j = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < c1; j += (int64_t)gridDim.x * blockDim.x) {
         int lj = a.low[j];
         if (lj >= 0 && lj == a.beta[j]) {
             a.classes[j] = -1;
-            a.rowpiv[lj] = pack_pivot((int)j, a.seg[j]);
+            const long long sj = a.seg[j];
+            rec_publish<false>(a.rec, lj, (int)j, a.pool[sj], sj, a.pool + sj + SEG_HDR);
             a.clear[lj] = 1;
         }
     }
@@ -76,9 +61,7 @@ __global__ void k_p1_first(PmsArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.st->reps = 0;
         a.st->wl_count = 0;
-        a.st->wl_cursor = 0;
-        a.st->wide_count = 0;
-        a.st->wide_cursor = 0;
+        for (int t = 0; t < 4; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
     }
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.m; j += (int64_t)gridDim.x * blockDim.x) {
         int lj = a.low[j];
@@ -91,8 +74,8 @@ __global__ void k_p1_first(PmsArgs a) {
         if (lj >= 0) {
             // a column whose low already has a pivot to its left is a repeat:
             // the pivot itself records first[low], so only the others race
-            const unsigned long long w = a.rowpiv[lj];
-            if (w == NO_PIVOT || pivot_col(w) >= (int)j) atomicMin(&a.first[lj], (int)j);
+            const int pc = a.rec[lj].col;
+            if (pc < 0 || pc >= (int)j) atomicMin(&a.first[lj], (int)j);
         }
     }
 }
@@ -113,6 +96,7 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
 #pragma unroll
     for (int d = 0; d < MAXC; d++) mx[d] = -1;
     int reps = 0;
+    int cur_inst = -1, cur_reps = 0;  // per-instance counts, flushed on change
     const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
@@ -125,9 +109,19 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
                 for (int d = 0; d < MAXC; d++)
                     if (d == b) mx[d] = max(mx[d], lj);
                 reps++;
+                if (a.ireps) {
+                    const int ib = a.inst[j];
+                    if (ib != cur_inst) {
+                        if (cur_reps) atomicAdd(&a.ireps[cur_inst], cur_reps);
+                        cur_inst = ib;
+                        cur_reps = 0;
+                    }
+                    cur_reps++;
+                }
             }
         }
     }
+    if (cur_reps) atomicAdd(&a.ireps[cur_inst], cur_reps);
     __syncthreads();
     if (reps) atomicAdd(&sreps, reps);
 #pragma unroll
@@ -240,7 +234,8 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
                 if (d == bkt[t]) pre[d] = max(pre[d], lj);
         } else if (a.classes[j] == 0 && lj > ceil) {
             a.classes[j] = -1;
-            a.rowpiv[lj] = pack_pivot((int)j, a.seg[j]);
+            const long long sj = a.seg[j];
+            rec_publish<false>(a.rec, lj, (int)j, a.pool[sj], sj, a.pool + sj + SEG_HDR);
             a.clear[lj] = 1;
         }
     }
@@ -266,130 +261,99 @@ __global__ void k_p1_worklist(PmsArgs a) {
             }
             want = lj >= 0 && a.classes[j] == 0;
         }
-        warp_append(want, (int)j, a.worklist, &a.st->wl_count);
+        warp_append(want, (int)j, a.worklist, &a.st->t_count[0]);
     }
 }
 
 // -------------------------------------------------------------- Phase II
-// phase_ii (pms_functions.cu:87-112) for one column j by a group of G lanes.
-// A/B/C are the group's shared buffers of `cap` ints (A: the column, B: merge
-// output, C: the staged pivot).  Returns false if j was handed to the next
-// tier (too wide) — its state is written back first — or if a pool
-// allocation failed (nothing of j is changed then).
-template <int G, class Tile>
-__device__ void reduce_column(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int *C, int cap,
-                              int32_t *handoff, int *handoff_cnt, long long &adds, long long &slots) {
-    const int lane = tile.thread_rank();
-    int lj = a.low[j];
-    unsigned long long w = ld_acquire(&a.rowpiv[lj]);
-    if (w == NO_PIVOT || pivot_col(w) >= j) return;
-    const long long sj = a.seg[j];
-    int n = a.pool[sj];
-    const int capj = a.pool[sj + 1];
-    if (n > cap) {
-        if (lane == 0) handoff[atomicAdd(handoff_cnt, 1)] = j;
-        return;
+// Pool allocation for column j: the global bump pointer, or the pool region
+// of j's instance when the columns belong to several instances.
+__device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long long ints) {
+    if (!a.inst) return pool_alloc(a.st, ints);
+    const int b = a.inst[j];
+    const unsigned long long off = atomicAdd(&a.ipool[2 * b], (unsigned long long)ints);
+    if (off + (unsigned long long)ints > a.ipool[2 * b + 1]) {
+        atomicExch(&a.iover[b], 1);
+        atomicExch(&a.st->overflow, 1);
+        return -1;
     }
-    group_copy<G>(tile, A, a.pool + sj + SEG_HDR, n);
-    bool made_pivot = false, handed = false;
-    for (;;) {
-        const long long sp = pivot_seg(w);
-        const int np = a.pool[sp];
-        if (n + np > cap) { handed = true; break; }
-        group_copy<G>(tile, C, a.pool + sp + SEG_HDR, np);
-        const int nn = merge_xor<G>(tile, A, n, C, np, B);
-        slots += n + np + nn;
-        adds++;
-        n = nn;
-        int *t = A; A = B; B = t;
-        lj = n ? A[n - 1] : -1;
-        if (lj < 0) break;
-        if (a.left[lj] == j) made_pivot = true;
-        if (lane == 0) a.clear[lj] = 1;
-        if (made_pivot) break;
-        w = ld_acquire(&a.rowpiv[lj]);
-        if (w == NO_PIVOT || pivot_col(w) >= j) break;
-    }
-    // write the column back: in place when it fits, else a fresh segment
-    long long dst = sj;
-    int dcap = capj;
-    if (n > capj) {
-        dcap = round4(max(2 * n, 16));
-        long long off = 0;
-        if (lane == 0) off = pool_alloc(a.st, SEG_HDR + dcap);
-        off = tile.shfl(off, 0);
-        if (off < 0) return;  // pool exhausted: j keeps its pre-sweep state
-        dst = off;
-    }
-    group_copy<G>(tile, a.pool + dst + SEG_HDR, A, n);
-    if (lane == 0) {
-        a.pool[dst] = n;
-        a.pool[dst + 1] = dcap;
-        a.seg[j] = dst;
-        a.low[j] = lj;
-    }
-    if (made_pivot) {
-        fence_acq_rel();
-        tile.sync();
-        if (lane == 0) {
-            a.classes[j] = -1;
-            st_release(&a.rowpiv[lj], pack_pivot(j, dst));
-        }
-    } else if (handed) {
-        if (lane == 0) handoff[atomicAdd(handoff_cnt, 1)] = j;
-    }
-    tile.sync();
+    return (long long)off;
 }
 
-// Narrow tier: G lanes per column, the column in shared memory (A/B, CAP
-// ints each), the pivot in registers when it has at most G entries (the
-// common case: most pivots are apparent pairs with 3 entries) and read from
-// the store otherwise.  Each addition is two dependent round trips: the pivot
-// word (with left[] alongside) and the pivot's header + rows in one go.
-// Reads up to G ints past a segment's start, which the pool's tail padding
-// keeps in bounds.
-template <int G, class Tile>
-__device__ void reduce_column_narrow(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int cap,
-                                     long long &adds, long long &slots) {
+// Phase II tiers.  A column is reduced with its rows in shared memory across
+// its whole chain of additions; a column that would outgrow its tier is
+// written back and queued for the next tier:
+//   tier 0  8 lanes per column, CAP 128      (4 columns per warp)
+//   tier 1  a warp per column,  CAP 512      (pivot staged in shared memory
+//                                             when wider than the warp)
+//   tier 2  a CTA per column,   CAP 8192     (block-wide merge)
+//   tier 3  a CTA per column,   buffers in the pool (no limit)
+// Pivots of at most G entries (most are apparent pairs of 3 entries) are held
+// one per lane and merged by segment copies (merge_xor_seg).  The queues
+// ping-pong between the worklist and widelist arrays.  Each addition costs
+// one dependent round trip when the pivot has at most four entries (its
+// record carries them, with left[] for the beta check) and two otherwise;
+// reading G ints past a segment start stays in bounds through the pool's
+// tail padding.
+template <int G, bool SMALL_PIVOTS_ONLY, class Tile>
+__device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int *C, int cap,
+                                   int32_t *out_list, int *out_cnt, long long &adds, long long &slots) {
     const int lane = tile.thread_rank();
     int lj = a.low[j];
-    unsigned long long w = ld_acquire(&a.rowpiv[lj]);
-    if (w == NO_PIVOT || pivot_col(w) >= j) return;
+    int4 h, e;
+    rec_load(&a.rec[lj], h, e);
+    if (h.x < 0 || h.x >= j) return;  // no pivot to the left of j yet
     const long long sj = a.seg[j];
     int n = a.pool[sj];
     const int capj = a.pool[sj + 1];
     if (n > cap) {
-        if (lane == 0) a.widelist[atomicAdd(&a.st->wide_count, 1)] = j;
+        if (lane == 0) out_list[atomicAdd(out_cnt, 1)] = j;
         return;
     }
     group_copy<G>(tile, A, a.pool + sj + SEG_HDR, n);
     bool made_pivot = false, handed = false;
     for (;;) {
-        const long long sp = pivot_seg(w);
-        const int np = a.pool[sp];
-        const int pv = a.pool[sp + SEG_HDR + lane];
-        if (n + np > cap) { handed = true; break; }
+        // the pivot's rows: from the record when it holds them all, else from
+        // the pivot's segment after an acquire of the record
+        int np, pv;
+        const int *P = nullptr;
+        if (rec_complete(h, e)) {
+            np = h.y;
+            pv = rec_entry(e, lane & 3);
+        } else {
+            ld_acquire_i32(&a.rec[lj].col);
+            const int4 h2 = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+            np = h2.y;
+            P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
+            pv = P[lane];
+        }
+        if (n + np > cap || (SMALL_PIVOTS_ONLY && np > G)) { handed = true; break; }
         int nn;
-        if (np <= G) nn = merge_xor_small<G>(tile, A, n, pv, np, B);
-        else nn = merge_xor<G>(tile, A, n, a.pool + sp + SEG_HDR, np, B);
+        if (np <= G) {
+            nn = merge_xor_seg<G>(tile, A, n, pv, np, B);
+        } else if (C) {
+            group_copy<G>(tile, C, P, np);
+            nn = merge_xor<G>(tile, A, n, C, np, B);
+        } else {
+            nn = merge_xor<G>(tile, A, n, P, np, B);
+        }
         slots += n + np + nn;
         adds++;
         n = nn;
         int *t = A; A = B; B = t;
         lj = n ? A[n - 1] : -1;
         if (lj < 0) break;
-        const int lf = a.left[lj];
-        w = ld_acquire(&a.rowpiv[lj]);
+        rec_load(&a.rec[lj], h, e);
         if (lane == 0) a.clear[lj] = 1;
-        if (lf == j) { made_pivot = true; break; }
-        if (w == NO_PIVOT || pivot_col(w) >= j) break;
+        if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
+        if (h.x < 0 || h.x >= j) break;
     }
     long long dst = sj;
     int dcap = capj;
     if (n > capj) {
-        dcap = round4(max(2 * n, 16));
+        dcap = round4(max(n + (n >> 1), 16));
         long long off = 0;
-        if (lane == 0) off = pool_alloc(a.st, SEG_HDR + dcap);
+        if (lane == 0) off = col_alloc(a, j, SEG_HDR + dcap);
         off = tile.shfl(off, 0);
         if (off < 0) return;  // pool exhausted: j keeps its pre-sweep state
         dst = off;
@@ -406,143 +370,171 @@ __device__ void reduce_column_narrow(const Tile &tile, const PmsArgs &a, int j, 
         tile.sync();
         if (lane == 0) {
             a.classes[j] = -1;
-            st_release(&a.rowpiv[lj], pack_pivot(j, dst));
+            rec_publish(a.rec, lj, j, n, dst, A);
         }
     } else if (handed) {
-        if (lane == 0) a.widelist[atomicAdd(&a.st->wide_count, 1)] = j;
+        if (lane == 0) out_list[atomicAdd(out_cnt, 1)] = j;
     }
     tile.sync();
 }
 
-template <int G, int CAP>
-__global__ void __launch_bounds__(256) k_p2_narrow(PmsArgs a) {
+__device__ __forceinline__ void tier_stats(const PmsArgs &a, int tier, long long adds, long long slots) {
+    if (adds) {
+        atomicAdd(&a.st->additions, (unsigned long long)adds);
+        atomicAdd(&a.st->slots, (unsigned long long)slots);
+        atomicAdd(&a.st->tier_adds[tier], (unsigned long long)adds);
+        atomicAdd(&a.st->tier_slots[tier], (unsigned long long)slots);
+    }
+}
+
+// Tiers 0 and 1: groups of G lanes, each group with A/B buffers of CAP ints
+// and, with STAGE, a C buffer into which a pivot wider than the group is
+// staged; without it (tier 0) such a pivot is searched in the store.
+template <int G, int CAP, int BLOCK, bool STAGE>
+__global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
     if (a.st->converged) return;
     extern __shared__ int smem[];
     auto tile = cg::tiled_partition<G>(cg::this_thread_block());
     const int gid = threadIdx.x / G;
-    int *buf = smem + (size_t)gid * 2 * CAP;
-    const int count = a.st->wl_count;
+    int *buf = smem + (size_t)gid * (STAGE ? 3 : 2) * CAP;
+    int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
+    int32_t *out_list = (tier & 1) ? a.worklist : a.widelist;
+    const int count = a.st->t_count[tier];
     long long adds = 0, slots = 0;
     for (;;) {
         int idx = 0;
-        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->wl_cursor, 1);
+        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->t_cursor[tier], 1);
         idx = tile.shfl(idx, 0);
         if (idx >= count) break;
-        reduce_column_narrow<G>(tile, a, a.worklist[idx], buf, buf + CAP, CAP, adds, slots);
+        reduce_column_smem<G, false>(tile, a, in_list[idx], buf, buf + CAP, STAGE ? buf + 2 * CAP : nullptr, CAP,
+                                     out_list, &a.st->t_count[tier + 1], adds, slots);
     }
-    if (tile.thread_rank() == 0 && adds) {
-        atomicAdd(&a.st->additions, (unsigned long long)adds);
-        atomicAdd(&a.st->slots, (unsigned long long)slots);
-    }
+    if (tile.thread_rank() == 0) tier_stats(a, tier, adds, slots);
 }
 
-// Wide tier: one warp per column with large shared buffers; columns wider
-// still fall through to the global tier (handoff list = worklist, reused).
-template <int CAP>
-__global__ void __launch_bounds__(32) k_p2_wide(PmsArgs a) {
+// Tiers 2 and 3: the whole CTA on one column.  With cap > 0 the column and
+// the staged pivot live in shared memory (A/B/C of cap ints); with cap == 0
+// they live in pool-allocated buffers that grow as needed.
+__device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, int *sC, int cap, int *scratch,
+                                    int32_t *out_list, int *out_cnt, long long &adds, long long &slots) {
+    __shared__ long long s_off;
+    __shared__ int s_small[4];
+    const int tid = threadIdx.x;
+    int lj = a.low[j];
+    int4 h, e;
+    rec_load(&a.rec[lj], h, e);
+    if (h.x < 0 || h.x >= j) return;
+    const long long sj = a.seg[j];
+    int n = a.pool[sj];
+    const int capj = a.pool[sj + 1];
+    const bool smem_mode = cap > 0;
+    if (smem_mode && n > cap) {
+        if (tid == 0) out_list[atomicAdd(out_cnt, 1)] = j;
+        return;
+    }
+    int *A, *B;
+    int bcap;
+    if (smem_mode) {
+        A = sA; B = sB; bcap = cap;
+        block_copy(A, a.pool + sj + SEG_HDR, n);
+    } else {
+        bcap = round4(max(2 * n, 4096));
+        if (tid == 0) s_off = col_alloc(a, j, 2ll * bcap);
+        __syncthreads();
+        if (s_off < 0) return;
+        A = a.pool + s_off; B = A + bcap;
+        block_copy(A, a.pool + sj + SEG_HDR, n);
+    }
+    bool made_pivot = false, handed = false;
+    for (;;) {
+        int np;
+        const int *P;
+        if (rec_complete(h, e)) {
+            np = h.y;
+            if (tid < np) s_small[tid] = rec_entry(e, tid);
+            __syncthreads();
+            P = s_small;
+        } else {
+            ld_acquire_i32(&a.rec[lj].col);
+            const int4 h2 = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+            np = h2.y;
+            P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
+        }
+        if (n + np > bcap) {
+            if (smem_mode) { handed = true; break; }
+            const int ncap = round4(2 * (n + np));
+            if (tid == 0) s_off = col_alloc(a, j, 2ll * ncap);
+            __syncthreads();
+            if (s_off < 0) return;  // j keeps its pre-sweep state
+            int *NA = a.pool + s_off;
+            block_copy(NA, A, n);
+            A = NA; B = NA + ncap; bcap = ncap;
+        }
+        if (smem_mode && P != s_small) {
+            block_copy(sC, P, np);
+            P = sC;
+        }
+        const int nn = merge_xor_block(A, n, P, np, B, scratch);
+        slots += n + np + nn;
+        adds++;
+        n = nn;
+        int *t = A; A = B; B = t;
+        lj = n ? A[n - 1] : -1;
+        if (lj < 0) break;
+        rec_load(&a.rec[lj], h, e);
+        if (tid == 0) a.clear[lj] = 1;
+        if (h.z == j) { made_pivot = true; break; }
+        if (h.x < 0 || h.x >= j) break;
+    }
+    long long dst = sj;
+    int dcap = capj;
+    if (n > capj) {
+        dcap = round4(max(n + (n >> 1), 16));
+        if (tid == 0) s_off = col_alloc(a, j, SEG_HDR + dcap);
+        __syncthreads();
+        if (s_off < 0) return;
+        dst = s_off;
+    }
+    block_copy(a.pool + dst + SEG_HDR, A, n);
+    if (tid == 0) {
+        a.pool[dst] = n;
+        a.pool[dst + 1] = dcap;
+        a.seg[j] = dst;
+        a.low[j] = lj;
+    }
+    if (made_pivot) {
+        fence_acq_rel();
+        __syncthreads();
+        if (tid == 0) {
+            a.classes[j] = -1;
+            rec_publish(a.rec, lj, j, n, dst, A);
+        }
+    } else if (handed) {
+        if (tid == 0) out_list[atomicAdd(out_cnt, 1)] = j;
+    }
+    __syncthreads();
+}
+
+template <int CAP, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
     if (a.st->converged) return;
     extern __shared__ int smem[];
-    auto tile = cg::tiled_partition<32>(cg::this_thread_block());
-    const int count = a.st->wide_count;
+    __shared__ int scratch[2 * (BLOCK / 32)];
+    __shared__ int s_idx;
+    int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
+    int32_t *out_list = (tier & 1) ? a.worklist : a.widelist;
+    const int count = a.st->t_count[tier];
     long long adds = 0, slots = 0;
     for (;;) {
-        int idx = 0;
-        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->wide_cursor, 1);
-        idx = tile.shfl(idx, 0);
+        if (threadIdx.x == 0) s_idx = atomicAdd(&a.st->t_cursor[tier], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        __syncthreads();
         if (idx >= count) break;
-        reduce_column<32>(tile, a, a.widelist[idx], smem, smem + CAP, smem + 2 * CAP, CAP, a.worklist,
-                          &a.st->wl_count, adds, slots);
+        reduce_column_block(a, in_list[idx], smem, smem + CAP, smem + 2 * CAP, CAP, scratch, out_list,
+                            tier < 3 ? &a.st->t_count[tier + 1] : nullptr, adds, slots);
     }
-    if (tile.thread_rank() == 0 && adds) {
-        atomicAdd(&a.st->additions, (unsigned long long)adds);
-        atomicAdd(&a.st->slots, (unsigned long long)slots);
-    }
-}
-
-// Global tier: one warp per column, buffers bump-allocated in the pool.
-__global__ void __launch_bounds__(32) k_p2_global(PmsArgs a) {
-    if (a.st->converged) return;
-    auto tile = cg::tiled_partition<32>(cg::this_thread_block());
-    const int lane = tile.thread_rank();
-    const int count = a.st->wl_count;
-    long long adds = 0, slots = 0;
-    for (int idx = blockIdx.x; idx < count; idx += gridDim.x) {
-        const int j = a.worklist[idx];
-        int lj = a.low[j];
-        unsigned long long w = ld_acquire(&a.rowpiv[lj]);
-        if (w == NO_PIVOT || pivot_col(w) >= j) continue;
-        const long long sj = a.seg[j];
-        int n = a.pool[sj];
-        const int capj = a.pool[sj + 1];
-        const int *A = a.pool + sj + SEG_HDR;
-        int *X = nullptr, *Y = nullptr;
-        int bcap = 0;
-        bool made_pivot = false, failed = false;
-        for (;;) {
-            const long long sp = pivot_seg(w);
-            const int np = a.pool[sp];
-            if (n + np > bcap) {
-                int ncap = round4(max(2 * (n + np), 1024));
-                long long off = 0;
-                if (lane == 0) off = pool_alloc(a.st, 2ll * ncap);
-                off = tile.shfl(off, 0);
-                if (off < 0) { failed = true; break; }
-                int *NX = a.pool + off, *NY = NX + ncap;
-                group_copy<32>(tile, NX, A, n);
-                A = NX; X = NX; Y = NY; bcap = ncap;
-            }
-            int *out = (A == X) ? Y : X;
-            const int nn = merge_xor<32>(tile, A, n, a.pool + sp + SEG_HDR, np, out);
-            slots += n + np + nn;
-            adds++;
-            n = nn;
-            A = out;
-            lj = n ? A[n - 1] : -1;
-            if (lj < 0) break;
-            if (a.left[lj] == j) made_pivot = true;
-            if (lane == 0) a.clear[lj] = 1;
-            if (made_pivot) break;
-            w = ld_acquire(&a.rowpiv[lj]);
-            if (w == NO_PIVOT || pivot_col(w) >= j) break;
-        }
-        if (failed) continue;
-        long long dst = sj;
-        int dcap = capj;
-        if (n > capj) {
-            dcap = round4(max(2 * n, 16));
-            long long off = 0;
-            if (lane == 0) off = pool_alloc(a.st, SEG_HDR + dcap);
-            off = tile.shfl(off, 0);
-            if (off < 0) continue;
-            dst = off;
-        }
-        if (A != a.pool + dst + SEG_HDR) group_copy<32>(tile, a.pool + dst + SEG_HDR, A, n);
-        if (lane == 0) {
-            a.pool[dst] = n;
-            a.pool[dst + 1] = dcap;
-            a.seg[j] = dst;
-            a.low[j] = lj;
-        }
-        if (made_pivot) {
-            fence_acq_rel();
-            tile.sync();
-            if (lane == 0) {
-                a.classes[j] = -1;
-                st_release(&a.rowpiv[lj], pack_pivot(j, dst));
-            }
-        }
-        tile.sync();
-    }
-    if (lane == 0 && adds) {
-        atomicAdd(&a.st->additions, (unsigned long long)adds);
-        atomicAdd(&a.st->slots, (unsigned long long)slots);
-    }
-}
-
-// Resets the global-tier queue before the wide kernel hands columns over.
-__global__ void k_reset_global_queue(DevStatus *st) {
-    if (st->converged) return;
-    st->wl_count = 0;
+    if (threadIdx.x == 0) tier_stats(a, tier, adds, slots);
 }
 
 __global__ void k_count_sweep(DevStatus *st) {
@@ -550,109 +542,149 @@ __global__ void k_count_sweep(DevStatus *st) {
 }
 
 // ------------------------------------------------------------------ driver
-#ifndef OPH_NARROW_G
-#define OPH_NARROW_G 8
+#ifndef OPH_T0_G
+#define OPH_T0_G 8
 #endif
-#ifndef OPH_NARROW_CAP
-#define OPH_NARROW_CAP 128
+#ifndef OPH_T0_CAP
+#define OPH_T0_CAP 128
 #endif
-constexpr int NARROW_G = OPH_NARROW_G;
-constexpr int NARROW_CAP = OPH_NARROW_CAP;
-constexpr int WIDE_CAP = 8192;
+#ifndef OPH_T1_CAP
+#define OPH_T1_CAP 512
+#endif
+#ifndef OPH_T1_G
+#define OPH_T1_G 32
+#endif
+constexpr int T0_G = OPH_T0_G, T0_CAP = OPH_T0_CAP, T0_BLOCK = 256;
+constexpr int T1_G = OPH_T1_G, T1_CAP = OPH_T1_CAP, T1_BLOCK = 256;
+constexpr int T2_CAP = 8192, T2_BLOCK = 256;
+constexpr int T3_BLOCK = 256;
+
+// Occupancy-filling grid for a kernel with `smem` bytes of dynamic shared
+// memory (attribute set once per device).
+template <class K>
+static int fill_grid(Context *ctx, K kernel, int block, size_t smem, int *done) {
+    if (!done[ctx->device & 63]) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return -1;
+        done[ctx->device & 63] = 1;
+    }
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, block, smem) != cudaSuccess) return -1;
+    return ctx->sm_count * (nb < 1 ? 1 : nb);
+}
+
+int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
+    static int done0[64], done1[64], done2[64];
+    g->s0 = (size_t)(T0_BLOCK / T0_G) * 2 * T0_CAP * sizeof(int);
+    g->s1 = (size_t)(T1_BLOCK / T1_G) * 3 * T1_CAP * sizeof(int);
+    g->s2 = (size_t)3 * T2_CAP * sizeof(int);
+    g->g0 = fill_grid(ctx, k_p2_tier<T0_G, T0_CAP, T0_BLOCK, false>, T0_BLOCK, g->s0, done0);
+    g->g1 = fill_grid(ctx, k_p2_tier<T1_G, T1_CAP, T1_BLOCK, true>, T1_BLOCK, g->s1, done1);
+    g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
+    g->g3 = ctx->sm_count * 2;
+    g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
+    g->t = (int)std::max<int64_t>(1, ntiles);
+    if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0) {
+        fprintf(stderr, "openph_gb300: Phase II kernel set-up failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+        return OPH_ERR_CUDA;
+    }
+    return OPH_OK;
+}
+
+void launch_phase0(const PmsArgs &a, int64_t c0, int64_t c1, int grid, cudaStream_t s) {
+    k_phase0<<<grid, 256, 0, s>>>(a, c0, c1);
+}
+
+// ev (optional, 6 events): before Phase I, after Phase I, after each tier.
+static void launch_sweep_ev(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, cudaEvent_t *ev) {
+    if (ev) cudaEventRecord(ev[0], s);
+    k_p1_first<<<g.m, 256, 0, s>>>(a);
+    k_p1_tiles<<<g.t, P1_THREADS, 0, s>>>(a);
+    k_p1_scan<<<1, 32 * MAXC, 0, s>>>(a);
+    k_p1_mark<<<g.t, P1_THREADS, 0, s>>>(a);
+    k_p1_worklist<<<g.m, 256, 0, s>>>(a);
+    if (ev) cudaEventRecord(ev[1], s);
+    k_p2_tier<T0_G, T0_CAP, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0);
+    if (ev) cudaEventRecord(ev[2], s);
+    k_p2_tier<T1_G, T1_CAP, T1_BLOCK, true><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
+    if (ev) cudaEventRecord(ev[3], s);
+    k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
+    if (ev) cudaEventRecord(ev[4], s);
+    k_p2_block<0, T3_BLOCK><<<g.g3, T3_BLOCK, 0, s>>>(a, 3);
+    k_count_sweep<<<1, 1, 0, s>>>(a.st);
+    if (ev) cudaEventRecord(ev[5], s);
+}
+
+void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) { launch_sweep_ev(a, g, s, nullptr); }
+
+constexpr int KERNELS_PER_SWEEP = 10;
 
 int run_pms(Context *ctx, Work &w, oph_info *info) {
     const int64_t m = w.m;
     PmsArgs a{};
     a.m = m; a.low = w.low; a.classes = w.classes; a.clear = w.clear; a.dim = w.dim; a.first = w.first;
-    a.left = w.left; a.beta = w.beta; a.worklist = w.worklist; a.widelist = w.widelist; a.seg = w.seg;
-    a.rowpiv = w.rowpiv; a.agg = w.agg; a.ntiles = w.ntiles; a.pool = w.pool; a.st = w.st;
+    a.beta = w.beta; a.worklist = w.worklist; a.widelist = w.widelist; a.seg = w.seg;
+    a.rec = w.rec; a.agg = w.agg; a.ntiles = w.ntiles; a.pool = w.pool; a.st = w.st;
     cudaStream_t s = ctx->stream;
-
-    static bool attr_done[64] = {};
-    const size_t narrow_smem = (size_t)(256 / NARROW_G) * 2 * NARROW_CAP * sizeof(int);
-    const size_t wide_smem = (size_t)3 * WIDE_CAP * sizeof(int);
-    if (!attr_done[ctx->device & 63]) {
-        OPH_CUDA_TRY(cudaFuncSetAttribute(k_p2_narrow<NARROW_G, NARROW_CAP>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem));
-        OPH_CUDA_TRY(cudaFuncSetAttribute(k_p2_wide<WIDE_CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)wide_smem));
-        attr_done[ctx->device & 63] = true;
-    }
-    int nb_narrow = 0;
-    OPH_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_narrow, k_p2_narrow<NARROW_G, NARROW_CAP>, 256,
-                                                               narrow_smem));
-    if (nb_narrow < 1) nb_narrow = 1;
-    const int grid_narrow = ctx->sm_count * nb_narrow;
-    int nb_wide = 0;
-    OPH_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb_wide, k_p2_wide<WIDE_CAP>, 32, wide_smem));
-    if (nb_wide < 1) nb_wide = 1;
-    const int grid_wide = ctx->sm_count * nb_wide;
-    const int grid_m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
-    const int grid_t = (int)std::max<int64_t>(1, w.ntiles);
+    SweepGrids g;
+    int rc = sweep_grids(ctx, m, w.ntiles, &g);
+    if (rc) return rc;
 
     OPH_CUDA_TRY(cudaMemsetAsync(w.first, 0x7f, sizeof(int32_t) * m, s));
-    OPH_CUDA_TRY(cudaMemsetAsync(w.rowpiv, 0xff, sizeof(unsigned long long) * m, s));
     OPH_CUDA_TRY(cudaMemsetAsync(w.classes, 0, m, s));
     OPH_CUDA_TRY(cudaMemsetAsync(w.clear, 0, m, s));
 
     cudaEventRecord(ctx->ev[0], s);
-    k_phase0<<<grid_m, 256, 0, s>>>(a);
+    launch_phase0(a, 0, m, g.m, s);
     ctx->launches++;
     OPH_CUDA_TRY(cudaGetLastError());
 
-    // profiling: 4 events per sweep (before Phase I, before/after the narrow
-    // tier, after the wide and global tiers), reused batch after batch
+    // per-phase events: 6 per sweep, reused batch after batch
     constexpr int MAX_BATCH = 16;
-    if (ctx->profile && ctx->pev_n < 4 * MAX_BATCH + 2) {
-        ctx->pev = (cudaEvent_t *)realloc(ctx->pev, sizeof(cudaEvent_t) * (4 * MAX_BATCH + 2));
-        for (int i = ctx->pev_n; i < 4 * MAX_BATCH + 2; i++) cudaEventCreate(&ctx->pev[i]);
-        ctx->pev_n = 4 * MAX_BATCH + 2;
+    const int nev = 6 * MAX_BATCH + 1;
+    if ((ctx->profile || getenv("OPH_TRACE")) && ctx->pev_n < nev) {
+        ctx->pev = (cudaEvent_t *)realloc(ctx->pev, sizeof(cudaEvent_t) * nev);
+        for (int i = ctx->pev_n; i < nev; i++) cudaEventCreate(&ctx->pev[i]);
+        ctx->pev_n = nev;
     }
-    if (ctx->profile) cudaEventRecord(ctx->pev[4 * MAX_BATCH], s);  // end of Phase 0
+    // OPH_TRACE=1: one sweep per batch, per-tier queue sizes, additions and
+    // times printed to stderr (diagnostics only)
+    static const int trace = getenv("OPH_TRACE") ? atoi(getenv("OPH_TRACE")) : 0;
+    const bool timed = ctx->profile || trace;
+    if (timed) cudaEventRecord(ctx->pev[6 * MAX_BATCH], s);  // end of Phase 0
 
     const int max_sweeps = ctx->max_sweeps > 0 ? ctx->max_sweeps : 1 << 20;
     int sweeps_launched = 0;
-    int batch = 2;
+    int batch = trace ? 1 : 2;
     DevStatus hs{};
-    int rc = OPH_OK;
     float p2_ms = 0, p2w_ms = 0, p1_ms = 0;
-    int p2_launches = 0;
-    int regrows = 0;
+    int p2_launches = 0, regrows = 0;
     for (;;) {
         const int nb = std::min(batch, max_sweeps - sweeps_launched);
+        DevStatus before = hs;
         for (int b = 0; b < nb; b++) {
-            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b], s);
-            k_p1_first<<<grid_m, 256, 0, s>>>(a);
-            k_p1_tiles<<<grid_t, P1_THREADS, 0, s>>>(a);
-            k_p1_scan<<<1, 32 * MAXC, 0, s>>>(a);
-            k_p1_mark<<<grid_t, P1_THREADS, 0, s>>>(a);
-            k_p1_worklist<<<grid_m, 256, 0, s>>>(a);
-            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b + 1], s);
-            k_p2_narrow<NARROW_G, NARROW_CAP><<<grid_narrow, 256, narrow_smem, s>>>(a);
-            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b + 2], s);
-            k_reset_global_queue<<<1, 1, 0, s>>>(w.st);
-            k_p2_wide<WIDE_CAP><<<grid_wide, 32, wide_smem, s>>>(a);
-            k_p2_global<<<ctx->sm_count * 4, 32, 0, s>>>(a);
-            k_count_sweep<<<1, 1, 0, s>>>(w.st);
-            if (ctx->profile) cudaEventRecord(ctx->pev[4 * b + 3], s);
-            ctx->launches += 10;
+            launch_sweep_ev(a, g, s, timed ? ctx->pev + 6 * b : nullptr);
+            ctx->launches += KERNELS_PER_SWEEP;
         }
         sweeps_launched += nb;
         OPH_CUDA_TRY(cudaGetLastError());
         OPH_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, w.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
         OPH_CUDA_TRY(cudaStreamSynchronize(s));
         hs = *ctx->h_status;
-        if (ctx->profile) {
-            // sweeps past convergence return at once; count only working ones
+        if (timed) {
             const int worked = std::max(0, std::min(nb, hs.sweeps - (sweeps_launched - nb)));
             for (int b = 0; b < nb; b++) {
-                float t1 = 0, t2 = 0, t3 = 0;
-                cudaEventElapsedTime(&t1, ctx->pev[4 * b], ctx->pev[4 * b + 1]);
-                cudaEventElapsedTime(&t2, ctx->pev[4 * b + 1], ctx->pev[4 * b + 2]);
-                cudaEventElapsedTime(&t3, ctx->pev[4 * b + 2], ctx->pev[4 * b + 3]);
-                p1_ms += t1;
-                p2_ms += t2;
-                p2w_ms += t3;
+                float t[5];
+                for (int q = 0; q < 5; q++) cudaEventElapsedTime(&t[q], ctx->pev[6 * b + q], ctx->pev[6 * b + q + 1]);
+                p1_ms += t[0];
+                p2_ms += t[1];
+                p2w_ms += t[2] + t[3] + t[4];
+                if (trace && b < worked)
+                    fprintf(stderr, "sweep %d: queued t0=%d t1=%d t2=%d t3=%d | adds t0=%llu t1=%llu t2=%llu t3=%llu | "
+                                    "ms p1=%.3f t0=%.3f t1=%.3f t2=%.3f t3=%.3f\n", hs.sweeps, hs.t_count[0],
+                            hs.t_count[1], hs.t_count[2], hs.t_count[3], hs.tier_adds[0] - before.tier_adds[0],
+                            hs.tier_adds[1] - before.tier_adds[1], hs.tier_adds[2] - before.tier_adds[2],
+                            hs.tier_adds[3] - before.tier_adds[3], t[0], t[1], t[2], t[3], t[4]);
             }
             p2_launches += worked;
         }
@@ -660,8 +692,8 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         if (hs.overflow) {
             // a column could not be written back: grow the store and run the
             // sweep again from the consistent state the kernels left
-            int g = grow_pool(ctx, w);
-            if (g != OPH_OK) { rc = g; break; }
+            int gr = grow_pool(ctx, w);
+            if (gr != OPH_OK) { rc = gr; break; }
             a.pool = w.pool;
             regrows++;
             if (hs.converged) break;
@@ -669,7 +701,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         }
         if (hs.converged) break;
         if (sweeps_launched >= max_sweeps) { rc = OPH_ERR_TIMEOUT; break; }
-        batch = std::min(batch * 2, MAX_BATCH);
+        if (!trace) batch = std::min(batch * 2, MAX_BATCH);
     }
     cudaEventRecord(ctx->ev[1], s);
     OPH_CUDA_TRY(cudaEventSynchronize(ctx->ev[1]));
@@ -677,12 +709,16 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
     if (ctx->profile) {
         float p0 = 0;
-        cudaEventElapsedTime(&p0, ctx->ev[0], ctx->pev[4 * MAX_BATCH]);
+        cudaEventElapsedTime(&p0, ctx->ev[0], ctx->pev[6 * MAX_BATCH]);
         ctx->prof.phase2_narrow_ms = p2_ms;
         ctx->prof.phase2_wide_ms = p2w_ms;
         ctx->prof.phase1_ms = p1_ms;
         ctx->prof.setup_ms += p0;
         ctx->prof.phase2_launches = p2_launches;
+        for (int t = 0; t < 4; t++) {
+            ctx->prof.tier_additions[t] = (int64_t)hs.tier_adds[t];
+            ctx->prof.tier_slots[t] = (int64_t)hs.tier_slots[t];
+        }
     }
     if (info) {
         info->sweeps = hs.sweeps;

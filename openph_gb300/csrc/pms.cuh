@@ -1,0 +1,46 @@
+// Shared between the pms driver (pms.cu) and the request server (server.cu).
+#pragma once
+#include "oph_host.h"
+
+namespace oph {
+
+// Device views of one pms reduction.  With `inst` set the columns belong to
+// several independent instances (the server's active requests): each has its
+// own pool region (ipool[2b] = bump pointer, ipool[2b+1] = end), its own
+// repeated-low count per sweep (ireps[b]) and its own overflow flag.
+struct PmsArgs {
+    int64_t m;
+    int32_t *low;
+    int8_t *classes;
+    uint8_t *clear;
+    const int8_t *dim;
+    int32_t *first;
+    const int32_t *beta;
+    int32_t *worklist;
+    int32_t *widelist;
+    int64_t *seg;
+    PivRec *rec;
+    int32_t *agg;
+    int64_t ntiles;
+    int *pool;
+    DevStatus *st;
+    int *inst;                    // per column: instance slot, or nullptr (one instance)
+    unsigned long long *ipool;    // per instance: bump pointer, end
+    int *ireps;                   // per instance: repeated lows seen by the last Phase I
+    int *iover;                   // per instance: a pool allocation failed
+};
+
+// Launch geometry of the Phase II tiers (occupancy-derived, per device).
+struct SweepGrids {
+    int m, t;               // grid of the per-column passes, Phase I tiles
+    int g0, g1, g2, g3;     // Phase II tier grids
+    size_t s0, s1, s2;      // their dynamic shared memory
+};
+
+int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g);
+// One sweep (Phase I, Phase II tiers, sweep counter) on `stream`.
+void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t stream);
+// Phase 0 over columns [c0, c1).
+void launch_phase0(const PmsArgs &a, int64_t c0, int64_t c1, int grid, cudaStream_t stream);
+
+}  // namespace oph

@@ -1,0 +1,585 @@
+// Reduction server with continuous batching.
+//
+// Requests (boundary matrices) are queued by oph_server_submit and reduced by
+// one worker thread that owns a CUDA stream and a fixed device arena (the
+// HBM budget).  All active requests live in ONE block-diagonal column space:
+// request r holds columns [c0, c0 + m) and its rows are shifted by c0, so one
+// pms sweep (pms.cu: Phase I + the Phase II tiers) advances every active
+// request at once.  Between sweeps the worker
+//   * retires every request whose last Phase I found no repeated low (its
+//     lows are final): its lows and ess are copied out and its columns and
+//     pool region are freed;
+//   * admits queued requests, first come first served, while a column range
+//     and a pool region fit in the arena; a request whose column range starts
+//     before another's is still independent (rows of distinct requests are
+//     disjoint and earlier ranges only hold smaller rows);
+//   * regrows the pool region of any request whose column store overflowed
+//     (copy, then rebase its segments and its pivot records).
+// A request therefore joins the running batch at the next sweep boundary and
+// leaves it as soon as it converges.  The reduction of a request is the
+// same whether it runs alone or in the mix: block-diagonal columns never add
+// into each other, and the lows of a reduced matrix are unique.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "pms.cuh"
+
+namespace oph {
+
+namespace {
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// First-fit allocator over [0, cap) with coalescing.
+struct RangeAlloc {
+    std::map<int64_t, int64_t> free;  // start -> length
+    int64_t cap = 0, used = 0;
+    void init(int64_t c) {
+        cap = c;
+        used = 0;
+        free.clear();
+        if (c > 0) free[0] = c;
+    }
+    int64_t alloc(int64_t len, int64_t align) {
+        for (auto it = free.begin(); it != free.end(); ++it) {
+            const int64_t s = (it->first + align - 1) / align * align;
+            const int64_t e = it->first + it->second;
+            if (s + len <= e) {
+                const int64_t fs = it->first;
+                free.erase(it);
+                if (s > fs) free[fs] = s - fs;
+                if (s + len < e) free[s + len] = e - (s + len);
+                used += len;
+                return s;
+            }
+        }
+        return -1;
+    }
+    void release(int64_t s, int64_t len) {
+        used -= len;
+        auto it = free.emplace(s, len).first;
+        auto nx = std::next(it);
+        if (nx != free.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free.erase(nx);
+        }
+        if (it != free.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free.erase(it);
+            }
+        }
+    }
+};
+
+}  // namespace
+
+struct Request {
+    int64_t ticket = 0, m = 0, nnz = 0;
+    std::vector<int64_t> colptr;
+    std::vector<int32_t> rows;
+    std::vector<int32_t> low, ess;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int sweeps = 0, status = OPH_OK, slot = -1;
+    bool done = false;
+    int64_t c0 = -1, reg = -1, reg_ints = 0;
+};
+
+// ------------------------------------------------------------------ kernels
+// Admission: columns [c0, c0+m) of request slot `b`, input staged at
+// colptr/rows (local), segments packed from pool offset `base`.
+__global__ void k_srv_init(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                           int64_t c0, int b, int64_t base, PmsArgs a) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = c0 + jj;
+        const int64_t lo = colptr[jj], hi = colptr[jj + 1];
+        const int64_t s = base + 8 * jj + 4 * ((lo + 3) >> 2);
+        const int64_t e = base + 8 * (jj + 1) + 4 * ((hi + 3) >> 2);
+        const int n = (int)(hi - lo);
+        a.seg[j] = s;
+        a.pool[s] = n;
+        a.pool[s + 1] = (int)(e - s - SEG_HDR);
+        for (int64_t k = lo; k < hi; k++) a.pool[s + SEG_HDR + (k - lo)] = rows[k] + (int32_t)c0;
+        a.low[j] = n > 0 ? rows[hi - 1] + (int32_t)c0 : -1;
+        const_cast<int8_t *>(a.dim)[j] = (int8_t)(n - 1 > 126 ? 126 : n - 1);
+        a.inst[j] = b;
+        a.classes[j] = 0;
+        a.clear[j] = 0;
+        a.first[j] = FIRST_NONE;
+        const_cast<int32_t *>(a.beta)[j] = -1;
+        int4 *r = reinterpret_cast<int4 *>(a.rec + j);
+        r[0] = make_int4(-1, 0, FIRST_NONE, 0);
+        r[1] = make_int4(-1, -1, -1, -1);
+    }
+}
+
+__global__ void k_srv_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                           int64_t c0, PmsArgs a) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t k = colptr[jj]; k < colptr[jj + 1]; k++) atomicMin(&a.rec[rows[k] + c0].left, (int)(c0 + jj));
+}
+
+__global__ void k_srv_beta(int64_t m, int64_t c0, PmsArgs a) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = c0 + jj;
+        const int l = a.rec[i].left;
+        if (l == FIRST_NONE) a.rec[i].left = -1;
+        else atomicMax(const_cast<int32_t *>(a.beta) + l, (int)i);
+    }
+}
+
+// Retirement: local lows and ess of columns [c0, c0+m) into out (2m ints).
+__global__ void k_srv_out1(int64_t m, int64_t c0, PmsArgs a, int32_t *out) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int l = a.low[c0 + jj];
+        out[jj] = l >= 0 ? (int32_t)(l - c0) : -1;
+        out[m + jj] = l >= 0 ? 0 : 1;
+    }
+}
+__global__ void k_srv_out2(int64_t m, int64_t c0, PmsArgs a, int32_t *out) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int l = a.low[c0 + jj];
+        if (l >= 0) out[m + (l - c0)] = 0;
+    }
+}
+// ... then the columns become inert (no low, cleared, no instance).
+__global__ void k_srv_inert(int64_t m, int64_t c0, PmsArgs a) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = c0 + jj;
+        a.low[j] = -1;
+        a.classes[j] = 1;
+        a.clear[j] = 0;
+        a.inst[j] = -1;
+        a.first[j] = FIRST_NONE;
+        int4 *r = reinterpret_cast<int4 *>(a.rec + j);
+        r[0] = make_int4(-1, 0, -1, 0);
+        r[1] = make_int4(-1, -1, -1, -1);
+    }
+}
+
+// Regrow: shift the segments of columns [c0, c0+m) and the segment fields of
+// their rows' pivot records by `delta` ints.
+__global__ void k_srv_rebase(int64_t m, int64_t c0, int64_t delta, PmsArgs a) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = c0 + jj;
+        a.seg[j] += delta;
+        if (a.rec[j].col >= 0) a.rec[j].seg4 = (unsigned)((((long long)a.rec[j].seg4) * 4 + delta) >> 2);
+    }
+}
+
+__global__ void k_srv_set_region(unsigned long long *ipool, int *ireps, int *iover, int b, unsigned long long used,
+                                 unsigned long long end) {
+    ipool[2 * b] = used;
+    ipool[2 * b + 1] = end;
+    ireps[b] = 0;
+    iover[b] = 0;
+}
+
+__global__ void k_srv_sweep_reset(DevStatus *st) {
+    st->converged = 0;
+    st->overflow = 0;
+}
+
+// ------------------------------------------------------------------ server
+struct Server {
+    Context *ctx = nullptr;  // owns the stream and the device buffers
+    int64_t budget = 0, mcap = 0, pool_ints = 0;
+    int max_slots = 0;
+    PmsArgs a{};
+    SweepGrids g{};
+    int *h_ireps = nullptr, *h_iover = nullptr;
+    RangeAlloc cols, pool;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request *> pending;
+    std::map<int64_t, Request *> all;
+    std::vector<Request *> slots;
+    std::thread worker;
+    bool stop = false;
+    int64_t next_ticket = 1;
+    // statistics
+    int64_t completed = 0, sweeps = 0, admitted = 0, regrows = 0;
+    int error = OPH_OK;
+
+    int64_t packed_ints(int64_t m, int64_t nnz) const { return 8 * (m + 1) + 4 * ((nnz + 3) / 4) + 64; }
+    int64_t region_ints(int64_t m, int64_t nnz) const { return packed_ints(m, nnz) * 3 + 4096; }
+
+    int grid(int64_t n) const {
+        int64_t gsz = (n + 255) / 256, cap = (int64_t)ctx->sm_count * 16;
+        return (int)std::max<int64_t>(1, std::min(gsz, cap));
+    }
+
+    // Admission of one request into slot b; called by the worker only.
+    int admit(Request *r, int b) {
+        cudaStream_t s = ctx->stream;
+        const int64_t stage_ints = 2 * (r->m + 1) + r->nnz + 4;
+        const int64_t reg_ints = region_ints(r->m, r->nnz);
+        const int64_t c0 = cols.alloc(std::max<int64_t>(r->m, 1), 1);
+        if (c0 < 0) return 1;
+        const int64_t reg = pool.alloc(reg_ints, 64);
+        if (reg < 0) { cols.release(c0, std::max<int64_t>(r->m, 1)); return 1; }
+        const int64_t stg = pool.alloc(stage_ints, 64);
+        if (stg < 0) {
+            cols.release(c0, std::max<int64_t>(r->m, 1));
+            pool.release(reg, reg_ints);
+            return 1;
+        }
+        r->c0 = c0; r->reg = reg; r->reg_ints = reg_ints; r->slot = b;
+        int64_t *d_colptr = reinterpret_cast<int64_t *>(a.pool + stg);
+        int32_t *d_rows = a.pool + stg + 2 * (r->m + 1);
+        cudaMemcpyAsync(d_colptr, r->colptr.data(), sizeof(int64_t) * (r->m + 1), cudaMemcpyHostToDevice, s);
+        if (r->nnz) cudaMemcpyAsync(d_rows, r->rows.data(), sizeof(int32_t) * r->nnz, cudaMemcpyHostToDevice, s);
+        if (r->m > 0) {
+            k_srv_init<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, b, reg, a);
+            k_srv_left<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, a);
+            k_srv_beta<<<grid(r->m), 256, 0, s>>>(r->m, c0, a);
+        }
+        k_srv_set_region<<<1, 1, 0, s>>>(a.ipool, a.ireps, a.iover, b,
+                                         (unsigned long long)(reg + packed_ints(r->m, r->nnz)),
+                                         (unsigned long long)(reg + reg_ints));
+        if (r->m > 0) launch_phase0(a, c0, c0 + r->m, grid(r->m), s);
+        // the staged input is consumed by the kernels above before the next
+        // host read of the stream, so its region can be reused after that
+        cudaStreamSynchronize(s);
+        pool.release(stg, stage_ints);
+        r->t_admit = now_ms();
+        slots[b] = r;
+        admitted++;
+        return 0;
+    }
+
+    void retire(Request *r) {
+        cudaStream_t s = ctx->stream;
+        const int64_t m = r->m;
+        r->low.resize(m);
+        r->ess.resize(m);
+        if (m > 0) {
+            const int64_t out = pool.alloc(2 * m + 4, 64);
+            int32_t *d_out = a.pool + (out >= 0 ? out : r->reg);  // the request's own region is free to reuse
+            k_srv_out1<<<grid(m), 256, 0, s>>>(m, r->c0, a, d_out);
+            k_srv_out2<<<grid(m), 256, 0, s>>>(m, r->c0, a, d_out);
+            cudaMemcpyAsync(r->low.data(), d_out, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(r->ess.data(), d_out + m, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
+            k_srv_inert<<<grid(m), 256, 0, s>>>(m, r->c0, a);
+            cudaStreamSynchronize(s);
+            if (out >= 0) pool.release(out, 2 * m + 4);
+        }
+        cols.release(r->c0, std::max<int64_t>(m, 1));
+        pool.release(r->reg, r->reg_ints);
+        slots[r->slot] = nullptr;
+        r->t_done = now_ms();
+        r->colptr.clear(); r->colptr.shrink_to_fit();
+        r->rows.clear(); r->rows.shrink_to_fit();
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            r->done = true;
+            completed++;
+        }
+        cv_done.notify_all();
+    }
+
+    // Moves the pool region of request r to one twice as large.
+    int regrow(Request *r) {
+        cudaStream_t s = ctx->stream;
+        unsigned long long reg[2];
+        cudaMemcpy(reg, a.ipool + 2 * r->slot, sizeof(reg), cudaMemcpyDeviceToHost);
+        const int64_t used = std::min<int64_t>((int64_t)reg[0], r->reg + r->reg_ints) - r->reg;
+        const int64_t nints = r->reg_ints * 2;
+        const int64_t nreg = pool.alloc(nints, 64);
+        if (nreg < 0) return OPH_ERR_OOM;
+        cudaMemcpyAsync(a.pool + nreg, a.pool + r->reg, sizeof(int) * used, cudaMemcpyDeviceToDevice, s);
+        if (r->m > 0) k_srv_rebase<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, nreg - r->reg, a);
+        k_srv_set_region<<<1, 1, 0, s>>>(a.ipool, a.ireps, a.iover, r->slot, (unsigned long long)(nreg + used),
+                                         (unsigned long long)(nreg + nints));
+        cudaStreamSynchronize(s);
+        pool.release(r->reg, r->reg_ints);
+        r->reg = nreg;
+        r->reg_ints = nints;
+        regrows++;
+        return OPH_OK;
+    }
+
+    void fail_all(int rc) {
+        std::lock_guard<std::mutex> lk(mu);
+        error = rc;
+        for (auto &kv : all)
+            if (!kv.second->done) {
+                kv.second->status = rc;
+                kv.second->done = true;
+            }
+        cv_done.notify_all();
+    }
+
+    void run() {
+        cudaSetDevice(ctx->device);
+        cudaStream_t s = ctx->stream;
+        for (;;) {
+            // admission, first come first served
+            int active = 0;
+            for (auto *r : slots) active += r != nullptr;
+            for (;;) {
+                Request *r = nullptr;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    if (active == 0)
+                        cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+                    if (stop && pending.empty() && active == 0) return;
+                    if (pending.empty()) break;
+                    r = pending.front();
+                }
+                int b = -1;
+                for (int k = 0; k < max_slots; k++)
+                    if (!slots[k]) { b = k; break; }
+                if (b < 0 || admit(r, b) != 0) break;  // no room now: retry after the next sweep
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    pending.pop_front();
+                }
+                active++;
+            }
+            if (active == 0) {
+                if (!pending.empty()) {
+                    // the head request cannot fit even in an empty arena
+                    std::lock_guard<std::mutex> lk(mu);
+                    Request *r = pending.front();
+                    pending.pop_front();
+                    r->status = OPH_ERR_OOM;
+                    r->done = true;
+                    cv_done.notify_all();
+                }
+                continue;
+            }
+            // one sweep over every active request
+            int64_t hi = 0;
+            for (auto *r : slots)
+                if (r) hi = std::max(hi, r->c0 + std::max<int64_t>(r->m, 1));
+            PmsArgs sa = a;
+            sa.m = hi;
+            sa.ntiles = (hi + 2047) / 2048;
+            SweepGrids gg = g;
+            gg.m = grid(hi);
+            gg.t = (int)std::max<int64_t>(1, sa.ntiles);
+            cudaMemsetAsync(a.ireps, 0, sizeof(int) * max_slots, s);
+            k_srv_sweep_reset<<<1, 1, 0, s>>>(a.st);
+            launch_sweep(sa, gg, s);
+            cudaMemcpyAsync(h_ireps, a.ireps, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(h_iover, a.iover, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess) {
+                fail_all(OPH_ERR_CUDA);
+                return;
+            }
+            sweeps++;
+            for (auto *r : slots)
+                if (r) r->sweeps++;
+            // regrow first: an overflowed request is not converged
+            for (int b = 0; b < max_slots; b++)
+                if (slots[b] && h_iover[b]) {
+                    if (regrow(slots[b]) != OPH_OK) {
+                        fail_all(OPH_ERR_OOM);
+                        return;
+                    }
+                }
+            for (int b = 0; b < max_slots; b++)
+                if (slots[b] && h_ireps[b] == 0 && !h_iover[b]) retire(slots[b]);
+        }
+    }
+};
+
+}  // namespace oph
+
+using namespace oph;
+
+struct oph_server : public oph::Server {};
+
+extern "C" {
+
+__attribute__((visibility("default"))) int oph_server_create(int device, int64_t budget_bytes, int32_t max_active,
+                                                             oph_server **out) {
+    if (!out || budget_bytes < (int64_t)(64 << 20) || max_active < 1 || max_active > 65536) return OPH_ERR_BAD_INPUT;
+    *out = nullptr;
+    oph_server *sv = new oph_server();
+    oph_context *raw = nullptr;
+    int rc = oph_context_create(device, &raw);
+    if (rc) {
+        delete sv;
+        return rc;
+    }
+    sv->ctx = reinterpret_cast<Context *>(raw);
+    Context *ctx = sv->ctx;
+    sv->budget = budget_bytes;
+    sv->max_slots = max_active;
+    // the arena: per-column arrays for mcap columns (a tenth of the budget)
+    // and a segment pool for the rest (at most what 32-bit segment fields
+    // address)
+    const int64_t per_col = 4 + 1 + 1 + 1 + 4 + 4 + 4 + 4 + 8 + (int64_t)sizeof(PivRec) + 4;
+    sv->mcap = std::min<int64_t>(budget_bytes / 10 / per_col, (1ll << 29) - 1);
+    int64_t pool_bytes = budget_bytes - sv->mcap * per_col - (64 << 20);
+    sv->pool_ints = std::min<int64_t>(pool_bytes / 4 - POOL_PAD, MAX_POOL_INTS - 1);
+    const int64_t mc = sv->mcap;
+    PmsArgs &a = sv->a;
+    a.low = (int32_t *)ctx_alloc(ctx, S_LOW, 4 * mc);
+    a.classes = (int8_t *)ctx_alloc(ctx, S_CLASSES, mc);
+    a.clear = (uint8_t *)ctx_alloc(ctx, S_CLEAR, mc);
+    a.dim = (int8_t *)ctx_alloc(ctx, S_DIM, mc);
+    a.first = (int32_t *)ctx_alloc(ctx, S_FIRST, 4 * mc);
+    a.beta = (int32_t *)ctx_alloc(ctx, S_BETA, 4 * mc);
+    a.worklist = (int32_t *)ctx_alloc(ctx, S_WORK, 4 * mc);
+    a.widelist = (int32_t *)ctx_alloc(ctx, S_WIDE, 4 * mc);
+    a.seg = (int64_t *)ctx_alloc(ctx, S_SEG, 8 * mc);
+    a.rec = (PivRec *)ctx_alloc(ctx, S_ROWPIV, sizeof(PivRec) * mc);
+    a.inst = (int *)ctx_alloc(ctx, S_LOWTRUE, 4 * mc);
+    a.agg = (int32_t *)ctx_alloc(ctx, S_AGG, sizeof(int32_t) * MAXC * ((mc + 2047) / 2048 + 1));
+    a.ipool = (unsigned long long *)ctx_alloc(ctx, S_INSTOFF, 16 * (size_t)max_active);
+    a.ireps = (int *)ctx_alloc(ctx, S_TRACK, 4 * (size_t)max_active);
+    a.iover = (int *)ctx_alloc(ctx, S_TMP, 4 * (size_t)max_active);
+    a.st = (DevStatus *)ctx_alloc(ctx, S_STATUS, sizeof(DevStatus));
+    a.pool = (int *)ctx_alloc(ctx, S_POOL, sizeof(int) * (sv->pool_ints + POOL_PAD));
+    bool ok = a.low && a.classes && a.clear && a.dim && a.first && a.beta && a.worklist && a.widelist && a.seg &&
+              a.rec && a.inst && a.agg && a.ipool && a.ireps && a.iover && a.st && a.pool;
+    if (ok) ok = cudaMallocHost((void **)&sv->h_ireps, 4 * (size_t)max_active) == cudaSuccess &&
+                 cudaMallocHost((void **)&sv->h_iover, 4 * (size_t)max_active) == cudaSuccess;
+    if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
+    if (!ok) {
+        if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
+        if (sv->h_iover) cudaFreeHost(sv->h_iover);
+        oph_context_destroy(raw);
+        delete sv;
+        return OPH_ERR_OOM;
+    }
+    cudaStream_t s = ctx->stream;
+    // every column starts inert
+    cudaMemsetAsync(a.low, 0xff, 4 * mc, s);
+    cudaMemsetAsync(a.classes, 1, mc, s);
+    cudaMemsetAsync(a.clear, 0, mc, s);
+    cudaMemsetAsync(a.inst, 0xff, 4 * mc, s);
+    cudaMemsetAsync(a.first, 0x7f, 4 * mc, s);
+    cudaMemsetAsync(a.iover, 0, 4 * (size_t)max_active, s);
+    k_srv_inert<<<sv->grid(mc), 256, 0, s>>>(mc, 0, a);
+    DevStatus init{};
+    init.pool_used = 0;
+    init.pool_size = (unsigned long long)sv->pool_ints;
+    cudaMemcpyAsync(a.st, &init, sizeof(init), cudaMemcpyHostToDevice, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+        oph_context_destroy(raw);
+        delete sv;
+        return OPH_ERR_CUDA;
+    }
+    sv->cols.init(mc);
+    sv->pool.init(sv->pool_ints);
+    sv->slots.assign(max_active, nullptr);
+    sv->worker = std::thread([sv] { sv->run(); });
+    *out = sv;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_server_submit(oph_server *sv, int64_t m, const int64_t *colptr,
+                                                             const int32_t *rows, int64_t *ticket) {
+    if (!sv || m < 0 || !colptr || !ticket || colptr[0] != 0) return OPH_ERR_BAD_INPUT;
+    const int64_t nnz = colptr[m];
+    if (nnz < 0 || (nnz > 0 && !rows)) return OPH_ERR_BAD_INPUT;
+    if (m > sv->mcap || sv->region_ints(m, nnz) + 2 * (m + 1) + nnz > sv->pool_ints) return OPH_ERR_OOM;
+    // the same structural checks as the single-matrix path, on the host
+    for (int64_t j = 0; j < m; j++) {
+        if (colptr[j + 1] < colptr[j]) return OPH_ERR_BAD_INPUT;
+        int prev = -1;
+        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) {
+            if (rows[k] <= prev || rows[k] >= m) return OPH_ERR_BAD_INPUT;
+            prev = rows[k];
+        }
+        if (colptr[j + 1] - colptr[j] > MAXC - 1) return OPH_ERR_BAD_INPUT;
+    }
+    Request *r = new Request();
+    r->m = m;
+    r->nnz = nnz;
+    r->colptr.assign(colptr, colptr + m + 1);
+    if (nnz) r->rows.assign(rows, rows + nnz);
+    r->t_submit = now_ms();
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->error) {
+            delete r;
+            return sv->error;
+        }
+        r->ticket = sv->next_ticket++;
+        sv->all[r->ticket] = r;
+        sv->pending.push_back(r);
+        *ticket = r->ticket;
+    }
+    sv->cv_work.notify_one();
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_server_wait(oph_server *sv, int64_t ticket, int32_t *low,
+                                                           int32_t *ess, oph_request_info *info, int64_t timeout_ms) {
+    if (!sv) return OPH_ERR_BAD_INPUT;
+    std::unique_lock<std::mutex> lk(sv->mu);
+    auto it = sv->all.find(ticket);
+    if (it == sv->all.end()) return OPH_ERR_BAD_INPUT;
+    Request *r = it->second;
+    auto ready = [&] { return r->done; };
+    if (timeout_ms < 0) sv->cv_done.wait(lk, ready);
+    else if (!sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready)) return OPH_ERR_TIMEOUT;
+    sv->all.erase(it);
+    lk.unlock();
+    const int rc = r->status;
+    if (rc == OPH_OK && r->m > 0) {
+        if (low) memcpy(low, r->low.data(), sizeof(int32_t) * r->m);
+        if (ess) memcpy(ess, r->ess.data(), sizeof(int32_t) * r->m);
+    }
+    if (info) {
+        info->latency_ms = r->t_done - r->t_submit;
+        info->queue_ms = r->t_admit > 0 ? r->t_admit - r->t_submit : 0;
+        info->sweeps = r->sweeps;
+        info->status = rc;
+        info->m = r->m;
+        info->submit_ms = r->t_submit;
+        info->done_ms = r->t_done;
+    }
+    delete r;
+    return rc;
+}
+
+__attribute__((visibility("default"))) int oph_server_stats(oph_server *sv, oph_server_counters *out) {
+    if (!sv || !out) return OPH_ERR_BAD_INPUT;
+    std::lock_guard<std::mutex> lk(sv->mu);
+    int active = 0;
+    for (auto *r : sv->slots) active += r != nullptr;
+    out->completed = sv->completed;
+    out->pending = (int64_t)sv->pending.size();
+    out->active = active;
+    out->sweeps = sv->sweeps;
+    out->regrows = sv->regrows;
+    out->pool_bytes_in_use = sv->pool.used * 4;
+    out->columns_in_use = sv->cols.used;
+    out->arena_bytes = sv->budget;
+    return OPH_OK;
+}
+
+__attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
+    if (!sv) return OPH_OK;
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv_work.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    for (auto &kv : sv->all) delete kv.second;
+    if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
+    if (sv->h_iover) cudaFreeHost(sv->h_iover);
+    oph_context_destroy(reinterpret_cast<oph_context *>(sv->ctx));
+    delete sv;
+    return OPH_OK;
+}
+
+}  // extern "C"

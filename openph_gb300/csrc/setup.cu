@@ -65,19 +65,24 @@ __global__ void k_setup_columns(const int64_t *__restrict__ colptr, const int32_
     }
 }
 
-// left[i] = first column holding row i (atomicMin over the entries).
+// left[i] = first column holding row i (atomicMin over the entries, into
+// the pivot records, which start as the 0x7f byte pattern).
 __global__ void k_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                       int32_t *__restrict__ left) {
+                       PivRec *__restrict__ rec) {
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
-        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) atomicMin(&left[rows[k]], (int)j);
+        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) atomicMin(&rec[rows[k]].left, (int)j);
 }
 
-// beta[j] = largest row whose first column is j; left[] := -1 where unset.
-__global__ void k_beta(int32_t *__restrict__ left, int64_t m, int32_t *__restrict__ beta) {
+// beta[j] = largest row whose first column is j; each record is then set to
+// "no pivot" with its left (-1 where no column holds the row).
+__global__ void k_beta(PivRec *__restrict__ rec, int64_t m, int32_t *__restrict__ beta) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
-        int l = left[i];
-        if (l == FIRST_NONE) left[i] = -1;
+        int l = rec[i].left;
+        if (l == FIRST_NONE) l = -1;
         else atomicMax(&beta[l], (int)i);
+        int4 *r = reinterpret_cast<int4 *>(rec + i);
+        r[0] = make_int4(-1, 0, l, 0);
+        r[1] = make_int4(-1, -1, -1, -1);
     }
 }
 
@@ -129,10 +134,10 @@ int setup_store(Context *ctx, Work &w, bool need_beta) {
                                                                     w.st);
     OPH_CUDA_TRY(cudaGetLastError());
     if (need_beta) {
-        OPH_CUDA_TRY(cudaMemsetAsync(w.left, 0x7f, sizeof(int32_t) * m, ctx->stream));
+        OPH_CUDA_TRY(cudaMemsetAsync(w.rec, 0x7f, sizeof(PivRec) * m, ctx->stream));
         OPH_CUDA_TRY(cudaMemsetAsync(w.beta, 0xff, sizeof(int32_t) * m, ctx->stream));
-        k_left<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.left);
-        k_beta<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.left, m, w.beta);
+        k_left<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.rec);
+        k_beta<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.rec, m, w.beta);
         OPH_CUDA_TRY(cudaGetLastError());
     }
     return OPH_OK;
@@ -148,7 +153,7 @@ int grow_pool(Context *ctx, Work &w) {
     int64_t used = (int64_t)(hs.pool_used < hs.pool_size ? hs.pool_used : hs.pool_size);
     int64_t want = ctx->pool_ints * 2;
     if (want < used + (16 << 20)) want = used + (16 << 20);
-    if (want >= (int64_t)(PIV_OFF_MASK << 2)) return OPH_ERR_OVERFLOW;
+    if (want >= MAX_POOL_INTS) return OPH_ERR_OVERFLOW;
     int *np = (int *)ctx_alloc(ctx, S_POOL2, sizeof(int) * (want + POOL_PAD));
     if (!np) return OPH_ERR_OOM;
     OPH_CUDA_TRY(cudaMemcpyAsync(np, w.pool, sizeof(int) * used, cudaMemcpyDeviceToDevice, ctx->stream));

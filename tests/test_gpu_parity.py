@@ -153,3 +153,23 @@ def test_zero_columns(cuda_lib):
         low, ess, *_ = ph(algo, np.zeros(0, np.int32), np.zeros(0, np.int32), 4, 3)
         np.testing.assert_array_equal(low, np.zeros(4, np.int32))
         np.testing.assert_array_equal(ess, np.ones(4, np.int32))
+
+
+@pytest.mark.parametrize("algo", ["pms", "twist"])
+def test_lower_star_512_full_size(ctx, algo):
+    """The 512 x 512 lower-star configuration (1,568,771 columns), bit-exact."""
+    bm = cx.lower_star_image(512, 512, seed=3)
+    want, want_ess, _ = oracle.twist(bm)
+    low, ess, _ = ctx.reduce(bm, algo)
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_rips_torus_1m(ctx):
+    """A 1M-column torus Rips complex (the 5M configuration's family)."""
+    bm = cx.rips_torus(400, 1_000_000, seed=2)
+    want, want_ess, _ = oracle.twist(bm)
+    low, ess, info = ctx.reduce(bm, "pms")
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+    assert info["regrows"] == 0
