@@ -198,6 +198,18 @@ int oph_context_set_profile(oph_context *ctx, int on);
 /* Per-phase device times and launch counts of the last reduction on ctx. */
 int oph_last_profile(oph_context *ctx, oph_profile *out);
 
+/* Autotuning of the pms Phase II narrow tier (lanes per column and shared
+ * staging capacity).  oph_context_autotune reduces the given host CSC matrix
+ * once per candidate (after one warm-up) and keeps the fastest for later
+ * reductions on ctx; oph_context_autotune_batch does the same on a batch.
+ * lanes/cap/best_ms receive the choice (each may be NULL). */
+int oph_context_autotune(oph_context *ctx, int64_t m, const int64_t *colptr, const int32_t *rows, int32_t *lanes,
+                         int32_t *cap, float *best_ms);
+int oph_context_autotune_batch(oph_context *ctx, int32_t count, const int64_t *col_off, const int64_t *colptr,
+                               const int32_t *rows, int32_t *lanes, int32_t *cap, float *best_ms);
+/* Set the narrow-tier configuration directly (must be a candidate). */
+int oph_context_set_tier0(oph_context *ctx, int32_t lanes, int32_t cap);
+
 /* Testing hooks: cap the sweep count (0 = default) and the initial column
  * store size in bytes (0 = default), to exercise the timeout and regrow
  * paths without faulting anything. */

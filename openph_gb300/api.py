@@ -113,6 +113,11 @@ def lib():
         L.oph_server_stats.argtypes = [vp, C.POINTER(ServerCounters)]
         L.oph_server_destroy.argtypes = [vp]
         L.oph_context_set_profile.argtypes = [vp, C.c_int]
+        L.oph_context_autotune.argtypes = [vp, C.c_int64, i64, vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_float)]
+        L.oph_context_autotune_batch.argtypes = [vp, C.c_int32, i64, i64, vp, C.POINTER(C.c_int32),
+                                                 C.POINTER(C.c_int32), C.POINTER(C.c_float)]
+        L.oph_context_set_tier0.argtypes = [vp, C.c_int32, C.c_int32]
         L.oph_last_profile.argtypes = [vp, C.POINTER(Profile)]
         _lib = L
     return _lib
@@ -290,6 +295,30 @@ class Context:
         if rc != OPH_OK:
             raise OphError(rc, f"oph_reduce_batch_device({algo!r})")
         return info.as_dict()
+
+    def autotune(self, bm):
+        """Pick the narrow-tier lanes/capacity on a representative matrix."""
+        lanes, cap, ms = C.c_int32(), C.c_int32(), C.c_float()
+        rc = lib().oph_context_autotune(self._h, bm.m, bm.colptr, _ptr(bm.rows if bm.nnz else None),
+                                        C.byref(lanes), C.byref(cap), C.byref(ms))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_context_autotune")
+        return {"lanes": lanes.value, "cap": cap.value, "ms": ms.value}
+
+    def autotune_batch(self, col_off, colptr, rows):
+        lanes, cap, ms = C.c_int32(), C.c_int32(), C.c_float()
+        rows = np.ascontiguousarray(rows, np.int32)
+        rc = lib().oph_context_autotune_batch(self._h, len(col_off) - 1, np.ascontiguousarray(col_off, np.int64),
+                                              np.ascontiguousarray(colptr, np.int64), _ptr(rows), C.byref(lanes),
+                                              C.byref(cap), C.byref(ms))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_context_autotune_batch")
+        return {"lanes": lanes.value, "cap": cap.value, "ms": ms.value}
+
+    def set_tier0(self, lanes: int, cap: int):
+        rc = lib().oph_context_set_tier0(self._h, int(lanes), int(cap))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_context_set_tier0")
 
     def set_profile(self, on: bool = True):
         lib().oph_context_set_profile(self._h, 1 if on else 0)

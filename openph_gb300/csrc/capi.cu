@@ -11,8 +11,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "oph_host.h"
+#include "pms.cuh"
 
 using namespace oph;
 
@@ -593,6 +595,84 @@ __attribute__((visibility("default"))) void openph(char *algstr, int *h_rows_in,
         if (h_low)
             for (int i = 0; i < m; i++) h_low[i] = 0;
     }
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------- autotune
+static int autotune_run(oph_context *ctx, int32_t *lanes, int32_t *cap, float *best_ms,
+                        int (*run)(oph_context *, void *), void *arg) {
+    int best = -1;
+    float best_t = 0;
+    for (int v = 0; v < T0_CANDIDATES; v++) {
+        ctx->tier0 = v;
+        int rc = run(ctx, arg);  // warm-up (and set-up of the candidate)
+        if (rc) return rc;
+        cudaEventRecord(ctx->ev[4], ctx->stream);
+        rc = run(ctx, arg);
+        if (rc) return rc;
+        cudaEventRecord(ctx->ev[5], ctx->stream);
+        cudaEventSynchronize(ctx->ev[5]);
+        float t = 0;
+        cudaEventElapsedTime(&t, ctx->ev[4], ctx->ev[5]);
+        if (best < 0 || t < best_t) { best = v; best_t = t; }
+    }
+    ctx->tier0 = best;
+    int l = 0, c = 0;
+    t0_candidate(best, &l, &c);
+    if (lanes) *lanes = l;
+    if (cap) *cap = c;
+    if (best_ms) *best_ms = best_t;
+    return OPH_OK;
+}
+
+struct TuneOne { int64_t m; const int64_t *colptr; const int32_t *rows; int32_t *low; };
+struct TuneBatch { int32_t count; const int64_t *col_off, *colptr; const int32_t *rows; int32_t *low; };
+
+extern "C" {
+
+__attribute__((visibility("default"))) int oph_context_set_tier0(oph_context *ctx, int32_t lanes, int32_t cap) {
+    if (!ctx) return OPH_ERR_BAD_INPUT;
+    for (int v = 0; v < T0_CANDIDATES; v++) {
+        int l, c;
+        t0_candidate(v, &l, &c);
+        if (l == lanes && c == cap) {
+            ctx->tier0 = v;
+            return OPH_OK;
+        }
+    }
+    return OPH_ERR_BAD_INPUT;
+}
+
+__attribute__((visibility("default"))) int oph_context_autotune(oph_context *ctx, int64_t m, const int64_t *colptr,
+                                                                const int32_t *rows, int32_t *lanes, int32_t *cap,
+                                                                float *best_ms) {
+    if (!ctx || m < 0 || !colptr) return OPH_ERR_BAD_INPUT;
+    std::vector<int32_t> low(m > 0 ? m : 1);
+    TuneOne t{m, colptr, rows, low.data()};
+    return autotune_run(ctx, lanes, cap, best_ms,
+                        [](oph_context *c, void *p) {
+                            TuneOne *a = (TuneOne *)p;
+                            return oph_reduce(c, OPH_ALGO_PMS, a->m, a->colptr, a->rows, a->low, nullptr, nullptr,
+                                              nullptr);
+                        },
+                        &t);
+}
+
+__attribute__((visibility("default"))) int oph_context_autotune_batch(oph_context *ctx, int32_t count,
+                                                                      const int64_t *col_off, const int64_t *colptr,
+                                                                      const int32_t *rows, int32_t *lanes,
+                                                                      int32_t *cap, float *best_ms) {
+    if (!ctx || count < 1 || !col_off || !colptr) return OPH_ERR_BAD_INPUT;
+    std::vector<int32_t> low(col_off[count] > 0 ? col_off[count] : 1);
+    TuneBatch t{count, col_off, colptr, rows, low.data()};
+    return autotune_run(ctx, lanes, cap, best_ms,
+                        [](oph_context *c, void *p) {
+                            TuneBatch *a = (TuneBatch *)p;
+                            return oph_reduce_batch(c, OPH_ALGO_PMS, a->count, a->col_off, a->colptr, a->rows,
+                                                    a->low, nullptr, nullptr);
+                        },
+                        &t);
 }
 
 }  // extern "C"

@@ -83,6 +83,7 @@ struct Context {
     int pev_n = 0;
     oph_profile prof{};             // last reduction
     int launches = 0;               // kernels launched by the current reduction
+    int tier0 = 0;                  // Phase II tier-0 candidate (autotuned)
 };
 
 // buffer slots of Context::bufs

@@ -573,12 +573,53 @@ static int fill_grid(Context *ctx, K kernel, int block, size_t smem, int *done) 
     return ctx->sm_count * (nb < 1 ? 1 : nb);
 }
 
+// Tier-0 candidates for the autotuner: lanes per column x shared capacity.
+// Candidate 0 is the default.
+struct T0Cand {
+    int lanes, cap;
+};
+static const T0Cand kT0[T0_CANDIDATES] = {{8, 128}, {4, 128}, {8, 64}, {8, 256}, {16, 128}, {16, 256}};
+
+template <int G, int CAP>
+static int t0_grid(Context *ctx, size_t *smem) {
+    static int done[64];
+    *smem = (size_t)(T0_BLOCK / G) * 2 * CAP * sizeof(int);
+    return fill_grid(ctx, k_p2_tier<G, CAP, T0_BLOCK, false>, T0_BLOCK, *smem, done);
+}
+static int t0_grid_of(Context *ctx, int v, size_t *smem) {
+    switch (v) {
+        case 1: return t0_grid<4, 128>(ctx, smem);
+        case 2: return t0_grid<8, 64>(ctx, smem);
+        case 3: return t0_grid<8, 256>(ctx, smem);
+        case 4: return t0_grid<16, 128>(ctx, smem);
+        case 5: return t0_grid<16, 256>(ctx, smem);
+        default: return t0_grid<8, 128>(ctx, smem);
+    }
+}
+static void launch_t0(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) {
+    switch (g.v0) {
+        case 1: k_p2_tier<4, 128, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+        case 2: k_p2_tier<8, 64, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+        case 3: k_p2_tier<8, 256, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+        case 4: k_p2_tier<16, 128, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+        case 5: k_p2_tier<16, 256, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+        default: k_p2_tier<8, 128, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+    }
+}
+
+int t0_candidate(int v, int *lanes, int *cap) {
+    if (v < 0 || v >= T0_CANDIDATES) return -1;
+    *lanes = kT0[v].lanes;
+    *cap = kT0[v].cap;
+    return 0;
+}
+
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
-    static int done0[64], done1[64], done2[64];
-    g->s0 = (size_t)(T0_BLOCK / T0_G) * 2 * T0_CAP * sizeof(int);
+    static int done1[64], done2[64];
+    g->v0 = (ctx->tier0 >= 0 && ctx->tier0 < T0_CANDIDATES) ? ctx->tier0 : 0;
     g->s1 = (size_t)(T1_BLOCK / T1_G) * 3 * T1_CAP * sizeof(int);
     g->s2 = (size_t)3 * T2_CAP * sizeof(int);
-    g->g0 = fill_grid(ctx, k_p2_tier<T0_G, T0_CAP, T0_BLOCK, false>, T0_BLOCK, g->s0, done0);
+    g->g0 = t0_grid_of(ctx, g->v0, &g->s0);
     g->g1 = fill_grid(ctx, k_p2_tier<T1_G, T1_CAP, T1_BLOCK, true>, T1_BLOCK, g->s1, done1);
     g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
     g->g3 = ctx->sm_count * 2;
@@ -604,7 +645,7 @@ static void launch_sweep_ev(const PmsArgs &a, const SweepGrids &g, cudaStream_t 
     k_p1_mark<<<g.t, P1_THREADS, 0, s>>>(a);
     k_p1_worklist<<<g.m, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
-    k_p2_tier<T0_G, T0_CAP, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0);
+    launch_t0(a, g, s);
     if (ev) cudaEventRecord(ev[2], s);
     k_p2_tier<T1_G, T1_CAP, T1_BLOCK, true><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
     if (ev) cudaEventRecord(ev[3], s);

@@ -31,7 +31,12 @@ struct PmsArgs {
 };
 
 // Launch geometry of the Phase II tiers (occupancy-derived, per device).
+constexpr int T0_CANDIDATES = 6;
+// Lanes per column and shared capacity of tier-0 candidate v (-1 if none).
+int t0_candidate(int v, int *lanes, int *cap);
+
 struct SweepGrids {
+    int v0;                 // tier-0 candidate in use
     int m, t;               // grid of the per-column passes, Phase I tiles
     int g0, g1, g2, g3;     // Phase II tier grids
     size_t s0, s1, s2;      // their dynamic shared memory

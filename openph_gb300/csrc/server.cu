@@ -424,7 +424,7 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     // address)
     const int64_t per_col = 4 + 1 + 1 + 1 + 4 + 4 + 4 + 4 + 8 + (int64_t)sizeof(PivRec) + 4;
     sv->mcap = std::min<int64_t>(budget_bytes / 10 / per_col, (1ll << 29) - 1);
-    int64_t pool_bytes = budget_bytes - sv->mcap * per_col - (64 << 20);
+    int64_t pool_bytes = budget_bytes - sv->mcap * per_col - budget_bytes / 16;
     sv->pool_ints = std::min<int64_t>(pool_bytes / 4 - POOL_PAD, MAX_POOL_INTS - 1);
     const int64_t mc = sv->mcap;
     PmsArgs &a = sv->a;

@@ -173,3 +173,27 @@ def test_rips_torus_1m(ctx):
     np.testing.assert_array_equal(low, want)
     np.testing.assert_array_equal(ess, want_ess)
     assert info["regrows"] == 0
+
+
+@pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256)])
+def test_every_tier0_candidate_is_exact(cuda_lib, lanes, cap):
+    from openph_gb300.api import Context
+    bm = cx.lower_star_image(48, 48, seed=6, sigma=3.0)
+    want, want_ess, _ = oracle.twist(bm)
+    with Context(0) as c:
+        c.set_tier0(lanes, cap)
+        low, ess, _ = c.reduce(bm, "pms")
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_autotune_picks_a_candidate(cuda_lib):
+    from openph_gb300.api import Context
+    bm = cx.rips_cube(30, seed=4)
+    with Context(0) as c:
+        choice = c.autotune(bm)
+        assert (choice["lanes"], choice["cap"]) in {(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256)}
+        low, _, _ = c.reduce(bm, "pms")
+    np.testing.assert_array_equal(low, oracle.twist(bm)[0])
+    with pytest.raises(OphError):
+        Context(0).set_tier0(3, 100)
