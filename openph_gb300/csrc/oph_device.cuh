@@ -61,6 +61,7 @@ struct DevStatus {
     long long resume_pos;          //   (column or row index; -1 = finished)
     int max_dim;                   // largest nnz(col) - 1 seen by the set-up
     int pad;
+    int ucount[2];                     // compacted Phase I: list sizes (ping-pong)
     unsigned long long tier_adds[4];   // additions performed by each Phase II tier
     unsigned long long tier_slots[4];  // |P| + |T| + |T xor P| summed per tier
 };

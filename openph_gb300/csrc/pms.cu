@@ -54,6 +54,21 @@ __global__ void k_phase0(PmsArgs a, int64_t c0, int64_t c1) {
 }
 
 // --------------------------------------------------------------- Phase I
+// The columns a Phase I pass visits: with a compacted list, its U entries in
+// column order (only unresolved columns can repeat a low or become new
+// pivots: a pivot always holds the first occurrence of its low and a cleared
+// or zero column has none); without one, all m columns.
+__device__ __forceinline__ int64_t p1_count(const PmsArgs &a) { return a.ulist ? (int64_t)*a.ucur : a.m; }
+__device__ __forceinline__ int64_t p1_col(const PmsArgs &a, int64_t idx) {
+    return a.ulist ? (int64_t)a.ulist[idx] : idx;
+}
+// Another column to the left holds the same low: a published pivot, or an
+// earlier column recorded in first[].
+__device__ __forceinline__ bool is_repeat(const PmsArgs &a, int64_t j, int lj) {
+    const int pc = a.rec[lj].col;
+    return (pc >= 0 && pc < (int)j) || a.first[lj] != (int)j;
+}
+
 // (a) apply pending clears (clear_positives, pms_functions.cu:131-140) and
 //     record the first column of every low.
 __global__ void k_p1_first(PmsArgs a) {
@@ -63,7 +78,10 @@ __global__ void k_p1_first(PmsArgs a) {
         a.st->wl_count = 0;
         for (int t = 0; t < 4; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
     }
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.m; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = p1_count(a);
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = p1_col(a, idx);
         int lj = a.low[j];
         if (a.clear[j]) {
             a.clear[j] = 0;
@@ -86,9 +104,12 @@ __device__ __forceinline__ int warp_max(int v) {
     return v;
 }
 
-// (b) per-tile maxima of repeated lows, per dimension bucket; counts repeats.
+// (b) per-tile maxima of repeated lows, per dimension bucket; counts repeats
+//     (per instance too, when the columns belong to several).
 __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
     if (a.st->converged) return;
+    const int64_t n = p1_count(a);
+    if ((int64_t)blockIdx.x * P1_TILE >= n) return;
     __shared__ int sm[P1_THREADS / 32][MAXC];
     __shared__ int sreps;
     if (threadIdx.x == 0) sreps = 0;
@@ -100,11 +121,12 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
     const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
-        int64_t j = base + t;
-        if (j < a.m) {
-            int lj = a.low[j];
-            if (lj >= 0 && a.first[lj] != (int)j) {
-                int b = a.dim[j] + 1;
+        const int64_t idx = base + t;
+        if (idx < n) {
+            const int64_t j = p1_col(a, idx);
+            const int lj = a.low[j];
+            if (lj >= 0 && is_repeat(a, j, lj)) {
+                const int b = a.dim[j] + 1;
 #pragma unroll
                 for (int d = 0; d < MAXC; d++)
                     if (d == b) mx[d] = max(mx[d], lj);
@@ -148,7 +170,7 @@ __global__ void k_p1_scan(PmsArgs a) {
     }
     const int d = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (d >= MAXC) return;
-    const int64_t n = a.ntiles;
+    const int64_t n = (p1_count(a) + P1_TILE - 1) / P1_TILE;
     const int64_t chunk = (n + 31) / 32;
     const int64_t lo = lane * chunk, hi = min(n, lo + chunk);
     int local = -1;
@@ -170,10 +192,15 @@ __global__ void k_p1_scan(PmsArgs a) {
 }
 
 // (d) mark pivots: first for its low, unclassified, low above the running
-//     ceiling of repeated lows in its bucket.
+//     ceiling of repeated lows in its bucket.  With a compacted list, also
+//     count per tile the columns that stay unresolved.
 __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
     if (a.st->converged) return;
+    const int64_t n = p1_count(a);
+    if ((int64_t)blockIdx.x * P1_TILE >= n) return;
     __shared__ int sm[P1_THREADS / 32][MAXC];
+    __shared__ int skeep;
+    if (threadIdx.x == 0) skeep = 0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
     int lows[P1_ITEMS], bkt[P1_ITEMS];
@@ -183,13 +210,14 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
     for (int d = 0; d < MAXC; d++) mx[d] = -1;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
-        int64_t j = base + t;
+        const int64_t idx = base + t;
         lows[t] = -1; bkt[t] = 0; rep[t] = false;
-        if (j < a.m) {
-            int lj = a.low[j];
+        if (idx < n) {
+            const int64_t j = p1_col(a, idx);
+            const int lj = a.low[j];
             lows[t] = lj;
             bkt[t] = a.dim[j] + 1;
-            if (lj >= 0 && a.first[lj] != (int)j) {
+            if (lj >= 0 && is_repeat(a, j, lj)) {
                 rep[t] = true;
 #pragma unroll
                 for (int d = 0; d < MAXC; d++)
@@ -218,31 +246,121 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
         for (int w = 0; w < wid; w++) c = max(c, sm[w][d]);
         pre[d] = max(pre[d], c);
     }
+    int keep = 0;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
-        int64_t j = base + t;
-        if (j >= a.m) break;
-        int lj = lows[t];
+        const int64_t idx = base + t;
+        if (idx >= n) break;
+        const int64_t j = p1_col(a, idx);
+        const int lj = lows[t];
         if (lj < 0) continue;
         int ceil = -1;
 #pragma unroll
         for (int d = 0; d < MAXC; d++)
             if (d == bkt[t]) ceil = pre[d];
+        const int cls = a.classes[j];
         if (rep[t]) {
 #pragma unroll
             for (int d = 0; d < MAXC; d++)
                 if (d == bkt[t]) pre[d] = max(pre[d], lj);
-        } else if (a.classes[j] == 0 && lj > ceil) {
+            keep += cls == 0;
+        } else if (cls == 0 && lj > ceil) {
             a.classes[j] = -1;
             const long long sj = a.seg[j];
             rec_publish<false>(a.rec, lj, (int)j, a.pool[sj], sj, a.pool + sj + SEG_HDR);
             a.clear[lj] = 1;
+        } else {
+            keep += cls == 0;
         }
+    }
+    if (a.ulist) {
+        if (keep) atomicAdd(&skeep, keep);
+        __syncthreads();
+        if (threadIdx.x == 0) a.kagg[blockIdx.x] = skeep;
     }
 }
 
-// (e) reset first[], apply the clears of this Phase I, and compact the
-//     unresolved columns (unclassified, nonzero low) into the worklist.
+// (e) compacted list: exclusive scan of the per-tile counts (one block).
+__global__ void k_p1_kscan(PmsArgs a) {
+    if (a.st->converged) return;
+    __shared__ int wsum[32];
+    const int64_t n = (p1_count(a) + P1_TILE - 1) / P1_TILE;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int carry = 0;
+    for (int64_t b0 = 0; b0 < n; b0 += blockDim.x) {
+        const int64_t t = b0 + threadIdx.x;
+        const int v = t < n ? a.kagg[t] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        int before = carry, total = 0;
+        for (int w = 0; w < nw; w++) {
+            if (w < wid) before += wsum[w];
+            total += wsum[w];
+        }
+        if (t < n) a.kagg[t] = before + incl - v;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *a.unext = carry;
+}
+
+// (f) compacted list: the columns that stay unresolved, in order, into the
+//     next list, and into the Phase II queue; first[] reset (once per row, by
+//     its winner).  Clears marked in (d) are applied by the next Phase I
+//     (Phase II skips such columns).
+__global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
+    if (a.st->converged) return;
+    const int64_t n = p1_count(a);
+    if ((int64_t)blockIdx.x * P1_TILE >= n) return;
+    __shared__ int wsum[P1_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
+    int cols[P1_ITEMS];
+    unsigned keepmask = 0;
+    int cnt = 0;
+#pragma unroll
+    for (int t = 0; t < P1_ITEMS; t++) {
+        const int64_t idx = base + t;
+        cols[t] = -1;
+        if (idx < n) {
+            const int64_t j = p1_col(a, idx);
+            const int lj = a.low[j];
+            if (lj >= 0 && a.first[lj] == (int)j) a.first[lj] = FIRST_NONE;
+            if (lj >= 0 && a.classes[j] == 0) {
+                cols[t] = (int)j;
+                keepmask |= 1u << t;
+                cnt++;
+            }
+        }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) wsum[wid] = incl;
+    __syncthreads();
+    int off = a.kagg[blockIdx.x] + incl - cnt;
+    for (int w = 0; w < wid; w++) off += wsum[w];
+#pragma unroll
+    for (int t = 0; t < P1_ITEMS; t++)
+        if (keepmask & (1u << t)) a.ulist_next[off++] = cols[t];
+    // Phase II takes the same columns from a queue filled by warp-aggregated
+    // appends: concurrently reduced columns then come from all over the
+    // matrix instead of one neighbourhood (which contends on shared pivots)
+#pragma unroll
+    for (int t = 0; t < P1_ITEMS; t++) warp_append((keepmask >> t) & 1u, cols[t], a.worklist, &a.st->t_count[0]);
+}
+
+// (e') without a compacted list: reset first[], apply the clears of this
+//      Phase I, and queue the unresolved columns (any order) for Phase II.
 __global__ void k_p1_worklist(PmsArgs a) {
     if (a.st->converged) return;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -299,7 +417,9 @@ template <int G, bool SMALL_PIVOTS_ONLY, class Tile>
 __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int *C, int cap,
                                    int32_t *out_list, int *out_cnt, long long &adds, long long &slots) {
     const int lane = tile.thread_rank();
+    if (a.clear[j]) return;  // positive: cleared by the next Phase I
     int lj = a.low[j];
+    if (lj < 0) return;
     int4 h, e;
     rec_load(&a.rec[lj], h, e);
     if (h.x < 0 || h.x >= j) return;  // no pivot to the left of j yet
@@ -397,9 +517,9 @@ __global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
     auto tile = cg::tiled_partition<G>(cg::this_thread_block());
     const int gid = threadIdx.x / G;
     int *buf = smem + (size_t)gid * (STAGE ? 3 : 2) * CAP;
-    int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
+    int32_t *in_list = tier == 0 ? a.t0_list : (tier & 1) ? a.widelist : a.worklist;
     int32_t *out_list = (tier & 1) ? a.worklist : a.widelist;
-    const int count = a.st->t_count[tier];
+    const int count = tier == 0 ? *a.t0_count : a.st->t_count[tier];
     long long adds = 0, slots = 0;
     for (;;) {
         int idx = 0;
@@ -420,7 +540,9 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
     __shared__ long long s_off;
     __shared__ int s_small[4];
     const int tid = threadIdx.x;
+    if (a.clear[j]) return;
     int lj = a.low[j];
+    if (lj < 0) return;
     int4 h, e;
     rec_load(&a.rec[lj], h, e);
     if (h.x < 0 || h.x >= j) return;
@@ -521,9 +643,9 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
     extern __shared__ int smem[];
     __shared__ int scratch[2 * (BLOCK / 32)];
     __shared__ int s_idx;
-    int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
+    int32_t *in_list = tier == 0 ? a.t0_list : (tier & 1) ? a.widelist : a.worklist;
     int32_t *out_list = (tier & 1) ? a.worklist : a.widelist;
-    const int count = a.st->t_count[tier];
+    const int count = tier == 0 ? *a.t0_count : a.st->t_count[tier];
     long long adds = 0, slots = 0;
     for (;;) {
         if (threadIdx.x == 0) s_idx = atomicAdd(&a.st->t_cursor[tier], 1);
@@ -586,6 +708,10 @@ static int t0_grid(Context *ctx, size_t *smem) {
     *smem = (size_t)(T0_BLOCK / G) * 2 * CAP * sizeof(int);
     return fill_grid(ctx, k_p2_tier<G, CAP, T0_BLOCK, false>, T0_BLOCK, *smem, done);
 }
+template <int G, int CAP>
+static void t0_launch(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) {
+    k_p2_tier<G, CAP, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0);
+}
 static int t0_grid_of(Context *ctx, int v, size_t *smem) {
     switch (v) {
         case 1: return t0_grid<4, 128>(ctx, smem);
@@ -598,12 +724,12 @@ static int t0_grid_of(Context *ctx, int v, size_t *smem) {
 }
 static void launch_t0(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) {
     switch (g.v0) {
-        case 1: k_p2_tier<4, 128, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
-        case 2: k_p2_tier<8, 64, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
-        case 3: k_p2_tier<8, 256, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
-        case 4: k_p2_tier<16, 128, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
-        case 5: k_p2_tier<16, 256, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
-        default: k_p2_tier<8, 128, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0); break;
+        case 1: t0_launch<4, 128>(a, g, s); break;
+        case 2: t0_launch<8, 64>(a, g, s); break;
+        case 3: t0_launch<8, 256>(a, g, s); break;
+        case 4: t0_launch<16, 128>(a, g, s); break;
+        case 5: t0_launch<16, 256>(a, g, s); break;
+        default: t0_launch<8, 128>(a, g, s); break;
     }
 }
 
@@ -636,14 +762,38 @@ void launch_phase0(const PmsArgs &a, int64_t c0, int64_t c1, int grid, cudaStrea
     k_phase0<<<grid, 256, 0, s>>>(a, c0, c1);
 }
 
+__global__ void k_iota(int32_t *p, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        p[i] = (int32_t)i;
+}
+
 // ev (optional, 6 events): before Phase I, after Phase I, after each tier.
-static void launch_sweep_ev(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, cudaEvent_t *ev) {
+static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t s, cudaEvent_t *ev, int parity) {
+    PmsArgs a = a0;
+    if (a0.ulist) {
+        // the list read this sweep and the one it compacts into
+        int32_t *L[2] = {a0.ulist, a0.ulist_next};
+        int *C[2] = {&a0.st->ucount[0], &a0.st->ucount[1]};
+        a.ulist = L[parity & 1];
+        a.ulist_next = L[(parity + 1) & 1];
+        a.ucur = C[parity & 1];
+        a.unext = C[(parity + 1) & 1];
+    }
+    {
+        a.t0_list = a.worklist;
+        a.t0_count = &a0.st->t_count[0];
+    }
     if (ev) cudaEventRecord(ev[0], s);
     k_p1_first<<<g.m, 256, 0, s>>>(a);
     k_p1_tiles<<<g.t, P1_THREADS, 0, s>>>(a);
     k_p1_scan<<<1, 32 * MAXC, 0, s>>>(a);
     k_p1_mark<<<g.t, P1_THREADS, 0, s>>>(a);
-    k_p1_worklist<<<g.m, 256, 0, s>>>(a);
+    if (a.ulist) {
+        k_p1_kscan<<<1, 1024, 0, s>>>(a);
+        k_p1_scatter<<<g.t, P1_THREADS, 0, s>>>(a);
+    } else {
+        k_p1_worklist<<<g.m, 256, 0, s>>>(a);
+    }
     if (ev) cudaEventRecord(ev[1], s);
     launch_t0(a, g, s);
     if (ev) cudaEventRecord(ev[2], s);
@@ -656,9 +806,11 @@ static void launch_sweep_ev(const PmsArgs &a, const SweepGrids &g, cudaStream_t 
     if (ev) cudaEventRecord(ev[5], s);
 }
 
-void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) { launch_sweep_ev(a, g, s, nullptr); }
+void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int parity) {
+    launch_sweep_ev(a, g, s, nullptr, parity);
+}
 
-constexpr int KERNELS_PER_SWEEP = 10;
+constexpr int KERNELS_PER_SWEEP = 11;
 
 int run_pms(Context *ctx, Work &w, oph_info *info) {
     const int64_t m = w.m;
@@ -666,10 +818,26 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     a.m = m; a.low = w.low; a.classes = w.classes; a.clear = w.clear; a.dim = w.dim; a.first = w.first;
     a.beta = w.beta; a.worklist = w.worklist; a.widelist = w.widelist; a.seg = w.seg;
     a.rec = w.rec; a.agg = w.agg; a.ntiles = w.ntiles; a.pool = w.pool; a.st = w.st;
+    // Phase I over a compacted list of the unresolved columns: every column
+    // at first, then only those still unresolved after each sweep
+#ifndef OPH_PHASE1_LIST
+#define OPH_PHASE1_LIST 1
+#endif
+    if (OPH_PHASE1_LIST) {
+        a.ulist = (int32_t *)ctx_alloc(ctx, S_ULIST, sizeof(int32_t) * 2 * (m > 0 ? m : 1));
+        a.kagg = (int32_t *)ctx_alloc(ctx, S_KAGG, sizeof(int32_t) * (w.ntiles + 1));
+        if (!a.ulist || !a.kagg) return OPH_ERR_OOM;
+        a.ulist_next = a.ulist + m;
+    }
     cudaStream_t s = ctx->stream;
     SweepGrids g;
     int rc = sweep_grids(ctx, m, w.ntiles, &g);
     if (rc) return rc;
+    if (a.ulist) {
+        k_iota<<<g.m, 256, 0, s>>>(a.ulist, m);
+        const int mi = (int)m;
+        OPH_CUDA_TRY(cudaMemcpyAsync(&w.st->ucount[0], &mi, sizeof(int), cudaMemcpyHostToDevice, s));
+    }
 
     OPH_CUDA_TRY(cudaMemsetAsync(w.first, 0x7f, sizeof(int32_t) * m, s));
     OPH_CUDA_TRY(cudaMemsetAsync(w.classes, 0, m, s));
@@ -704,7 +872,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         const int nb = std::min(batch, max_sweeps - sweeps_launched);
         DevStatus before = hs;
         for (int b = 0; b < nb; b++) {
-            launch_sweep_ev(a, g, s, timed ? ctx->pev + 6 * b : nullptr);
+            launch_sweep_ev(a, g, s, timed ? ctx->pev + 6 * b : nullptr, sweeps_launched + b);
             ctx->launches += KERNELS_PER_SWEEP;
         }
         sweeps_launched += nb;

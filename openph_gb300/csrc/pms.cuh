@@ -28,6 +28,15 @@ struct PmsArgs {
     unsigned long long *ipool;    // per instance: bump pointer, end
     int *ireps;                   // per instance: repeated lows seen by the last Phase I
     int *iover;                   // per instance: a pool allocation failed
+    // compacted Phase I (single matrix): the unresolved columns in column
+    // order, ping-ponged between two arrays; counts in ucur / unext
+    int32_t *ulist;               // nullptr: Phase I visits every column
+    int32_t *ulist_next;
+    int *ucur, *unext;
+    int32_t *kagg;                // per tile: columns kept, then their offsets
+    // Phase II tier-0 queue (the compacted list, or the worklist)
+    int32_t *t0_list;
+    int *t0_count;
 };
 
 // Launch geometry of the Phase II tiers (occupancy-derived, per device).
@@ -43,8 +52,9 @@ struct SweepGrids {
 };
 
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g);
-// One sweep (Phase I, Phase II tiers, sweep counter) on `stream`.
-void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t stream);
+// One sweep (Phase I, Phase II tiers, sweep counter) on `stream`; with a
+// compacted list, `parity` selects which of the two arrays is current.
+void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t stream, int parity = 0);
 // Phase 0 over columns [c0, c1).
 void launch_phase0(const PmsArgs &a, int64_t c0, int64_t c1, int grid, cudaStream_t stream);
 

@@ -213,7 +213,9 @@ struct Server {
     int error = OPH_OK;
 
     int64_t packed_ints(int64_t m, int64_t nnz) const { return 8 * (m + 1) + 4 * ((nnz + 3) / 4) + 64; }
-    int64_t region_ints(int64_t m, int64_t nnz) const { return packed_ints(m, nnz) * 3 + 4096; }
+    int64_t region_ints(int64_t m, int64_t nnz) const { return packed_ints(m, nnz) * 4 + 4096; }
+    // staging regions of admitted requests, released after the next sync
+    std::vector<std::pair<int64_t, int64_t>> staged;
 
     int grid(int64_t n) const {
         int64_t gsz = (n + 255) / 256, cap = (int64_t)ctx->sm_count * 16;
@@ -249,42 +251,57 @@ struct Server {
                                          (unsigned long long)(reg + packed_ints(r->m, r->nnz)),
                                          (unsigned long long)(reg + reg_ints));
         if (r->m > 0) launch_phase0(a, c0, c0 + r->m, grid(r->m), s);
-        // the staged input is consumed by the kernels above before the next
-        // host read of the stream, so its region can be reused after that
-        cudaStreamSynchronize(s);
-        pool.release(stg, stage_ints);
+        // the staged input is read by the kernels above: its region is
+        // released after the sweep's synchronisation
+        staged.emplace_back(stg, stage_ints);
         r->t_admit = now_ms();
         slots[b] = r;
         admitted++;
         return 0;
     }
 
-    void retire(Request *r) {
+    // Retires every converged request: output kernels for all of them, then
+    // the copies to the host, one synchronisation, then the notifications.
+    void retire_all(const std::vector<Request *> &done) {
+        if (done.empty()) return;
         cudaStream_t s = ctx->stream;
-        const int64_t m = r->m;
-        r->low.resize(m);
-        r->ess.resize(m);
-        if (m > 0) {
-            const int64_t out = pool.alloc(2 * m + 4, 64);
-            int32_t *d_out = a.pool + (out >= 0 ? out : r->reg);  // the request's own region is free to reuse
-            k_srv_out1<<<grid(m), 256, 0, s>>>(m, r->c0, a, d_out);
-            k_srv_out2<<<grid(m), 256, 0, s>>>(m, r->c0, a, d_out);
-            cudaMemcpyAsync(r->low.data(), d_out, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
-            cudaMemcpyAsync(r->ess.data(), d_out + m, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s);
-            k_srv_inert<<<grid(m), 256, 0, s>>>(m, r->c0, a);
-            cudaStreamSynchronize(s);
-            if (out >= 0) pool.release(out, 2 * m + 4);
+        std::vector<std::pair<int64_t, int64_t>> outs;
+        std::vector<int32_t *> dptr(done.size(), nullptr);
+        for (size_t k = 0; k < done.size(); k++) {
+            Request *r = done[k];
+            const int64_t m = r->m;
+            r->low.resize(m);
+            r->ess.resize(m);
+            if (m == 0) continue;
+            int64_t out = pool.alloc(2 * m + 4, 64);
+            if (out >= 0) outs.emplace_back(out, 2 * m + 4);
+            else out = r->reg;  // the request's own region is no longer read
+            dptr[k] = a.pool + out;
+            k_srv_out1<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
+            k_srv_out2<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
         }
-        cols.release(r->c0, std::max<int64_t>(m, 1));
-        pool.release(r->reg, r->reg_ints);
-        slots[r->slot] = nullptr;
-        r->t_done = now_ms();
-        r->colptr.clear(); r->colptr.shrink_to_fit();
-        r->rows.clear(); r->rows.shrink_to_fit();
+        for (size_t k = 0; k < done.size(); k++) {
+            Request *r = done[k];
+            if (r->m == 0) continue;
+            cudaMemcpyAsync(r->low.data(), dptr[k], sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(r->ess.data(), dptr[k] + r->m, sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
+            k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
+        }
+        cudaStreamSynchronize(s);
+        for (auto &o : outs) pool.release(o.first, o.second);
+        const double t = now_ms();
         {
             std::lock_guard<std::mutex> lk(mu);
-            r->done = true;
-            completed++;
+            for (Request *r : done) {
+                cols.release(r->c0, std::max<int64_t>(r->m, 1));
+                pool.release(r->reg, r->reg_ints);
+                slots[r->slot] = nullptr;
+                r->t_done = t;
+                r->colptr.clear(); r->colptr.shrink_to_fit();
+                r->rows.clear(); r->rows.shrink_to_fit();
+                r->done = true;
+                completed++;
+            }
         }
         cv_done.notify_all();
     }
@@ -324,7 +341,11 @@ struct Server {
     void run() {
         cudaSetDevice(ctx->device);
         cudaStream_t s = ctx->stream;
+        // OPH_TRACE=1: one line per sweep on stderr (diagnostics only)
+        const bool trace = getenv("OPH_TRACE") != nullptr;
         for (;;) {
+            const double t_round = now_ms();
+            const int64_t admitted_before = admitted;
             // admission, first come first served
             int active = 0;
             for (auto *r : slots) active += r != nullptr;
@@ -379,6 +400,8 @@ struct Server {
                 fail_all(OPH_ERR_CUDA);
                 return;
             }
+            for (auto &st : staged) pool.release(st.first, st.second);
+            staged.clear();
             sweeps++;
             for (auto *r : slots)
                 if (r) r->sweeps++;
@@ -390,8 +413,16 @@ struct Server {
                         return;
                     }
                 }
+            std::vector<Request *> done;
             for (int b = 0; b < max_slots; b++)
-                if (slots[b] && h_ireps[b] == 0 && !h_iover[b]) retire(slots[b]);
+                if (slots[b] && h_ireps[b] == 0 && !h_iover[b]) done.push_back(slots[b]);
+            const double t_swept = now_ms();
+            retire_all(done);
+            if (trace)
+                fprintf(stderr, "server sweep %lld: span %lld cols, %d active, %lld admitted, %zu retired | "
+                                "round %.3f ms (sweep+admit %.3f, retire %.3f)\n",
+                        (long long)sweeps, (long long)hi, active, (long long)(admitted - admitted_before),
+                        done.size(), now_ms() - t_round, t_swept - t_round, now_ms() - t_swept);
         }
     }
 };

@@ -23,12 +23,14 @@ def make(workload: str, target_m: int, seed: int):
         return cx.lower_star_image(side, side, seed=seed)
     if workload == "rips_cube":
         return cx.rips_cube(50, seed=seed)
+    if workload == "batch":
+        return cx.rips_mixed_batch(target_m or 4096, seed)
     raise SystemExit(f"unknown workload {workload}")
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="rips_torus")
+    ap.add_argument("--workload", default="rips_torus", help="rips_torus, lower_star, rips_cube or batch")
     ap.add_argument("--target-m", type=int, default=1_000_000)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--algo", default="pms")
@@ -41,6 +43,19 @@ def main():
     bm = make(args.workload, args.target_m, args.seed)
     dev = torch.device("cuda", 0)
     ctx = api.Context(0)
+    if args.workload == "batch":
+        # --target-m is the number of complexes; one segmented pass each step
+        col_off, colptr, rows = (torch.from_numpy(x).to(dev) for x in bm[:3])
+        m, nnz = int(bm[0][-1]), int(bm[1][-1])
+        d_low = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        out = [ctx.reduce_batch_device(len(bm[0]) - 1, col_off.data_ptr(), colptr.data_ptr(), rows.data_ptr(), m,
+                                       nnz, d_low.data_ptr(), None, args.algo) for _ in range(args.steps)]
+        print(json.dumps({"workload": "batch", "count": len(bm[0]) - 1, "m": m, "nnz": nnz,
+                          "device_ms": [o["device_ms"] for o in out], "sweeps": out[-1]["sweeps"],
+                          "additions": out[-1]["additions"]}))
+        ctx.close()
+        return
     d_colptr = torch.from_numpy(bm.colptr).to(dev)
     d_rows = torch.from_numpy(bm.rows).to(dev)
     d_low = torch.empty(max(bm.m, 1), dtype=torch.int32, device=dev)
