@@ -250,7 +250,6 @@ def run_ours(args, ws, rank, local):
     ctx.set_profile(True)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     narrow_ms, wide_ms, p1_ms, launches, p2_launches, infos = 0.0, 0.0, 0.0, 0, 0, []
-    tier0_slots = 0
     barrier(dist, device)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
@@ -266,8 +265,13 @@ def run_ours(args, ws, rank, local):
             p1_ms += prof["phase1_ms"]
             launches += prof["kernel_launches"]
             p2_launches += prof["phase2_launches"]
-            tier0_slots += prof["tier_slots"][0]
         torch.cuda.synchronize()
+    # the exact |P| + |T| + |T xor P| of every tier-0 addition, from one more
+    # (untimed) reduction of the same matrix with slot tracking on
+    ctx.set_profile(True, slots=True)
+    step()
+    prof = ctx.last_profile()
+    tier0_slots = prof["tier_slots"][0]
     ctx.set_profile(False)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = max_over_ranks(sum(step_ms) / 1e3, dist, device)
@@ -325,7 +329,7 @@ def run_ours(args, ws, rank, local):
     # it performed (counted on the device), per launch; divided by its mean
     # launch time (CUDA events around each launch on the library's stream)
     per_red_narrow_s = narrow_ms / 1e3 / args.steps
-    t0_bytes = 4 * tier0_slots / args.steps
+    t0_bytes = 4 * tier0_slots
     achieved = t0_bytes / per_red_narrow_s / 1e9 if per_red_narrow_s > 0 else None
     traffic = load_traffic()
     launches_per_red = p2_launches / args.steps

@@ -189,11 +189,15 @@ typedef struct {
     int32_t phase2_launches;  /* narrow-tier launches that did work                */
     int32_t kernel_launches;  /* every kernel launched by the last reduction       */
     int64_t tier_additions[4];/* column additions done by each Phase II tier       */
-    int64_t tier_slots[4];    /* sum of |P| + |T| + |T xor P| per tier             */
+    int64_t tier_slots[4];    /* sum of |P| + |T| + |T xor P| per tier (tiers 0-1:
+                                 only with OPH_PROFILE_SLOTS)                      */
 } oph_profile;
 
-/* Turn per-phase CUDA-event timing on or off for later reductions on ctx
- * (off by default; on adds event records between the phase kernels). */
+#define OPH_PROFILE_EVENTS 1  /* per-phase CUDA-event timing                     */
+#define OPH_PROFILE_SLOTS 2   /* exact |T| tracking in the lazy tiers 0 and 1,   */
+                              /* for tier_slots (slower: not for timed runs)     */
+/* Select profiling for later reductions on ctx: an OR of OPH_PROFILE_*
+ * (0, the default, turns it off). */
 int oph_context_set_profile(oph_context *ctx, int on);
 /* Per-phase device times and launch counts of the last reduction on ctx. */
 int oph_last_profile(oph_context *ctx, oph_profile *out);

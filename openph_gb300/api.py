@@ -320,8 +320,10 @@ class Context:
         if rc != OPH_OK:
             raise OphError(rc, "oph_context_set_tier0")
 
-    def set_profile(self, on: bool = True):
-        lib().oph_context_set_profile(self._h, 1 if on else 0)
+    def set_profile(self, on: bool = True, slots: bool = False):
+        """Per-phase event timing (``on``); ``slots`` also tracks the exact
+        |P| + |T| + |T xor P| of every addition in the lazy tiers (slower)."""
+        lib().oph_context_set_profile(self._h, (1 if on else 0) | (2 if slots else 0))
 
     def last_profile(self):
         p = Profile()

@@ -336,7 +336,9 @@ __attribute__((visibility("default"))) int oph_context_set_limits(oph_context *c
 
 __attribute__((visibility("default"))) int oph_context_set_profile(oph_context *ctx, int on) {
     if (!ctx) return OPH_ERR_BAD_INPUT;
-    ctx->profile = on ? 1 : 0;
+    if (on & ~3) return OPH_ERR_BAD_INPUT;
+    ctx->profile = on & 1;
+    ctx->count_slots = (on >> 1) & 1;
     return OPH_OK;
 }
 

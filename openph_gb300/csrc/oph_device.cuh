@@ -64,6 +64,15 @@ struct DevStatus {
     int ucount[2];                     // compacted Phase I: list sizes (ping-pong)
     unsigned long long tier_adds[4];   // additions performed by each Phase II tier
     unsigned long long tier_slots[4];  // |P| + |T| + |T xor P| summed per tier
+    // diagnostics of the lazy tiers 0 and 1 (filled only in OPH_COUNTS builds),
+    // per tier t at [8t ..]: additions by a pivot held in its record, by a
+    // pivot of <= 4 rows read from its segment, by one of 5 .. G + 1 rows, by
+    // a wider one; flushes of pending toggles before the chain's end; top
+    // cancellations; columns entered; their rows on entry
+    unsigned long long diag[16];
+#if defined(OPH_COUNTS) && OPH_COUNTS
+    unsigned long long diag_sm[256];  // Phase II additions per SM
+#endif
 };
 
 __device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
@@ -248,6 +257,46 @@ __device__ __forceinline__ int merge_xor_seg(const Tile &tile, const int *A, int
         }
     }
     for (int q = src + lane; q < nA; q += G) B[q + shift] = A[q];
+    tile.sync();
+    return nA + nP - 2 * __popc(dmask);
+}
+
+// The same for a pivot of more entries (still at most G, one per lane): the
+// runs are found per element instead of per pivot entry.  With thr_k = the
+// first index of A that lies past P[k] (r_k, plus one when P[k] is in A, as
+// that element is dropped), the element at index i moves by
+// c - 2 * (common entries among the first c), c = #{k : thr_k <= i}, and c is
+// found by a binary search over the thresholds held in lanes (uniform trip
+// count, so every lane takes part in every shuffle).  Returns |A xor P|.
+template <int G, class Tile>
+__device__ __forceinline__ int merge_xor_thr(const Tile &tile, const int *A, int nA, int pv, int nP, int *B) {
+    const int lane = tile.thread_rank();
+    const unsigned lt = (1u << lane) - 1u;
+    int r = 0;
+    bool pdup = false;
+    if (lane < nP) {
+        r = lower_bound(A, nA, pv);
+        pdup = r < nA && A[r] == pv;
+    }
+    const unsigned dmask = tile.ballot(pdup);
+    if (lane < nP && !pdup) B[lane + r - 2 * __popc(dmask & lt)] = pv;
+    const int thr = r + (pdup ? 1 : 0);
+    int top = 1;
+    while (top * 2 <= nP) top *= 2;
+    for (int base = 0; base < nA; base += G) {
+        const int i = base + lane;
+        int c = 0;
+        for (int step = top; step > 0; step >>= 1) {
+            const int t = tile.shfl(thr, min(c + step - 1, G - 1));
+            if (c + step <= nP && t <= i) c += step;
+        }
+        const int rc = tile.shfl(r, min(c, G - 1));
+        if (i < nA) {
+            const bool drop = c < nP && ((dmask >> c) & 1u) && rc == i;
+            const int shift = c - 2 * __popc(dmask & ((c >= 32) ? 0xffffffffu : ((1u << c) - 1u)));
+            if (!drop) B[i + shift] = A[i];
+        }
+    }
     tile.sync();
     return nA + nP - 2 * __popc(dmask);
 }

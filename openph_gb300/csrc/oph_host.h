@@ -79,6 +79,7 @@ struct Context {
     int64_t budget = 0;
     int64_t pool_ints = 0;          // current pool capacity
     int profile = 0;                // record per-phase events
+    int count_slots = 0;            // exact |P| + |T| + |T xor P| in every tier
     cudaEvent_t *pev = nullptr;     // profiling events (pairs)
     int pev_n = 0;
     oph_profile prof{};             // last reduction

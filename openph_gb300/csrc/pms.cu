@@ -69,6 +69,9 @@ __device__ __forceinline__ bool is_repeat(const PmsArgs &a, int64_t j, int lj) {
     return (pc >= 0 && pc < (int)j) || a.first[lj] != (int)j;
 }
 
+#ifndef OPH_FIRST_CHECK
+#define OPH_FIRST_CHECK 1
+#endif
 // (a) apply pending clears (clear_positives, pms_functions.cu:131-140) and
 //     record the first column of every low.
 __global__ void k_p1_first(PmsArgs a) {
@@ -93,7 +96,11 @@ __global__ void k_p1_first(PmsArgs a) {
             // a column whose low already has a pivot to its left is a repeat:
             // the pivot itself records first[low], so only the others race
             const int pc = a.rec[lj].col;
-            if (pc < 0 || pc >= (int)j) atomicMin(&a.first[lj], (int)j);
+            // many columns can share a low: skip the atomic when first[]
+            // already holds a smaller column (a stale read only costs the
+            // atomic that would have been issued anyway)
+            if ((pc < 0 || pc >= (int)j) && (!OPH_FIRST_CHECK || a.first[lj] > (int)j))
+                atomicMin(&a.first[lj], (int)j);
         }
     }
 }
@@ -407,12 +414,52 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 //   tier 2  a CTA per column,   CAP 8192     (block-wide merge)
 //   tier 3  a CTA per column,   buffers in the pool (no limit)
 // Pivots of at most G entries (most are apparent pairs of 3 entries) are held
-// one per lane and merged by segment copies (merge_xor_seg).  The queues
+// one per lane and merged without staging (merge_xor_seg / merge_xor_thr).  The queues
 // ping-pong between the worklist and widelist arrays.  Each addition costs
 // one dependent round trip when the pivot has at most four entries (its
 // record carries them, with left[] for the beta check) and two otherwise;
 // reading G ints past a segment start stays in bounds through the pool's
 // tail padding.
+// Pivots of at most OPH_SEG_MAX entries are merged by runs (merge_xor_seg,
+// a loop over the pivot's entries), wider ones up to G by per-element
+// threshold search (merge_xor_thr, a loop over A's chunks).
+#ifndef OPH_SEG_MAX
+#define OPH_SEG_MAX 4
+#endif
+// Which of tiers 0 (bit 0) and 1 (bit 1) reduce lazy columns
+// (reduce_column_lazy); the others merge eagerly on every addition
+// (reduce_column_smem).
+#ifndef OPH_LAZY
+#define OPH_LAZY 2
+#endif
+// Phase II reads pivot records through L1 (1) or L2 only (0).  A record seen
+// through L1 may be stale, i.e. still unpublished (col -1) or partly
+// published; the first makes the column stop its chain for this sweep, the
+// second takes the acquire path, so a stale line costs time, not results.
+#ifndef OPH_REC_L1
+#define OPH_REC_L1 0
+#endif
+// Mark column lj positive (cleared by the next Phase I).  Every chain through
+// row lj marks it again; with OPH_CLEAR_CHECK the flag is read (alongside the
+// record) and written only while still 0, so the hot flags are not rewritten
+// by thousands of warps.
+#ifndef OPH_CLEAR_CHECK
+#define OPH_CLEAR_CHECK 1
+#endif
+template <bool CHECK = OPH_CLEAR_CHECK != 0>
+__device__ __forceinline__ void mark_clear(const PmsArgs &a, int lj, bool leader) {
+    if (!leader) return;
+    if (!CHECK || !a.clear[lj]) a.clear[lj] = 1;
+}
+__device__ __forceinline__ void rec_load_p2(const PivRec *r, int4 &h, int4 &e) {
+    if (OPH_REC_L1) {
+        const int4 *p = reinterpret_cast<const int4 *>(r);
+        h = __ldca(p);
+        e = __ldca(p + 1);
+    } else {
+        rec_load(r, h, e);
+    }
+}
 template <int G, bool SMALL_PIVOTS_ONLY, class Tile>
 __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int *C, int cap,
                                    int32_t *out_list, int *out_cnt, long long &adds, long long &slots) {
@@ -421,7 +468,7 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
     int lj = a.low[j];
     if (lj < 0) return;
     int4 h, e;
-    rec_load(&a.rec[lj], h, e);
+    rec_load_p2(&a.rec[lj], h, e);
     if (h.x < 0 || h.x >= j) return;  // no pivot to the left of j yet
     const long long sj = a.seg[j];
     int n = a.pool[sj];
@@ -449,8 +496,10 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
         }
         if (n + np > cap || (SMALL_PIVOTS_ONLY && np > G)) { handed = true; break; }
         int nn;
-        if (np <= G) {
+        if (np <= OPH_SEG_MAX) {
             nn = merge_xor_seg<G>(tile, A, n, pv, np, B);
+        } else if (np <= G) {
+            nn = merge_xor_thr<G>(tile, A, n, pv, np, B);
         } else if (C) {
             group_copy<G>(tile, C, P, np);
             nn = merge_xor<G>(tile, A, n, C, np, B);
@@ -463,10 +512,184 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
         int *t = A; A = B; B = t;
         lj = n ? A[n - 1] : -1;
         if (lj < 0) break;
-        rec_load(&a.rec[lj], h, e);
-        if (lane == 0) a.clear[lj] = 1;
+        rec_load_p2(&a.rec[lj], h, e);
+        mark_clear(a, lj, lane == 0);
         if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
         if (h.x < 0 || h.x >= j) break;
+    }
+    long long dst = sj;
+    int dcap = capj;
+    if (n > capj) {
+        dcap = round4(max(n + (n >> 1), 16));
+        long long off = 0;
+        if (lane == 0) off = col_alloc(a, j, SEG_HDR + dcap);
+        off = tile.shfl(off, 0);
+        if (off < 0) return;  // pool exhausted: j keeps its pre-sweep state
+        dst = off;
+    }
+    group_copy<G>(tile, a.pool + dst + SEG_HDR, A, n);
+    if (lane == 0) {
+        a.pool[dst] = n;
+        a.pool[dst + 1] = dcap;
+        a.seg[j] = dst;
+        a.low[j] = lj;
+    }
+    if (made_pivot) {
+        fence_acq_rel();
+        tile.sync();
+        if (lane == 0) {
+            a.classes[j] = -1;
+            rec_publish(a.rec, lj, j, n, dst, A);
+        }
+    } else if (handed) {
+        if (lane == 0) out_list[atomicAdd(out_cnt, 1)] = j;
+    }
+    tile.sync();
+}
+
+// The same chain of additions on a lazy column.  The column under reduction
+// is T = A xor D: A ascending in shared memory (the column as of the last
+// flush, less the entries popped off its top), D ascending in registers
+// (lane k < dn holds D[k]), the pending toggles, at most G of them.  Adding
+// a pivot P (whose last entry is low(T)) pops low(T) off whichever of A and
+// D holds it and toggles P's other entries in D: a ballot gives each one's
+// rank and a one-lane shuffle makes or closes its slot.  Equal tops of A and
+// D cancel as they surface.  D is merged into A (merge_xor_thr) only when a
+// pivot would not fit in what is left of D and when the chain ends, so an
+// addition costs O(|P|) register work instead of an O(|T|) copy: on the
+// long top-dimension chains of Rips complexes a flush comes every 6 (G = 8)
+// to 38 (G = 32) additions.  Pivots wider than G are merged eagerly into A.
+// With STATS the exact |T| is carried through every addition (membership of
+// each toggled row in A by binary search) for the |P| + |T| + |T xor P|
+// counters; without it only additions are counted.
+#ifndef OPH_COUNTS
+#define OPH_COUNTS 0
+#endif
+struct LazyDiag {
+    unsigned long long c[8];
+};
+template <int G, bool STATS, class Tile>
+__device__ void reduce_column_lazy(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int *C, int cap,
+                                   int32_t *out_list, int *out_cnt, long long &adds, long long &slots,
+                                   LazyDiag &dg) {
+    const int lane = tile.thread_rank();
+    if (a.clear[j]) return;  // positive: cleared by the next Phase I
+    int lj = a.low[j];
+    if (lj < 0) return;
+    int4 h, e;
+    rec_load_p2(&a.rec[lj], h, e);
+    if (h.x < 0 || h.x >= j) return;  // no pivot to the left of j yet
+    const long long sj = a.seg[j];
+    int n = a.pool[sj];
+    const int capj = a.pool[sj + 1];
+    if (n > cap) {
+        if (lane == 0) out_list[atomicAdd(out_cnt, 1)] = j;
+        return;
+    }
+    group_copy<G>(tile, A, a.pool + sj + SEG_HDR, n);
+    if (OPH_COUNTS) { dg.c[6]++; dg.c[7] += n; }
+    int dn = 0, dv = 0;
+    int tsize = n;  // |T|, kept with STATS
+    bool made_pivot = false, handed = false;
+    for (;;) {
+        int np, pv;
+        const int *P = nullptr;
+        if (rec_complete(h, e)) {
+            np = h.y;
+            pv = rec_entry(e, lane & 3);
+        } else {
+            ld_acquire_i32(&a.rec[lj].col);
+            const int4 h2 = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+            np = h2.y;
+            P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
+            pv = P[lane];
+        }
+        if (n + dn + np > cap) { handed = true; break; }
+        if (OPH_COUNTS) dg.c[np - 1 > G ? 3 : np > 4 ? 2 : P ? 1 : 0]++;
+        // pop low(T): the larger of the two (settled, so different) tops
+        if (n > 0 && A[n - 1] == lj) n--;
+        else dn--;
+        const int k = np - 1;  // P's entries below the low
+        int common = 1;        // |T and P|, with STATS
+        if (STATS && k <= G) {
+            for (int t = 0; t < k; t++) {
+                const int x = tile.shfl(pv, t);
+                const bool inD = tile.ballot(lane < dn && dv == x) != 0u;
+                const int r = lower_bound(A, n, x);
+                const bool inA = r < n && A[r] == x;
+                common += inA != inD;
+            }
+        }
+        if (k > G - dn && dn > 0) {  // no room in D: flush it into A
+            if (OPH_COUNTS) dg.c[4]++;
+            n = merge_xor_thr<G>(tile, A, n, dv, dn, B);
+            int *t = A; A = B; B = t;
+            dn = 0;
+        }
+        if (k > G) {
+            // a wide pivot, merged into A directly (staged when there is room)
+            const int *src = P;
+            if (C) {
+                group_copy<G>(tile, C, P, k);
+                src = C;
+            }
+            const int nn = merge_xor<G>(tile, A, n, src, k, B);
+            if (STATS) common += (n + k - nn) / 2;
+            n = nn;
+            int *t = A; A = B; B = t;
+        } else if (k <= 4) {
+            for (int t = 0; t < k; t++) {
+                const int x = tile.shfl(pv, t);
+                const bool valid = lane < dn;
+                const int r = __popc(tile.ballot(valid && dv < x));
+                if (tile.ballot(valid && dv == x)) {
+                    const int v = tile.shfl_down(dv, 1);
+                    if (lane >= r) dv = v;
+                    dn--;
+                } else {
+                    const int v = tile.shfl_up(dv, 1);
+                    if (lane > r) dv = v;
+                    if (lane == r) dv = x;
+                    dn++;
+                }
+            }
+        } else {
+            // D xor P' through shared memory (B is free between flushes)
+            if (lane < dn) B[lane] = dv;
+            tile.sync();
+            const int nd = merge_xor_thr<G>(tile, B, dn, pv, k, B + G);
+            dv = lane < nd ? B[G + lane] : 0;
+            tile.sync();
+            dn = nd;
+        }
+        if (STATS) {
+            const int nt = tsize + np - 2 * common;
+            slots += tsize + np + nt;
+            tsize = nt;
+        }
+        adds++;
+        // settle: equal tops of A and D cancel; the larger top is the low
+        for (;;) {
+            const int at = n > 0 ? A[n - 1] : -1;
+            const int dt = tile.shfl(dv, dn > 0 ? dn - 1 : 0);
+            if (dn > 0 && at == dt) {
+                n--;
+                dn--;
+                if (OPH_COUNTS) dg.c[5]++;
+                continue;
+            }
+            lj = dn > 0 ? max(at, dt) : at;
+            break;
+        }
+        if (lj < 0) break;
+        rec_load_p2(&a.rec[lj], h, e);
+        mark_clear(a, lj, lane == 0);
+        if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
+        if (h.x < 0 || h.x >= j) break;
+    }
+    if (dn > 0) {
+        n = merge_xor_thr<G>(tile, A, n, dv, dn, B);
+        int *t = A; A = B; B = t;
     }
     long long dst = sj;
     int dcap = capj;
@@ -510,7 +733,7 @@ __device__ __forceinline__ void tier_stats(const PmsArgs &a, int tier, long long
 // Tiers 0 and 1: groups of G lanes, each group with A/B buffers of CAP ints
 // and, with STAGE, a C buffer into which a pivot wider than the group is
 // staged; without it (tier 0) such a pivot is searched in the store.
-template <int G, int CAP, int BLOCK, bool STAGE>
+template <int G, int CAP, int BLOCK, bool STAGE, bool LAZY>
 __global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
     if (a.st->converged) return;
     extern __shared__ int smem[];
@@ -521,15 +744,41 @@ __global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
     int32_t *out_list = (tier & 1) ? a.worklist : a.widelist;
     const int count = tier == 0 ? *a.t0_count : a.st->t_count[tier];
     long long adds = 0, slots = 0;
+    LazyDiag dg{};
+#ifndef OPH_T0_GRAB
+#define OPH_T0_GRAB 1
+#endif
     for (;;) {
         int idx = 0;
-        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->t_cursor[tier], 1);
+        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->t_cursor[tier], OPH_T0_GRAB);
         idx = tile.shfl(idx, 0);
         if (idx >= count) break;
-        reduce_column_smem<G, false>(tile, a, in_list[idx], buf, buf + CAP, STAGE ? buf + 2 * CAP : nullptr, CAP,
-                                     out_list, &a.st->t_count[tier + 1], adds, slots);
+        const int end = min(idx + OPH_T0_GRAB, count);
+        for (; idx < end; idx++) {
+            int *C = STAGE ? buf + 2 * CAP : nullptr;
+            int *qn = &a.st->t_count[tier + 1];
+            if (!LAZY)
+                reduce_column_smem<G, false>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots);
+            else if (a.stats)
+                reduce_column_lazy<G, true>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots,
+                                            dg);
+            else
+                reduce_column_lazy<G, false>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots,
+                                             dg);
+        }
     }
-    if (tile.thread_rank() == 0) tier_stats(a, tier, adds, slots);
+    if (tile.thread_rank() == 0) {
+        tier_stats(a, tier, adds, slots);
+        if (OPH_COUNTS) {
+            for (int q = 0; q < 8; q++)
+                if (dg.c[q]) atomicAdd(&a.st->diag[8 * (tier & 1) + q], dg.c[q]);
+#if OPH_COUNTS
+            unsigned smid;
+            asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+            if (adds) atomicAdd(&a.st->diag_sm[smid & 255], (unsigned long long)adds);
+#endif
+        }
+    }
 }
 
 // Tiers 2 and 3: the whole CTA on one column.  With cap > 0 the column and
@@ -604,7 +853,7 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
         lj = n ? A[n - 1] : -1;
         if (lj < 0) break;
         rec_load(&a.rec[lj], h, e);
-        if (tid == 0) a.clear[lj] = 1;
+        mark_clear<false>(a, lj, tid == 0);  // few columns: no hot flags
         if (h.z == j) { made_pivot = true; break; }
         if (h.x < 0 || h.x >= j) break;
     }
@@ -677,7 +926,12 @@ __global__ void k_count_sweep(DevStatus *st) {
 #define OPH_T1_G 32
 #endif
 constexpr int T0_G = OPH_T0_G, T0_CAP = OPH_T0_CAP, T0_BLOCK = 256;
+#ifndef OPH_T1_STAGE
+#define OPH_T1_STAGE 1
+#endif
 constexpr int T1_G = OPH_T1_G, T1_CAP = OPH_T1_CAP, T1_BLOCK = 256;
+constexpr bool T1_STAGE = OPH_T1_STAGE != 0;
+constexpr bool T0_LAZY = (OPH_LAZY & 1) != 0, T1_LAZY = (OPH_LAZY & 2) != 0;
 constexpr int T2_CAP = 8192, T2_BLOCK = 256;
 constexpr int T3_BLOCK = 256;
 
@@ -706,11 +960,11 @@ template <int G, int CAP>
 static int t0_grid(Context *ctx, size_t *smem) {
     static int done[64];
     *smem = (size_t)(T0_BLOCK / G) * 2 * CAP * sizeof(int);
-    return fill_grid(ctx, k_p2_tier<G, CAP, T0_BLOCK, false>, T0_BLOCK, *smem, done);
+    return fill_grid(ctx, k_p2_tier<G, CAP, T0_BLOCK, false, T0_LAZY>, T0_BLOCK, *smem, done);
 }
 template <int G, int CAP>
 static void t0_launch(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) {
-    k_p2_tier<G, CAP, T0_BLOCK, false><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0);
+    k_p2_tier<G, CAP, T0_BLOCK, false, T0_LAZY><<<g.g0, T0_BLOCK, g.s0, s>>>(a, 0);
 }
 static int t0_grid_of(Context *ctx, int v, size_t *smem) {
     switch (v) {
@@ -743,10 +997,10 @@ int t0_candidate(int v, int *lanes, int *cap) {
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     static int done1[64], done2[64];
     g->v0 = (ctx->tier0 >= 0 && ctx->tier0 < T0_CANDIDATES) ? ctx->tier0 : 0;
-    g->s1 = (size_t)(T1_BLOCK / T1_G) * 3 * T1_CAP * sizeof(int);
+    g->s1 = (size_t)(T1_BLOCK / T1_G) * (T1_STAGE ? 3 : 2) * T1_CAP * sizeof(int);
     g->s2 = (size_t)3 * T2_CAP * sizeof(int);
     g->g0 = t0_grid_of(ctx, g->v0, &g->s0);
-    g->g1 = fill_grid(ctx, k_p2_tier<T1_G, T1_CAP, T1_BLOCK, true>, T1_BLOCK, g->s1, done1);
+    g->g1 = fill_grid(ctx, k_p2_tier<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY>, T1_BLOCK, g->s1, done1);
     g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
     g->g3 = ctx->sm_count * 2;
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
@@ -797,7 +1051,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
     if (ev) cudaEventRecord(ev[1], s);
     launch_t0(a, g, s);
     if (ev) cudaEventRecord(ev[2], s);
-    k_p2_tier<T1_G, T1_CAP, T1_BLOCK, true><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
+    k_p2_tier<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
     if (ev) cudaEventRecord(ev[3], s);
     k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
     if (ev) cudaEventRecord(ev[4], s);
@@ -818,6 +1072,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     a.m = m; a.low = w.low; a.classes = w.classes; a.clear = w.clear; a.dim = w.dim; a.first = w.first;
     a.beta = w.beta; a.worklist = w.worklist; a.widelist = w.widelist; a.seg = w.seg;
     a.rec = w.rec; a.agg = w.agg; a.ntiles = w.ntiles; a.pool = w.pool; a.st = w.st;
+    a.stats = ctx->count_slots;
     // Phase I over a compacted list of the unresolved columns: every column
     // at first, then only those still unresolved after each sweep
 #ifndef OPH_PHASE1_LIST
@@ -889,13 +1144,30 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
                 p2_ms += t[1];
                 p2w_ms += t[2] + t[3] + t[4];
                 if (trace && b < worked)
-                    fprintf(stderr, "sweep %d: queued t0=%d t1=%d t2=%d t3=%d | adds t0=%llu t1=%llu t2=%llu t3=%llu | "
-                                    "ms p1=%.3f t0=%.3f t1=%.3f t2=%.3f t3=%.3f\n", hs.sweeps, hs.t_count[0],
+                    fprintf(stderr, "sweep %d: unresolved %d queued t0=%d t1=%d t2=%d t3=%d | adds t0=%llu t1=%llu t2=%llu "
+                                    "t3=%llu | ms p1=%.3f t0=%.3f t1=%.3f t2=%.3f t3=%.3f\n", hs.sweeps,
+                            a.ulist ? hs.ucount[hs.sweeps & 1] : -1, hs.t_count[0],
                             hs.t_count[1], hs.t_count[2], hs.t_count[3], hs.tier_adds[0] - before.tier_adds[0],
                             hs.tier_adds[1] - before.tier_adds[1], hs.tier_adds[2] - before.tier_adds[2],
                             hs.tier_adds[3] - before.tier_adds[3], t[0], t[1], t[2], t[3], t[4]);
             }
             p2_launches += worked;
+#if OPH_COUNTS
+            if (trace > 2 && worked) {
+                fprintf(stderr, "  additions per SM:");
+                for (int q = 0; q < 256; q++)
+                    if (hs.diag_sm[q] - before.diag_sm[q]) fprintf(stderr, " %d:%llu", q, hs.diag_sm[q] - before.diag_sm[q]);
+                fprintf(stderr, "\n");
+            }
+#endif
+            if (trace > 1 && worked) {
+                for (int t = 0; t < 2; t++) {
+                    const unsigned long long *d = hs.diag + 8 * t, *e = before.diag + 8 * t;
+                    fprintf(stderr, "  tier %d: adds rec %llu seg<=4 %llu mid %llu wide %llu | flushes %llu cancels %llu | "
+                                    "columns %llu rows in %llu\n", t, d[0] - e[0], d[1] - e[1], d[2] - e[2],
+                            d[3] - e[3], d[4] - e[4], d[5] - e[5], d[6] - e[6], d[7] - e[7]);
+                }
+            }
         }
         if (hs.error) { rc = OPH_ERR_BAD_INPUT; break; }
         if (hs.overflow) {

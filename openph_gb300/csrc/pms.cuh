@@ -37,6 +37,8 @@ struct PmsArgs {
     // Phase II tier-0 queue (the compacted list, or the worklist)
     int32_t *t0_list;
     int *t0_count;
+    // exact |P| + |T| + |T xor P| counters in the lazy tiers (profiling)
+    int stats;
 };
 
 // Launch geometry of the Phase II tiers (occupancy-derived, per device).

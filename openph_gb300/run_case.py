@@ -1,7 +1,8 @@
 """Reduce one generated workload a few times on the GPU (for profiler runs).
 
-    python -m openph_gb300.run_case [--workload rips_torus|lower_star|rips_cube]
+    python -m openph_gb300.run_case [--workload rips_torus|lower_star|rips_cube|batch]
                                     [--target-m M] [--algo pms] [--steps K]
+                                    [--tier0 LANES,CAP] [--profile]
 
 Prints one JSON line with the device time per reduction and the library's
 counters.  The matrix is device-resident before the first reduction.
@@ -28,6 +29,13 @@ def make(workload: str, target_m: int, seed: int):
     raise SystemExit(f"unknown workload {workload}")
 
 
+def _prof(ctx, args) -> dict:
+    if not args.profile:
+        return {}
+    p = ctx.last_profile()
+    return {"profile": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in p.items()}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="rips_torus", help="rips_torus, lower_star, rips_cube or batch")
@@ -35,6 +43,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--algo", default="pms")
     ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--tier0", default="", help="tier-0 lanes,capacity (default: the library's choice)")
+    ap.add_argument("--profile", action="store_true", help="print per-phase times of the last step")
     args = ap.parse_args()
 
     import torch
@@ -43,6 +53,9 @@ def main():
     bm = make(args.workload, args.target_m, args.seed)
     dev = torch.device("cuda", 0)
     ctx = api.Context(0)
+    if args.tier0:
+        ctx.set_tier0(*map(int, args.tier0.split(",")))
+    ctx.set_profile(args.profile)
     if args.workload == "batch":
         # --target-m is the number of complexes; one segmented pass each step
         col_off, colptr, rows = (torch.from_numpy(x).to(dev) for x in bm[:3])
@@ -53,7 +66,7 @@ def main():
                                        nnz, d_low.data_ptr(), None, args.algo) for _ in range(args.steps)]
         print(json.dumps({"workload": "batch", "count": len(bm[0]) - 1, "m": m, "nnz": nnz,
                           "device_ms": [o["device_ms"] for o in out], "sweeps": out[-1]["sweeps"],
-                          "additions": out[-1]["additions"]}))
+                          "additions": out[-1]["additions"], **_prof(ctx, args)}))
         ctx.close()
         return
     d_colptr = torch.from_numpy(bm.colptr).to(dev)
@@ -66,7 +79,8 @@ def main():
                                      args.algo))
     print(json.dumps({"workload": args.workload, "m": bm.m, "nnz": bm.nnz, "algo": args.algo,
                       "device_ms": [o["device_ms"] for o in out], "sweeps": out[-1]["sweeps"],
-                      "additions": out[-1]["additions"], "pivots": int((d_low.cpu().numpy() >= 0).sum())}))
+                      "additions": out[-1]["additions"], "pivots": int((d_low.cpu().numpy() >= 0).sum()),
+                      **_prof(ctx, args)}))
     ctx.close()
 
 

@@ -197,3 +197,44 @@ def test_autotune_picks_a_candidate(cuda_lib):
     np.testing.assert_array_equal(low, oracle.twist(bm)[0])
     with pytest.raises(OphError):
         Context(0).set_tier0(3, 100)
+
+
+@pytest.fixture(scope="module")
+def torus_200k():
+    bm = cx.rips_torus(400, 200_000, seed=5)
+    low, ess, st = oracle.twist(bm)
+    return bm, low, ess, st
+
+
+@pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (16, 256)])
+def test_long_chains_every_tier0_candidate(cuda_lib, torus_200k, lanes, cap):
+    """Top-dimension chains of up to ~200 rows: lazy columns with pending
+    toggles of 4 to 16 lanes, flushes, wide pivots and tier hand-offs."""
+    from openph_gb300.api import Context
+    bm, want, want_ess, _ = torus_200k
+    with Context(0) as c:
+        c.set_tier0(lanes, cap)
+        low, ess, _ = c.reduce(bm, "pms")
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_slot_counters_match_twist(cuda_lib, torus_200k):
+    """With slot tracking on, the device's |P| + |T| + |T xor P| total agrees
+    with the twist oracle's to 0.5% (pms and twist add the same pivots, up to
+    the few extra additions pms makes on columns twist clears), and the
+    result is unchanged."""
+    from openph_gb300.api import Context
+    bm, want, want_ess, st = torus_200k
+    with Context(0) as c:
+        c.set_profile(True, slots=True)
+        low, ess, info = c.reduce(bm, "pms")
+        prof = c.last_profile()
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+    slots = sum(prof["tier_slots"])
+    want_slots = st["slots_read"] + st["slots_written"]
+    assert sum(prof["tier_additions"]) == info["additions"]
+    assert abs(info["additions"] - st["additions"]) <= 0.005 * st["additions"]
+    assert abs(slots - want_slots) <= 0.005 * want_slots
+    assert prof["tier_slots"][0] > 0
