@@ -414,8 +414,9 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 //   tier 2  a CTA per column,   CAP 8192     (block-wide merge)
 //   tier 3  a CTA per column,   buffers in the pool (no limit)
 // Pivots of at most G entries (most are apparent pairs of 3 entries) are held
-// one per lane and merged without staging (merge_xor_seg / merge_xor_thr).  The queues
-// ping-pong between the worklist and widelist arrays.  Each addition costs
+// one per lane and merged without staging, by runs or thresholds
+// (merge_xor_seg / merge_xor_thr).  The queues ping-pong between the worklist
+// and widelist arrays.  Each addition costs
 // one dependent round trip when the pivot has at most four entries (its
 // record carries them, with left[] for the beta check) and two otherwise;
 // reading G ints past a segment start stays in bounds through the pool's
