@@ -735,7 +735,7 @@ __device__ __forceinline__ void tier_stats(const PmsArgs &a, int tier, long long
 // and, with STAGE, a C buffer into which a pivot wider than the group is
 // staged; without it (tier 0) such a pivot is searched in the store.
 template <int G, int CAP, int BLOCK, bool STAGE, bool LAZY>
-__global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
+__device__ __forceinline__ void p2_tier_body(const PmsArgs &a, int tier) {
     if (a.st->converged) return;
     extern __shared__ int smem[];
     auto tile = cg::tiled_partition<G>(cg::this_thread_block());
@@ -780,6 +780,26 @@ __global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
 #endif
         }
     }
+}
+
+// Tier 0 (the autotuned narrow tier) with its occupancy target: resident
+// columns hide the record reads of the chains, so the register budget is
+// held to what T0_MINB blocks of BLOCK threads per SM allow.
+#ifndef OPH_T0_MINB
+#define OPH_T0_MINB 0
+#endif
+template <int G, int CAP, int BLOCK, bool STAGE, bool LAZY>
+#if OPH_T0_MINB > 0
+__global__ void __launch_bounds__(BLOCK, OPH_T0_MINB) k_p2_tier(PmsArgs a, int tier) {
+#else
+__global__ void __launch_bounds__(BLOCK) k_p2_tier(PmsArgs a, int tier) {
+#endif
+    p2_tier_body<G, CAP, BLOCK, STAGE, LAZY>(a, tier);
+}
+// Tier 1 (a warp per column; its shared buffers bound the occupancy).
+template <int G, int CAP, int BLOCK, bool STAGE, bool LAZY>
+__global__ void __launch_bounds__(BLOCK) k_p2_tier1(PmsArgs a, int tier) {
+    p2_tier_body<G, CAP, BLOCK, STAGE, LAZY>(a, tier);
 }
 
 // Tiers 2 and 3: the whole CTA on one column.  With cap > 0 the column and
@@ -955,7 +975,7 @@ static int fill_grid(Context *ctx, K kernel, int block, size_t smem, int *done) 
 struct T0Cand {
     int lanes, cap;
 };
-static const T0Cand kT0[T0_CANDIDATES] = {{8, 128}, {4, 128}, {8, 64}, {8, 256}, {16, 128}, {16, 256}};
+static const T0Cand kT0[T0_CANDIDATES] = {{8, 128}, {4, 128}, {8, 64}, {8, 256}, {16, 128}, {16, 256}, {32, 128}};
 
 template <int G, int CAP>
 static int t0_grid(Context *ctx, size_t *smem) {
@@ -974,6 +994,7 @@ static int t0_grid_of(Context *ctx, int v, size_t *smem) {
         case 3: return t0_grid<8, 256>(ctx, smem);
         case 4: return t0_grid<16, 128>(ctx, smem);
         case 5: return t0_grid<16, 256>(ctx, smem);
+        case 6: return t0_grid<32, 128>(ctx, smem);
         default: return t0_grid<8, 128>(ctx, smem);
     }
 }
@@ -984,6 +1005,7 @@ static void launch_t0(const PmsArgs &a, const SweepGrids &g, cudaStream_t s) {
         case 3: t0_launch<8, 256>(a, g, s); break;
         case 4: t0_launch<16, 128>(a, g, s); break;
         case 5: t0_launch<16, 256>(a, g, s); break;
+        case 6: t0_launch<32, 128>(a, g, s); break;
         default: t0_launch<8, 128>(a, g, s); break;
     }
 }
@@ -1001,7 +1023,7 @@ int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     g->s1 = (size_t)(T1_BLOCK / T1_G) * (T1_STAGE ? 3 : 2) * T1_CAP * sizeof(int);
     g->s2 = (size_t)3 * T2_CAP * sizeof(int);
     g->g0 = t0_grid_of(ctx, g->v0, &g->s0);
-    g->g1 = fill_grid(ctx, k_p2_tier<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY>, T1_BLOCK, g->s1, done1);
+    g->g1 = fill_grid(ctx, k_p2_tier1<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY>, T1_BLOCK, g->s1, done1);
     g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
     g->g3 = ctx->sm_count * 2;
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
@@ -1052,7 +1074,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
     if (ev) cudaEventRecord(ev[1], s);
     launch_t0(a, g, s);
     if (ev) cudaEventRecord(ev[2], s);
-    k_p2_tier<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
+    k_p2_tier1<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
     if (ev) cudaEventRecord(ev[3], s);
     k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
     if (ev) cudaEventRecord(ev[4], s);

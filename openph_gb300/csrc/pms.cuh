@@ -42,7 +42,7 @@ struct PmsArgs {
 };
 
 // Launch geometry of the Phase II tiers (occupancy-derived, per device).
-constexpr int T0_CANDIDATES = 6;
+constexpr int T0_CANDIDATES = 7;
 // Lanes per column and shared capacity of tier-0 candidate v (-1 if none).
 int t0_candidate(int v, int *lanes, int *cap);
 

@@ -175,7 +175,7 @@ def test_rips_torus_1m(ctx):
     assert info["regrows"] == 0
 
 
-@pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256)])
+@pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256), (32, 128)])
 def test_every_tier0_candidate_is_exact(cuda_lib, lanes, cap):
     from openph_gb300.api import Context
     bm = cx.lower_star_image(48, 48, seed=6, sigma=3.0)
@@ -192,7 +192,7 @@ def test_autotune_picks_a_candidate(cuda_lib):
     bm = cx.rips_cube(30, seed=4)
     with Context(0) as c:
         choice = c.autotune(bm)
-        assert (choice["lanes"], choice["cap"]) in {(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256)}
+        assert (choice["lanes"], choice["cap"]) in {(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256), (32, 128)}
         low, _, _ = c.reduce(bm, "pms")
     np.testing.assert_array_equal(low, oracle.twist(bm)[0])
     with pytest.raises(OphError):
@@ -206,7 +206,7 @@ def torus_200k():
     return bm, low, ess, st
 
 
-@pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (16, 256)])
+@pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (16, 256), (32, 128)])
 def test_long_chains_every_tier0_candidate(cuda_lib, torus_200k, lanes, cap):
     """Top-dimension chains of up to ~200 rows: lazy columns with pending
     toggles of 4 to 16 lanes, flushes, wide pivots and tier hand-offs."""
