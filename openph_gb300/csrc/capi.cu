@@ -112,6 +112,9 @@ __global__ void k_finalize2(const int32_t *__restrict__ low, int64_t m, const in
     }
 }
 
+// Tracker entries kept per reduction (the reference's arrays hold m + 1).
+constexpr int64_t MAX_TRACKED = 1 << 16;
+
 __global__ void k_fill_i32(int32_t *p, int64_t n, int32_t v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         p[i] = v;
@@ -524,8 +527,8 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
     int32_t *d_rows = (int32_t *)ctx_alloc(ctx, S_ROWS, sizeof(int32_t) * (nnz > 0 ? nnz : 1));
     int32_t *d_out = (int32_t *)ctx_alloc(ctx, S_ESS, sizeof(int32_t) * 2 * mm);
     int32_t *d_lt = (int32_t *)ctx_alloc(ctx, S_LOWTRUE, sizeof(int32_t) * 2 * mm);
-    double *d_acc = (double *)ctx_alloc(ctx, S_TRACK, sizeof(double) * 16);
-    if (!d_r1 || !d_c1 || !d_colptr || !d_rows || !d_out || !d_lt || !d_acc) return OPH_ERR_OOM;
+    double *d_acc = nullptr;
+    if (!d_r1 || !d_c1 || !d_colptr || !d_rows || !d_out || !d_lt) return OPH_ERR_OOM;
     if (nnz > 0) {
         OPH_CUDA_TRY(cudaMemcpyAsync(d_r1, h_rows_in, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
         OPH_CUDA_TRY(cudaMemcpyAsync(d_c1, h_cols_in, sizeof(int) * nnz, cudaMemcpyHostToDevice, s));
@@ -544,43 +547,86 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
     w.colptr = d_colptr;
     w.rows = d_rows;
     const bool track = h_low_true && (err_linf || err_lone || err_redu || err_ess);
+    int32_t *lt0 = d_lt, *esst = d_lt + mm;
+    if (track && m > 0) {
+        // low_true arrives 1-based and is compared 0-based like the
+        // reference (openph.cu:99-122); ess_true follows from it
+        OPH_CUDA_TRY(cudaMemcpyAsync(lt0, h_low_true, sizeof(int) * m, cudaMemcpyHostToDevice, s));
+        k_shift_down<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, lt0);
+        k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 0);
+        k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 1);
+    }
+    // pms records an entry per sweep (pms.cu:16,106); the other algorithms
+    // record the initial and the final state
+    Tracking tr;
+    const bool per_sweep = track && m > 0 && algo == OPH_ALGO_PMS;
+    if (per_sweep) {
+        tr.low_true = lt0;
+        tr.ess_true = esst;
+        tr.slots = (int)std::min<int64_t>(m + 1, MAX_TRACKED);
+        tr.ess_hat = (uint8_t *)ctx_alloc(ctx, S_ESSHAT, (size_t)m);
+        tr.acc = (double *)ctx_alloc(ctx, S_TRACK, sizeof(double) * (16 + 4 * (size_t)tr.slots));
+        if (!tr.ess_hat || !tr.acc) return OPH_ERR_OOM;
+        tr.acc += 16;
+        ctx->track = &tr;
+    } else if (track && m > 0) {
+        d_acc = (double *)ctx_alloc(ctx, S_TRACK, sizeof(double) * (16 + 4 * 2));
+        if (!d_acc) return OPH_ERR_OOM;
+    }
     Outputs o;
     o.low = d_out;
     o.one_based = 1;
     o.ess = d_out + mm;
     oph_info info{};
     rc = reduce_core(ctx, algo, w, o, &info);
+    ctx->track = nullptr;
     if (rc) return rc;
     if (m > 0) {
         OPH_CUDA_TRY(cudaMemcpyAsync(h_low, d_out, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
         if (h_ess) OPH_CUDA_TRY(cudaMemcpyAsync(h_ess, d_out + mm, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
     }
+    const int it = info.num_iters > 0 ? info.num_iters : 1;
     double acc[16] = {0};
+    std::vector<double> entries;
     if (track && m > 0) {
-        // progress trackers for the final state (tracker.cu:92-134); low_true
-        // arrives 1-based and is compared 0-based like the reference
-        int32_t *lt0 = d_lt, *esst = d_lt + mm;
-        OPH_CUDA_TRY(cudaMemcpyAsync(lt0, h_low_true, sizeof(int) * m, cudaMemcpyHostToDevice, s));
-        k_shift_down<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, lt0);
-        k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 0);
-        k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 1);
-        OPH_CUDA_TRY(cudaMemsetAsync(d_acc, 0, sizeof(double) * 16, s));
-        k_tracker<<<grid_for(ctx, m), 256, 0, s>>>(w.low, lt0, d_out + mm, esst, m, d_acc);
-        OPH_CUDA_TRY(cudaMemcpyAsync(acc, d_acc, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
+        // the final state, with the final essential estimate
+        double *fin = per_sweep ? tr.acc - 16 : d_acc;
+        OPH_CUDA_TRY(cudaMemsetAsync(fin, 0, sizeof(double) * 16, s));
+        k_tracker<<<grid_for(ctx, m), 256, 0, s>>>(w.low, lt0, d_out + mm, esst, m, fin);
+        OPH_CUDA_TRY(cudaMemcpyAsync(acc, fin, sizeof(double) * 16, cudaMemcpyDeviceToHost, s));
+        if (per_sweep) {
+            entries.resize(4 * (size_t)tr.slots);
+            OPH_CUDA_TRY(cudaMemcpyAsync(entries.data(), tr.acc, sizeof(double) * entries.size(),
+                                         cudaMemcpyDeviceToHost, s));
+        }
     }
     OPH_CUDA_TRY(cudaStreamSynchronize(s));
-    const int it = info.num_iters > 0 ? info.num_iters : 1;
     if (num_iters) *num_iters = it;
+    const int last = it - 1 < m ? it - 1 : m;
     if (time_track && m >= 1) {
         time_track[0] = 0.0f;
-        time_track[it - 1 < m ? it - 1 : m] = info.device_ms;
+        if (per_sweep) {
+            for (int k = 1; k < last && k - 1 < (int)tr.sweep_ms.size(); k++) time_track[k] = tr.sweep_ms[k - 1];
+            time_track[last] = (int)tr.sweep_ms.size() >= last ? tr.sweep_ms[last - 1] : info.device_ms;
+        } else {
+            time_track[last] = info.device_ms;
+        }
     }
     if (track && m > 0) {
-        const int last = it - 1 < m ? it - 1 : m;
-        if (err_lone) err_lone[last] = (float)(acc[0] / acc[4]);
-        if (err_linf) err_linf[last] = (float)(acc[1] / acc[5]);
-        if (err_redu) err_redu[last] = 0.0f;
-        if (err_ess) err_ess[last] = acc[2] == acc[3] ? 1.0f : (float)(acc[3] / acc[2]);
+        // normalised like openph.cu:184-193 (by the 1-based low_true's norms);
+        // err_ess = ess_true / ess_hat, 1 when equal (tracker.cu:124-133)
+        const double n1 = acc[4], ninf = acc[5], esst_sum = acc[3];
+        auto put = [&](int k, double lone, double linf, double unclassified, double ess_hat) {
+            if (err_lone) err_lone[k] = (float)(lone / n1);
+            if (err_linf) err_linf[k] = (float)(linf / ninf);
+            if (err_redu) err_redu[k] = (float)(unclassified / (double)m);
+            if (err_ess) err_ess[k] = ess_hat == esst_sum ? 1.0f : (float)(esst_sum / ess_hat);
+        };
+        if (per_sweep)
+            for (int k = 0; k < last && k < tr.slots; k++)
+                put(k, entries[4 * k], entries[4 * k + 1], entries[4 * k + 2], entries[4 * k + 3]);
+        // the last entry: the final lows, every column classified
+        put(last, acc[0], acc[1], 0.0, acc[2]);
     }
     return OPH_OK;
 }

@@ -1,5 +1,6 @@
 // Host-side internals shared by the translation units of libopenph_gb300.
 #pragma once
+#include <vector>
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -67,6 +68,20 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
 void *ctx_alloc(Context *ctx, int slot, size_t bytes);
 int ctx_sync_status(Context *ctx, Work &w, DevStatus *out);
 
+// Per-sweep progress trackers of a pms reduction (the reference's track(),
+// src/cuda/algorithms/tracker.cu:92-134, called once per iteration by
+// pms.cu:16,106).  Set on the context for one reduction by oph_openph when
+// the caller passes low_true and tracker arrays.
+struct Tracking {
+    const int32_t *low_true = nullptr;  // device, 0-based (-1 = none)
+    const int32_t *ess_true = nullptr;  // device
+    uint8_t *ess_hat = nullptr;         // device, m: running essential estimate
+    double *acc = nullptr;              // device, 4 per slot: sum |low - low_true|,
+                                        //   max |.|, #unclassified, sum ess_hat
+    int slots = 0;                      // slot 0 = before Phase 0, slot k = after sweep k
+    std::vector<float> sweep_ms;        // device time of each sweep that ran
+};
+
 struct Context {
     int device = 0;
     int sm_count = 0;
@@ -85,13 +100,14 @@ struct Context {
     oph_profile prof{};             // last reduction
     int launches = 0;               // kernels launched by the current reduction
     int tier0 = 0;                  // Phase II tier-0 candidate (autotuned)
+    Tracking *track = nullptr;      // per-sweep trackers for the current reduction
 };
 
 // buffer slots of Context::bufs
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_NSLOTS
 };
 
 }  // namespace oph

@@ -746,16 +746,12 @@ __device__ __forceinline__ void p2_tier_body(const PmsArgs &a, int tier) {
     const int count = tier == 0 ? *a.t0_count : a.st->t_count[tier];
     long long adds = 0, slots = 0;
     LazyDiag dg{};
-#ifndef OPH_T0_GRAB
-#define OPH_T0_GRAB 1
-#endif
     for (;;) {
         int idx = 0;
-        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->t_cursor[tier], OPH_T0_GRAB);
+        if (tile.thread_rank() == 0) idx = atomicAdd(&a.st->t_cursor[tier], 1);
         idx = tile.shfl(idx, 0);
         if (idx >= count) break;
-        const int end = min(idx + OPH_T0_GRAB, count);
-        for (; idx < end; idx++) {
+        {
             int *C = STAGE ? buf + 2 * CAP : nullptr;
             int *qn = &a.st->t_count[tier + 1];
             if (!LAZY)
@@ -1044,6 +1040,53 @@ __global__ void k_iota(int32_t *p, int64_t n) {
         p[i] = (int32_t)i;
 }
 
+// ---------------------------------------------------------------- trackers
+// The reference's essential estimate after an iteration (ess_hat,
+// src/cuda/algorithms/kernels.cu:114-124): a row that is some column's low,
+// and both ends of every known pivot pair, are not essential.  Kept as one
+// byte per column, all ones before Phase 0.
+__global__ void k_track_ess(PmsArgs a, uint8_t *__restrict__ ess_hat) {
+    if (a.st->converged) return;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.m; j += (int64_t)gridDim.x * blockDim.x) {
+        const int lj = a.low[j];
+        if (lj >= 0) ess_hat[lj] = 0;
+        const int pc = a.rec[j].col;
+        if (pc >= 0) {
+            ess_hat[pc] = 0;
+            ess_hat[j] = 0;
+        }
+    }
+}
+
+// The sums behind one tracker entry (tracker.cu:92-134): sum and maximum of
+// |low - low_true| (0-based, -1 = none), columns still unclassified
+// (classes == 0), and the size of the essential estimate.
+__global__ void k_track_sum(PmsArgs a, const int32_t *__restrict__ low_true, const uint8_t *__restrict__ ess_hat,
+                            double *acc, int check_converged) {
+    if (check_converged && a.st->converged) return;
+    double s = 0, mx = 0, un = 0, es = 0;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < a.m; j += (int64_t)gridDim.x * blockDim.x) {
+        const double d = fabs((double)a.low[j] - (double)low_true[j]);
+        s += d;
+        mx = fmax(mx, d);
+        un += a.classes[j] == 0 ? 1.0 : 0.0;
+        es += ess_hat[j];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        un += __shfl_xor_sync(0xffffffffu, un, o);
+        es += __shfl_xor_sync(0xffffffffu, es, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[0], s);
+        // maxima of non-negative doubles compare as their bit patterns
+        atomicMax((unsigned long long *)&acc[1], (unsigned long long)__double_as_longlong(mx));
+        atomicAdd(&acc[2], un);
+        atomicAdd(&acc[3], es);
+    }
+}
+
 // ev (optional, 6 events): before Phase I, after Phase I, after each tier.
 static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t s, cudaEvent_t *ev, int parity) {
     PmsArgs a = a0;
@@ -1081,6 +1124,13 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
     k_p2_block<0, T3_BLOCK><<<g.g3, T3_BLOCK, 0, s>>>(a, 3);
     k_count_sweep<<<1, 1, 0, s>>>(a.st);
     if (ev) cudaEventRecord(ev[5], s);
+}
+
+// The tracker entry of sweep `slot` (1-based), skipped once converged.
+static void launch_track(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, Tracking *t, int slot) {
+    if (!t || slot >= t->slots) return;
+    k_track_ess<<<g.m, 256, 0, s>>>(a, t->ess_hat);
+    k_track_sum<<<g.m, 256, 0, s>>>(a, t->low_true, t->ess_hat, t->acc + 4 * slot, 1);
 }
 
 void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int parity) {
@@ -1121,6 +1171,14 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     OPH_CUDA_TRY(cudaMemsetAsync(w.classes, 0, m, s));
     OPH_CUDA_TRY(cudaMemsetAsync(w.clear, 0, m, s));
 
+    Tracking *tr = ctx->track;
+    if (tr) {
+        // entry 0: the state before Phase 0, every column its own estimate
+        OPH_CUDA_TRY(cudaMemsetAsync(tr->ess_hat, 1, m, s));
+        OPH_CUDA_TRY(cudaMemsetAsync(tr->acc, 0, sizeof(double) * 4 * tr->slots, s));
+        k_track_sum<<<g.m, 256, 0, s>>>(a, tr->low_true, tr->ess_hat, tr->acc, 0);
+        tr->sweep_ms.clear();
+    }
     cudaEventRecord(ctx->ev[0], s);
     launch_phase0(a, 0, m, g.m, s);
     ctx->launches++;
@@ -1129,7 +1187,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     // per-phase events: 6 per sweep, reused batch after batch
     constexpr int MAX_BATCH = 16;
     const int nev = 6 * MAX_BATCH + 1;
-    if ((ctx->profile || getenv("OPH_TRACE")) && ctx->pev_n < nev) {
+    if ((ctx->profile || ctx->track || getenv("OPH_TRACE")) && ctx->pev_n < nev) {
         ctx->pev = (cudaEvent_t *)realloc(ctx->pev, sizeof(cudaEvent_t) * nev);
         for (int i = ctx->pev_n; i < nev; i++) cudaEventCreate(&ctx->pev[i]);
         ctx->pev_n = nev;
@@ -1137,7 +1195,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     // OPH_TRACE=1: one sweep per batch, per-tier queue sizes, additions and
     // times printed to stderr (diagnostics only)
     static const int trace = getenv("OPH_TRACE") ? atoi(getenv("OPH_TRACE")) : 0;
-    const bool timed = ctx->profile || trace;
+    const bool timed = ctx->profile || trace || tr;
     if (timed) cudaEventRecord(ctx->pev[6 * MAX_BATCH], s);  // end of Phase 0
 
     const int max_sweeps = ctx->max_sweeps > 0 ? ctx->max_sweeps : 1 << 20;
@@ -1151,6 +1209,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         DevStatus before = hs;
         for (int b = 0; b < nb; b++) {
             launch_sweep_ev(a, g, s, timed ? ctx->pev + 6 * b : nullptr, sweeps_launched + b);
+            launch_track(a, g, s, tr, sweeps_launched + b + 1);
             ctx->launches += KERNELS_PER_SWEEP;
         }
         sweeps_launched += nb;
@@ -1166,6 +1225,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
                 p1_ms += t[0];
                 p2_ms += t[1];
                 p2w_ms += t[2] + t[3] + t[4];
+                if (tr && b < worked) tr->sweep_ms.push_back(t[0] + t[1] + t[2] + t[3] + t[4]);
                 if (trace && b < worked)
                     fprintf(stderr, "sweep %d: unresolved %d queued t0=%d t1=%d t2=%d t3=%d | adds t0=%llu t1=%llu t2=%llu "
                                     "t3=%llu | ms p1=%.3f t0=%.3f t1=%.3f t2=%.3f t3=%.3f\n", hs.sweeps,

@@ -238,3 +238,38 @@ def test_slot_counters_match_twist(cuda_lib, torus_200k):
     assert abs(info["additions"] - st["additions"]) <= 0.005 * st["additions"]
     assert abs(slots - want_slots) <= 0.005 * want_slots
     assert prof["tier_slots"][0] > 0
+
+
+def test_pms_trackers_per_sweep(cuda_lib):
+    """openph()'s progress outputs for pms: one entry per sweep as in the
+    reference's track() calls (pms.cu:16,106, tracker.cu:92-134).  Entry 0
+    (before Phase 0) is checked exactly against numpy, the last entry is the
+    exact final state, and the entries between are finite progress values."""
+    bm = cx.rips_torus(400, 200_000, seed=5)
+    want, want_ess, _ = oracle.twist(bm)
+    r, c = bm.to_coo1()
+    low_true = (want + 1).astype(np.int32)
+    low, ess, linf, lone, redu, eerr, tt, it = ph("pms", r, c, bm.m, 0, low_true)
+    np.testing.assert_array_equal(low, low_true)
+    n = int(it[0])
+    assert n >= 3
+    # entry 0: the initial lows (last row of every column, -1 when empty)
+    lens = np.diff(bm.colptr)
+    init = np.where(lens > 0, bm.rows[np.maximum(bm.colptr[1:] - 1, 0)], -1).astype(np.float64)
+    d = np.abs(init - want)
+    n1, ninf = np.abs(low_true).sum(dtype=np.float64), np.abs(low_true).max()
+    assert lone[0] == pytest.approx(d.sum() / n1, rel=1e-6)
+    assert linf[0] == pytest.approx(d.max() / ninf, rel=1e-6)
+    assert redu[0] == pytest.approx(1.0)
+    ess_true = np.ones(bm.m)
+    ess_true[want >= 0] = 0
+    ess_true[want[want >= 0]] = 0
+    assert eerr[0] == pytest.approx(ess_true.sum() / bm.m, rel=1e-6)
+    # the last entry: exact
+    assert (lone[n - 1], linf[n - 1], redu[n - 1], eerr[n - 1]) == (0.0, 0.0, 0.0, 1.0)
+    # between: progress values in range, positive sweep times, nothing past n
+    for arr in (lone, linf, redu):
+        assert np.all(np.isfinite(arr[:n])) and np.all(arr[:n] >= 0)
+    assert np.all(redu[:n] <= 1.0) and np.all((eerr[:n] > 0) & (eerr[:n] <= 1.0))
+    assert np.all(tt[1:n] > 0) and tt[0] == 0
+    assert np.all(lone[n:] == -1)
