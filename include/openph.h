@@ -242,6 +242,30 @@ int oph_context_set_tier0(oph_context *ctx, int32_t lanes, int32_t cap);
  * paths without faulting anything. */
 int oph_context_set_limits(oph_context *ctx, int32_t max_sweeps, int64_t initial_pool_bytes);
 
+/* ------------------------------------------------- complexes on the device
+ * The reference reads boundary matrices produced on the host by Javaplex
+ * (example_factory.m:17-114, stream2cmo.m:1-26); no counterpart in its C
+ * code.  These build the filtered complex straight into device buffers, in
+ * the reduction's input layout (0-based CSC, columns in filtration order
+ * (value, dimension, vertex tuple), rows ascending), identical to the host
+ * generators of openph_gb300 (gen/ophgen.c: oph_rips, oph_lower_star).
+ * Call once with d_colptr == NULL for the sizes (*m, *nnz), allocate
+ * d_colptr[m + 1], d_rows[nnz] and optionally d_value[m] (FP64 filtration
+ * values), then call again with them.  Work runs on the context's stream and
+ * is complete on return; scratch is allocated from the stream's memory pool
+ * and released before returning. */
+#define OPH_GEN_MAX_POINTS 16384
+/* Vietoris-Rips complex of dimension <= 2 of n points (d_points: n x d FP64,
+ * row-major, on the device) with edges of length <= threshold (+inf: the
+ * full 2-skeleton); value = the largest pairwise Euclidean distance. */
+int oph_rips_device(oph_context *ctx, const double *d_points, int n, int d, double threshold, int64_t *m,
+                    int64_t *nnz, int64_t *d_colptr, int32_t *d_rows, double *d_value);
+/* Lower-star filtration of an h x w FP32 image (row-major, on the device) on
+ * the Freudenthal triangulation (diagonals (y,x)-(y+1,x+1)); value of a
+ * simplex = the largest value of its vertices.  h, w >= 2, h * w < 2^20. */
+int oph_lower_star_device(oph_context *ctx, const float *d_image, int h, int w, int64_t *m, int64_t *nnz,
+                          int64_t *d_colptr, int32_t *d_rows, double *d_value);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,6 +104,10 @@ def lib():
         L.oph_context_set_limits.argtypes = [vp, C.c_int32, C.c_int64]
         L.oph_reduce.argtypes = [vp, C.c_int, C.c_int64, i64, vp, i32, vp, vp, C.POINTER(Info)]
         L.oph_reduce_device.argtypes = [vp, C.c_int, C.c_int64, vp, vp, vp, vp, vp, C.POINTER(Info)]
+        L.oph_rips_device.argtypes = [vp, vp, C.c_int, C.c_int, C.c_double, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64), vp, vp, vp]
+        L.oph_lower_star_device.argtypes = [vp, vp, C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                            vp, vp, vp]
         L.oph_reduce_batch.argtypes = [vp, C.c_int, C.c_int32, i64, i64, vp, i32, vp, C.POINTER(Info)]
         L.oph_reduce_batch_device.argtypes = [vp, C.c_int, C.c_int32, vp, vp, vp, C.c_int64, C.c_int64, vp, vp,
                                               C.POINTER(Info)]
@@ -295,6 +299,39 @@ class Context:
         if rc != OPH_OK:
             raise OphError(rc, f"oph_reduce_batch_device({algo!r})")
         return info.as_dict()
+
+    def rips_device(self, points_ptr: int, n: int, d: int, threshold: float, alloc):
+        """Build the Rips complex of n x d FP64 points already on the device
+        (raw pointer).  ``alloc(m, nnz)`` returns raw device pointers
+        (colptr, rows, value) for the output (value may be None); returns
+        (m, nnz)."""
+        m, nnz = C.c_int64(), C.c_int64()
+        rc = lib().oph_rips_device(self._h, C.c_void_p(points_ptr), int(n), int(d), float(threshold), C.byref(m),
+                                   C.byref(nnz), None, None, None)
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_rips_device")
+        colptr, rows, value = alloc(m.value, nnz.value)
+        rc = lib().oph_rips_device(self._h, C.c_void_p(points_ptr), int(n), int(d), float(threshold), C.byref(m),
+                                   C.byref(nnz), C.c_void_p(colptr), C.c_void_p(rows),
+                                   C.c_void_p(value) if value else None)
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_rips_device")
+        return m.value, nnz.value
+
+    def lower_star_device(self, image_ptr: int, h: int, w: int, alloc):
+        """Build the lower-star complex of an h x w FP32 image on the device;
+        ``alloc`` as for rips_device; returns (m, nnz)."""
+        m, nnz = C.c_int64(), C.c_int64()
+        rc = lib().oph_lower_star_device(self._h, C.c_void_p(image_ptr), int(h), int(w), C.byref(m), C.byref(nnz),
+                                         None, None, None)
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_lower_star_device")
+        colptr, rows, value = alloc(m.value, nnz.value)
+        rc = lib().oph_lower_star_device(self._h, C.c_void_p(image_ptr), int(h), int(w), C.byref(m), C.byref(nnz),
+                                         C.c_void_p(colptr), C.c_void_p(rows), C.c_void_p(value) if value else None)
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_lower_star_device")
+        return m.value, nnz.value
 
     def autotune(self, bm):
         """Pick the narrow-tier lanes/capacity on a representative matrix."""

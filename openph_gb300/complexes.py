@@ -192,6 +192,80 @@ def lower_star(image: np.ndarray) -> BoundaryMatrix:
     return _take(cx, {"kind": "lower_star", "shape": (h, w)})
 
 
+# ------------------------------------------------------ on the device
+@dataclass
+class DeviceMatrix:
+    """A boundary matrix built in device memory (torch tensors): 0-based
+    CSC, columns in filtration order, and the FP64 filtration values."""
+
+    colptr: object  # torch.int64[m + 1]
+    rows: object  # torch.int32[nnz]
+    values: object  # torch.float64[m]
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def m(self) -> int:
+        return int(self.colptr.shape[0]) - 1
+
+    @property
+    def nnz(self) -> int:
+        return int(self.rows.shape[0])
+
+    def to_host(self) -> BoundaryMatrix:
+        return BoundaryMatrix(self.colptr.cpu().numpy(), self.rows.cpu().numpy(), self.values.cpu().numpy(),
+                              None, dict(self.meta))
+
+
+def _device_build(ctx, device, build):
+    import torch
+
+    from . import api
+    own = ctx is None
+    if own:
+        ctx = api.Context(device.index or 0)
+    try:
+        out = {}
+
+        def alloc(m, nnz):
+            out["colptr"] = torch.empty(m + 1, dtype=torch.int64, device=device)
+            out["rows"] = torch.empty(max(nnz, 1), dtype=torch.int32, device=device)
+            out["values"] = torch.empty(max(m, 1), dtype=torch.float64, device=device)
+            return out["colptr"].data_ptr(), out["rows"].data_ptr(), out["values"].data_ptr()
+
+        # inputs written on torch's stream must land before the context's
+        # stream reads them
+        torch.cuda.current_stream(device).synchronize()
+        m, nnz = build(ctx, alloc)
+        return out["colptr"], out["rows"][:nnz], out["values"][:m]
+    finally:
+        if own:
+            ctx.close()
+
+
+def rips_device(points, threshold: float = float("inf"), ctx=None, device=None) -> DeviceMatrix:
+    """The Rips complex of ``rips`` built on the GPU from points (a numpy
+    array or a CUDA tensor, n x d); identical output, device-resident."""
+    import torch
+    device = torch.device(device or "cuda")
+    pts = torch.as_tensor(points, dtype=torch.float64).to(device).contiguous()
+    n, d = pts.shape
+    colptr, rows, values = _device_build(
+        ctx, device, lambda c, alloc: c.rips_device(pts.data_ptr(), n, d, threshold, alloc))
+    return DeviceMatrix(colptr, rows, values, {"kind": "rips", "n_points": n, "threshold": threshold})
+
+
+def lower_star_device(image, ctx=None, device=None) -> DeviceMatrix:
+    """The lower-star complex of ``lower_star`` built on the GPU from an
+    h x w FP32 image (numpy or CUDA tensor)."""
+    import torch
+    device = torch.device(device or "cuda")
+    img = torch.as_tensor(image, dtype=torch.float32).to(device).contiguous()
+    h, w = img.shape
+    colptr, rows, values = _device_build(ctx, device,
+                                         lambda c, alloc: c.lower_star_device(img.data_ptr(), h, w, alloc))
+    return DeviceMatrix(colptr, rows, values, {"kind": "lower_star", "shape": (h, w)})
+
+
 # --------------------------------------------------- the benchmark shapes
 def rips_cube(n_points: int = 50, seed: int = 1) -> BoundaryMatrix:
     """Full 2-skeleton Rips complex of n points uniform in [0,1]^3."""

@@ -18,7 +18,6 @@
 
 using namespace oph;
 
-struct oph_context : public oph::Context {};
 
 namespace oph {
 

@@ -111,3 +111,6 @@ enum Slot {
 };
 
 }  // namespace oph
+
+// The C ABI's opaque context is the library's Context.
+struct oph_context : public oph::Context {};
