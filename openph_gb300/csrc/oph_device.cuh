@@ -261,6 +261,60 @@ __device__ __forceinline__ int merge_xor_seg(const Tile &tile, const int *A, int
     return nA + nP - 2 * __popc(dmask);
 }
 
+// Move A[a..b) to A[a + t..b + t) in place, 0 < t < G: chunks from the top
+// down, each loaded by the whole group before any lane stores.
+template <int G, class Tile>
+__device__ __forceinline__ void shift_up(const Tile &tile, int *A, int a, int b, int t) {
+    const int lane = tile.thread_rank();
+    for (int hi = b; hi > a; hi -= G) {
+        const int q = hi - G + lane;
+        const int v = q >= a ? A[q] : 0;
+        tile.sync();
+        if (q >= a) A[q + t] = v;
+    }
+}
+// The same with -G < t < 0: chunks from the bottom up.
+template <int G, class Tile>
+__device__ __forceinline__ void shift_down(const Tile &tile, int *A, int a, int b, int t) {
+    const int lane = tile.thread_rank();
+    for (int lo = a; lo < b; lo += G) {
+        const int q = lo + lane;
+        const int v = q < b ? A[q] : 0;
+        tile.sync();
+        if (q < b) A[q + t] = v;
+    }
+}
+
+// Add a pivot of three rows {x0, x1, low} (x0 < x1 < low = A[n - 1]) to A in
+// place.  The low cancels; x0 and x1 each insert or cancel, so A splits into
+// a prefix that stays, a middle run that moves by one and a top run that
+// moves by two or stays.  Returns the new length.  A needs room for n + 1.
+template <int G, class Tile>
+__device__ __forceinline__ int merge3_inplace(const Tile &tile, int *A, int n, int x0, int x1) {
+    const int lane = tile.thread_rank();
+    const int m1 = n - 1;
+    int r = 0;
+    if (lane < 2) r = lower_bound(A, m1, lane ? x1 : x0);
+    const int r0 = tile.shfl(r, 0), r1 = tile.shfl(r, 1);
+    const bool d0 = r0 < m1 && A[r0] == x0;
+    const bool d1 = r1 < m1 && A[r1] == x1;
+    tile.sync();
+    if (!d0) {
+        if (!d1) shift_up<G>(tile, A, r1, m1, 2);
+        shift_up<G>(tile, A, r0, r1, 1);
+    } else {
+        shift_down<G>(tile, A, r0 + 1, r1, -1);
+        if (d1) shift_down<G>(tile, A, r1 + 1, m1, -2);
+    }
+    tile.sync();
+    if (lane == 0) {
+        if (!d0) A[r0] = x0;
+        if (!d1) A[r1 + (d0 ? -1 : 1)] = x1;
+    }
+    tile.sync();
+    return n + 1 - 2 * ((int)d0 + (int)d1);
+}
+
 // The same for a pivot of more entries (still at most G, one per lane): the
 // runs are found per element instead of per pivot entry.  With thr_k = the
 // first index of A that lies past P[k] (r_k, plus one when P[k] is in A, as

@@ -427,6 +427,11 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 #ifndef OPH_SEG_MAX
 #define OPH_SEG_MAX 4
 #endif
+// Pivots of three rows read from their record are added in place
+// (merge3_inplace): only the rows above the first insertion point move.
+#ifndef OPH_INPLACE3
+#define OPH_INPLACE3 1
+#endif
 // Which of tiers 0 (bit 0) and 1 (bit 1) reduce lazy columns
 // (reduce_column_lazy); the others merge eagerly on every addition
 // (reduce_column_smem).
@@ -497,7 +502,12 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
         }
         if (n + np > cap || (SMALL_PIVOTS_ONLY && np > G)) { handed = true; break; }
         int nn;
-        if (np <= OPH_SEG_MAX) {
+        bool swap = true;
+        if (OPH_INPLACE3 && np == 3 && !P) {
+            // the common apparent pair: its rows are in the record
+            nn = merge3_inplace<G>(tile, A, n, e.x, e.y);
+            swap = false;
+        } else if (np <= OPH_SEG_MAX) {
             nn = merge_xor_seg<G>(tile, A, n, pv, np, B);
         } else if (np <= G) {
             nn = merge_xor_thr<G>(tile, A, n, pv, np, B);
@@ -510,7 +520,9 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
         slots += n + np + nn;
         adds++;
         n = nn;
-        int *t = A; A = B; B = t;
+        if (swap) {
+            int *t = A; A = B; B = t;
+        }
         lj = n ? A[n - 1] : -1;
         if (lj < 0) break;
         rec_load_p2(&a.rec[lj], h, e);
