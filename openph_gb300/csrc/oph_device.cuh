@@ -394,6 +394,73 @@ __device__ __forceinline__ int merge_xor_block(const int *A, int nA, const int *
     return nA + nP - 2 * common;
 }
 
+// Block-wide symmetric difference by merge path, for long columns.  The
+// union of A and P in sorted order (ties: A's copy first) is cut into
+// blockDim.x equal ranges; each thread finds its range's start by a binary
+// search on the diagonal and merges it sequentially.  A common value is A[i]
+// immediately followed by P[j], so taking A[i] cancels when P[j] == A[i] and
+// taking P[j] cancels when A[i - 1] == P[j]: no thread needs its neighbours.
+// A first pass counts each thread's kept elements, a block scan turns the
+// counts into offsets, a second pass writes.  Per thread: one search and
+// 2 (nA + nP) / blockDim.x merge steps, instead of a search per element.
+// `scratch` holds blockDim.x / 32 ints; B must not alias A or P.
+__device__ __forceinline__ int merge_xor_path(const int *A, int nA, const int *P, int nP, int *B, int *scratch) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    const int L = nA + nP;
+    const int K = (L + nt - 1) / nt;
+    const int d0 = min(tid * K, L), d1 = min(d0 + K, L);
+    int lo = max(0, d0 - nP), hi = min(d0, nA);
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (A[mid] <= P[d0 - mid - 1]) lo = mid + 1;
+        else hi = mid;
+    }
+    const int i0 = lo, j0 = d0 - lo;
+    int cnt = 0;
+    {
+        int i = i0, j = j0;
+        for (int d = d0; d < d1; d++) {
+            const int a = i < nA ? A[i] : 0x7fffffff, p = j < nP ? P[j] : 0x7fffffff;
+            if (i < nA && (j >= nP || a <= p)) {
+                cnt += (j < nP && p == a) ? 0 : 1;
+                i++;
+            } else {
+                cnt += (i > 0 && A[i - 1] == p) ? 0 : 1;
+                j++;
+            }
+        }
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) scratch[wid] = incl;
+    __syncthreads();
+    int off = incl - cnt, total = 0;
+    for (int q = 0; q < nw; q++) {
+        const int c = scratch[q];
+        if (q < wid) off += c;
+        total += c;
+    }
+    {
+        int i = i0, j = j0;
+        for (int d = d0; d < d1; d++) {
+            const int a = i < nA ? A[i] : 0x7fffffff, p = j < nP ? P[j] : 0x7fffffff;
+            if (i < nA && (j >= nP || a <= p)) {
+                if (!(j < nP && p == a)) B[off++] = a;
+                i++;
+            } else {
+                if (!(i > 0 && A[i - 1] == p)) B[off++] = p;
+                j++;
+            }
+        }
+    }
+    __syncthreads();
+    return total;
+}
+
 // Block copy of n ints (all threads of the CTA).
 __device__ __forceinline__ void block_copy(int *dst, const int *src, int n) {
     if ((((uintptr_t)dst | (uintptr_t)src) & 15) == 0) {

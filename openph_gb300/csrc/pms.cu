@@ -427,6 +427,10 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 #ifndef OPH_SEG_MAX
 #define OPH_SEG_MAX 4
 #endif
+// The CTA tiers merge by merge path (1) or by a rank search per element (0).
+#ifndef OPH_BLOCK_PATH
+#define OPH_BLOCK_PATH 1
+#endif
 // Pivots of three rows read from their record are added in place
 // (merge3_inplace): only the rows above the first insertion point move.
 #ifndef OPH_INPLACE3
@@ -874,7 +878,8 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
             block_copy(sC, P, np);
             P = sC;
         }
-        const int nn = merge_xor_block(A, n, P, np, B, scratch);
+        const int nn = OPH_BLOCK_PATH ? merge_xor_path(A, n, P, np, B, scratch)
+                                      : merge_xor_block(A, n, P, np, B, scratch);
         slots += n + np + nn;
         adds++;
         n = nn;
@@ -961,8 +966,12 @@ constexpr int T0_G = OPH_T0_G, T0_CAP = OPH_T0_CAP, T0_BLOCK = 256;
 constexpr int T1_G = OPH_T1_G, T1_CAP = OPH_T1_CAP, T1_BLOCK = 256;
 constexpr bool T1_STAGE = OPH_T1_STAGE != 0;
 constexpr bool T0_LAZY = (OPH_LAZY & 1) != 0, T1_LAZY = (OPH_LAZY & 2) != 0;
-constexpr int T2_CAP = 8192, T2_BLOCK = 256;
-constexpr int T3_BLOCK = 256;
+// Threads per column in the CTA tiers.
+#ifndef OPH_BLOCK_THREADS
+#define OPH_BLOCK_THREADS 256
+#endif
+constexpr int T2_CAP = 8192, T2_BLOCK = OPH_BLOCK_THREADS;
+constexpr int T3_BLOCK = OPH_BLOCK_THREADS;
 
 // Occupancy-filling grid for a kernel with `smem` bytes of dynamic shared
 // memory (attribute set once per device).
