@@ -21,10 +21,11 @@
 // test and, for a pivot of at most four entries (most pivots are apparent
 // pairs of three), the pivot's rows too: one dependent round trip per
 // addition instead of three.  Every field changes at most once per
-// reduction, from a marker (col -1, np 0, e -1) to its final value; the
-// publisher writes col last behind a fence.  A reader that sees col set but
-// any needed field still at its marker falls back to an acquire load of col
-// and re-reads the fields and the segment.
+// reduction, from a marker (col -1, np 0, seg4 SEG4_NONE, e -1) to its final
+// value; the publisher writes col last behind a fence.  A reader that sees
+// col set but needs the segment takes an acquire load of col (ordering its
+// reads of the segment) and re-reads np / seg4 only if its first read still
+// showed a marker (rec_header).
 #pragma once
 #include <cooperative_groups.h>
 #include <cstdint>
@@ -35,7 +36,8 @@ namespace cg = cooperative_groups;
 namespace oph {
 
 constexpr int SEG_HDR = 4;
-constexpr long long MAX_POOL_INTS = 4ll << 32;  // segment / 4 is held in 32 bits
+constexpr long long MAX_POOL_INTS = (4ll << 32) - 64;  // segment / 4 is held in 32 bits,
+constexpr unsigned SEG4_NONE = 0xffffffffu;           //   this value marking "not yet published"
 constexpr int FIRST_NONE = 0x7f7f7f7f;  // byte pattern 0x7f: "no column yet"
 constexpr int MAXC = 8;                 // dimension buckets handled by the Phase I scan (-1 .. 6)
 constexpr int POOL_PAD = 1024;          // ints of readable padding past the pool's end
@@ -106,6 +108,14 @@ __device__ __forceinline__ void st_release_i32(int *p, int v) {
 __device__ __forceinline__ bool rec_complete(const int4 &h, const int4 &e) {
     const int np = h.y;
     return np >= 1 && np <= 4 && e.x >= 0 && (np < 2 || e.y >= 0) && (np < 3 || e.z >= 0) && (np < 4 || e.w >= 0);
+}
+// np and seg4 of a published record after the acquire of its col: the
+// relaxed read's values when neither is a marker (each changes once), else
+// a fresh read.
+__device__ __forceinline__ int4 rec_header(const PivRec *r, const int4 &h) {
+    ld_acquire_i32(&r->col);
+    if (h.y > 0 && (unsigned)h.w != SEG4_NONE) return h;
+    return __ldcg(reinterpret_cast<const int4 *>(r));
 }
 __device__ __forceinline__ int rec_entry(const int4 &e, int k) {
     return k == 0 ? e.x : k == 1 ? e.y : k == 2 ? e.z : e.w;

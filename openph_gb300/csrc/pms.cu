@@ -498,8 +498,7 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
             np = h.y;
             pv = rec_entry(e, lane & 3);
         } else {
-            ld_acquire_i32(&a.rec[lj].col);
-            const int4 h2 = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+            const int4 h2 = rec_header(&a.rec[lj], h);
             np = h2.y;
             P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
             pv = P[lane];
@@ -615,8 +614,7 @@ __device__ void reduce_column_lazy(const Tile &tile, const PmsArgs &a, int j, in
             np = h.y;
             pv = rec_entry(e, lane & 3);
         } else {
-            ld_acquire_i32(&a.rec[lj].col);
-            const int4 h2 = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+            const int4 h2 = rec_header(&a.rec[lj], h);
             np = h2.y;
             P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
             pv = P[lane];
@@ -859,8 +857,7 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
             __syncthreads();
             P = s_small;
         } else {
-            ld_acquire_i32(&a.rec[lj].col);
-            const int4 h2 = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+            const int4 h2 = rec_header(&a.rec[lj], h);
             np = h2.y;
             P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
         }

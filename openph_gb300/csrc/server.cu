@@ -119,7 +119,7 @@ __global__ void k_srv_init(const int64_t *__restrict__ colptr, const int32_t *__
         a.first[j] = FIRST_NONE;
         const_cast<int32_t *>(a.beta)[j] = -1;
         int4 *r = reinterpret_cast<int4 *>(a.rec + j);
-        r[0] = make_int4(-1, 0, FIRST_NONE, 0);
+        r[0] = make_int4(-1, 0, FIRST_NONE, (int)SEG4_NONE);
         r[1] = make_int4(-1, -1, -1, -1);
     }
 }
@@ -163,7 +163,7 @@ __global__ void k_srv_inert(int64_t m, int64_t c0, PmsArgs a) {
         a.inst[j] = -1;
         a.first[j] = FIRST_NONE;
         int4 *r = reinterpret_cast<int4 *>(a.rec + j);
-        r[0] = make_int4(-1, 0, -1, 0);
+        r[0] = make_int4(-1, 0, -1, (int)SEG4_NONE);
         r[1] = make_int4(-1, -1, -1, -1);
     }
 }

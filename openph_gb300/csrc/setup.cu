@@ -81,7 +81,7 @@ __global__ void k_beta(PivRec *__restrict__ rec, int64_t m, int32_t *__restrict_
         if (l == FIRST_NONE) l = -1;
         else atomicMax(&beta[l], (int)i);
         int4 *r = reinterpret_cast<int4 *>(rec + i);
-        r[0] = make_int4(-1, 0, l, 0);
+        r[0] = make_int4(-1, 0, l, (int)SEG4_NONE);
         r[1] = make_int4(-1, -1, -1, -1);
     }
 }
