@@ -398,6 +398,59 @@ def run_ours(args, ws, rank, local):
 BATCH = {"count": 4096, "seed": 4, "lo": 20, "hi": 120}
 
 
+def _batch_cpu_instance(job):
+    """One batch instance through the reference-layout twist port (runs in a
+    spawned worker; raises col_width until the instance fits, as the
+    reference's users do)."""
+    colptr, rows = job
+    import oracle
+    from openph_gb300.complexes import BoundaryMatrix
+    bm = BoundaryMatrix(colptr, rows)
+    width = COL_WIDTH
+    while True:
+        rc, _, _, st = oracle.twist_fixed_p(bm, width)
+        if rc == 0:
+            return st["seconds"]
+        width *= 2
+
+
+def cpu_batch_sample(col_off, colptr, rows, seconds: float) -> dict:
+    """Complexes/s of the CPU twist port with one instance per process on
+    every host core (spawned workers, the instances in order), over about
+    `seconds` of wall time."""
+    def jobs():
+        for b in range(len(col_off) - 1):
+            c0, c1 = int(col_off[b]), int(col_off[b + 1])
+            yield colptr[c0:c1 + 1] - colptr[c0], rows[int(colptr[c0]):int(colptr[c1])]
+
+    return cpu_pool_sample(jobs(), seconds, "instances of the batch")
+
+
+def _pool_warm(_):
+    import oracle  # noqa: F401  (loads the port's library once per worker)
+    from openph_gb300 import complexes  # noqa: F401
+    return os.getpid()
+
+
+def cpu_pool_sample(jobs, seconds: float, what: str) -> dict:
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    done = 0
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(_pool_warm, range(4 * cores))  # workers started and imported before the clock
+        it = pool.imap(_batch_cpu_instance, jobs, chunksize=1)
+        t0 = time.perf_counter()
+        for _ in it:
+            done += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
+        wall = time.perf_counter() - t0
+        pool.terminate()
+    return {"value": done / wall, "unit": "complexes/s", "cores": cores, "kind": "port",
+            "sample": f"the first {done} {what}, one per process on {cores} host cores, "
+                      f"reference-layout twist port ({wall:.1f} s wall)"}
+
+
 def run_batch(args, ws, rank, local):
     """The batched workload: 4096 Rips complexes (n ~ U[20,120], half cube,
     half noisy circle) reduced in one segmented pass, against plain pms one
@@ -474,6 +527,29 @@ def run_batch(args, ws, rank, local):
             mismatches += 1
     seq_s = max_over_ranks(seq_ms / 1e3, dist, device)
 
+    # end to end through the C ABI: pinned host CSC in, host lows out
+    h_off = torch.from_numpy(col_off).pin_memory()
+    h_colptr = torch.from_numpy(colptr).pin_memory()
+    h_rows = torch.from_numpy(rows).pin_memory()
+    h_low = torch.empty(total_m, dtype=torch.int32).pin_memory()
+    L = api.lib()
+    info = api.Info()
+
+    def e2e_step():
+        rc = L.oph_reduce_batch(ctx._h, api.algo_id("pms"), count, h_off.numpy(), h_colptr.numpy(),
+                                C.c_void_p(h_rows.data_ptr()), h_low.numpy(), None, C.byref(info))
+        if rc != 0:
+            raise api.OphError(rc, "oph_reduce_batch")
+
+    e2e_step()
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_s += time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, dist, device)
+    e2e_equal = bool(np.array_equal(h_low.numpy(), low_batch))
+
     # oracle on a seeded sample of instances
     rng = np.random.default_rng(7)
     sample = sorted(rng.choice(count, size=min(count, 24), replace=False).tolist())
@@ -493,6 +569,11 @@ def run_batch(args, ws, rank, local):
                        "l2": "inputs (%.1f GB) larger than L2" % ((total_nnz * 4 + total_m * 8) / 1e9)},
             "plain_sequential": {"complexes_per_s": count / seq_s, "s_total": seq_s},
             "batched_over_plain": (count * args.steps / batch_s) / (count / seq_s),
+            "e2e": {"value": ws * count * args.steps / e2e_s, "unit": "complexes/s",
+                    "h2d_bytes_per_step": 8 * (count + 1) + 8 * (total_m + 1) + 4 * total_nnz,
+                    "d2h_bytes_per_step": 4 * total_m, "ms_per_step": 1e3 * e2e_s / args.steps,
+                    "api": "oph_reduce_batch C ABI", "equal_to_device_run": e2e_equal},
+            "cpu_baseline": cpu_batch_sample(col_off, colptr, rows, CPU_SAMPLE_SECONDS),
             "cols_per_s": ws * total_m * args.steps / batch_s,
             "sweeps": info["sweeps"], "device_additions": info["additions"], "regrows": info["regrows"],
             "pool_bytes": info["pool_bytes"],
@@ -627,6 +708,12 @@ def run_serve(args, ws, rank, local):
         "served_over_plain_at_saturation": best["served_per_s"] / plain_rate,
         "p50_ms_at_saturation": best["p50_ms"], "p99_ms_at_saturation": best["p99_ms"],
         "rate_sweep": results, "server": counters,
+        "e2e": {"value": best["served_per_s"], "unit": "complexes/s",
+                "h2d_bytes_per_step": int(np.mean([8 * (bm.m + 1) + 4 * bm.nnz for _, bm in reqs])),
+                "d2h_bytes_per_step": int(np.mean([8 * bm.m for _, bm in reqs])),
+                "api": "oph_server_submit / oph_server_wait (host CSC in, host lows and ess out; a step = one request)"},
+        "cpu_baseline": cpu_pool_sample(((bm.colptr, bm.rows) for _, bm in reqs), CPU_SAMPLE_SECONDS,
+                                        "requests of the stream"),
         "parity": {"served_equals_plain": mism == 0, "mismatches": mism, "oracle_checked_smallest": len(order),
                    "oracle_equal": bool(oracle_ok)},
     }
