@@ -31,6 +31,12 @@
 
 namespace oph {
 
+// OPH_COUNTS=1: diagnostic counters of the Phase II tiers (DevStatus::diag,
+// printed with OPH_TRACE=2).
+#ifndef OPH_COUNTS
+#define OPH_COUNTS 0
+#endif
+
 constexpr int P1_THREADS = 256;
 constexpr int P1_ITEMS = 8;
 constexpr int P1_TILE = P1_THREADS * P1_ITEMS;
@@ -80,6 +86,7 @@ __global__ void k_p1_first(PmsArgs a) {
         a.st->reps = 0;
         a.st->wl_count = 0;
         for (int t = 0; t < 4; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
+        if (OPH_COUNTS) a.st->diag[5] = 0;  // the eager tier's longest chain, per sweep
     }
     const int64_t n = p1_count(a);
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
@@ -321,6 +328,26 @@ __global__ void k_p1_kscan(PmsArgs a) {
 //     next list, and into the Phase II queue; first[] reset (once per row, by
 //     its winner).  Clears marked in (d) are applied by the next Phase I
 //     (Phase II skips such columns).
+// Whether unresolved column j can add anything in this sweep's Phase II: its
+// low lj has a pivot to its left now (published by Phase 0 / I), or one can
+// be published during Phase II.  The latter happens only through the beta
+// check, by the first column holding row lj (left[lj]), when that column is
+// left of j, unresolved and its chain still above lj.  Other columns would
+// find no pivot on their visit; leaving them out of the queue changes no
+// addition.
+#ifndef OPH_P2_FILTER
+#define OPH_P2_FILTER 1
+#endif
+__device__ __forceinline__ bool p2_ready(const PmsArgs &a, int j) {
+    if (a.clear[j]) return false;  // positive: cleared by the next Phase I
+    const int lj = a.low[j];
+    const int4 h = __ldcg(reinterpret_cast<const int4 *>(&a.rec[lj]));
+    if (h.x >= 0 && h.x < j) return true;
+    const int p = h.z;
+    if (p < 0 || p >= j) return false;
+    return a.classes[p] == 0 && a.low[p] > lj;
+}
+
 __global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
     if (a.st->converged) return;
     const int64_t n = p1_count(a);
@@ -359,11 +386,15 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++)
         if (keepmask & (1u << t)) a.ulist_next[off++] = cols[t];
-    // Phase II takes the same columns from a queue filled by warp-aggregated
+    // Phase II takes these columns from a queue filled by warp-aggregated
     // appends: concurrently reduced columns then come from all over the
-    // matrix instead of one neighbourhood (which contends on shared pivots)
+    // matrix instead of one neighbourhood (which contends on shared pivots).
+    // Only columns that can add this sweep are queued (p2_ready).
 #pragma unroll
-    for (int t = 0; t < P1_ITEMS; t++) warp_append((keepmask >> t) & 1u, cols[t], a.worklist, &a.st->t_count[0]);
+    for (int t = 0; t < P1_ITEMS; t++) {
+        const bool want = ((keepmask >> t) & 1u) && (!OPH_P2_FILTER || p2_ready(a, cols[t]));
+        warp_append(want, cols[t], a.worklist, &a.st->t_count[0]);
+    }
 }
 
 // (e') without a compacted list: reset first[], apply the clears of this
@@ -578,9 +609,6 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
 // With STATS the exact |T| is carried through every addition (membership of
 // each toggled row in A by binary search) for the |P| + |T| + |T xor P|
 // counters; without it only additions are counted.
-#ifndef OPH_COUNTS
-#define OPH_COUNTS 0
-#endif
 struct LazyDiag {
     unsigned long long c[8];
 };
@@ -768,8 +796,16 @@ __device__ __forceinline__ void p2_tier_body(const PmsArgs &a, int tier) {
         {
             int *C = STAGE ? buf + 2 * CAP : nullptr;
             int *qn = &a.st->t_count[tier + 1];
-            if (!LAZY)
+            if (!LAZY) {
+                const long long before = adds;
                 reduce_column_smem<G, false>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots);
+                if (OPH_COUNTS) {  // eager tier: visits, longest chain, columns that added
+                    const unsigned long long c = (unsigned long long)(adds - before);
+                    dg.c[4]++;
+                    dg.c[5] = c > dg.c[5] ? c : dg.c[5];
+                    dg.c[6] += c > 0;
+                }
+            }
             else if (a.stats)
                 reduce_column_lazy<G, true>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots,
                                             dg);
@@ -781,8 +817,11 @@ __device__ __forceinline__ void p2_tier_body(const PmsArgs &a, int tier) {
     if (tile.thread_rank() == 0) {
         tier_stats(a, tier, adds, slots);
         if (OPH_COUNTS) {
-            for (int q = 0; q < 8; q++)
-                if (dg.c[q]) atomicAdd(&a.st->diag[8 * (tier & 1) + q], dg.c[q]);
+            for (int q = 0; q < 8; q++) {
+                if (!dg.c[q]) continue;
+                if (!LAZY && q == 5) atomicMax(&a.st->diag[8 * (tier & 1) + q], dg.c[q]);
+                else atomicAdd(&a.st->diag[8 * (tier & 1) + q], dg.c[q]);
+            }
 #if OPH_COUNTS
             unsigned smid;
             asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
@@ -1261,8 +1300,13 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
                 fprintf(stderr, "\n");
             }
 #endif
+            if (trace > 1 && worked && !T0_LAZY) {
+                const unsigned long long *d = hs.diag, *e = before.diag;
+                fprintf(stderr, "  tier 0 (eager): visits %llu, columns that added %llu, longest chain %llu\n",
+                        d[4] - e[4], d[6] - e[6], d[5]);
+            }
             if (trace > 1 && worked) {
-                for (int t = 0; t < 2; t++) {
+                for (int t = T0_LAZY ? 0 : 1; t < 2; t++) {
                     const unsigned long long *d = hs.diag + 8 * t, *e = before.diag + 8 * t;
                     fprintf(stderr, "  tier %d: adds rec %llu seg<=4 %llu mid %llu wide %llu | flushes %llu cancels %llu | "
                                     "columns %llu rows in %llu\n", t, d[0] - e[0], d[1] - e[1], d[2] - e[2],
