@@ -200,42 +200,6 @@ __device__ __forceinline__ int merge_xor(const Tile &tile, const int *A, int nA,
     return nA + nP - 2 * common;
 }
 
-// The same symmetric difference when the pivot P has at most G entries and is
-// held one element per lane (lane k < nP holds P[k] in `pv`).  Lane k ranks
-// P[k] in A by binary search; every element x of A is then shifted by
-//   sum over k of [P[k] < x] * (P[k] common ? -1 : +1)
-// (the pivot broadcast by shuffles), and dropped if it equals some P[k].
-// No staging of P and no second pass over it.  Returns |A xor P|.
-template <int G, class Tile>
-__device__ __forceinline__ int merge_xor_small(const Tile &tile, const int *A, int nA, int pv, int nP, int *B) {
-    const int lane = tile.thread_rank();
-    const unsigned lt = (1u << lane) - 1u;
-    int r = 0;
-    bool pdup = false;
-    if (lane < nP) {
-        r = lower_bound(A, nA, pv);
-        pdup = r < nA && A[r] == pv;
-    }
-    const unsigned dmask = tile.ballot(pdup);
-    if (lane < nP && !pdup) B[lane + r - 2 * __popc(dmask & lt)] = pv;
-    for (int base = 0; base < nA; base += G) {
-        const int i = base + lane;
-        const bool v = i < nA;
-        const int x = v ? A[i] : 0;
-        int shift = 0;
-        bool drop = false;
-        for (int k = 0; k < nP; k++) {
-            const int pk = tile.shfl(pv, k);
-            const int s = ((dmask >> k) & 1u) ? -1 : 1;
-            shift += pk < x ? s : 0;
-            drop |= pk == x;
-        }
-        if (v && !drop) B[i + shift] = x;
-    }
-    tile.sync();
-    return nA + nP - 2 * __popc(dmask);
-}
-
 // Symmetric difference for a pivot of at most G entries held one per lane,
 // by segments: the pivot's entries, ranked in A (lanes k < nP, binary
 // search), cut A into nP + 1 runs that are copied with a constant shift each;
@@ -363,45 +327,6 @@ __device__ __forceinline__ int merge_xor_thr(const Tile &tile, const int *A, int
     }
     tile.sync();
     return nA + nP - 2 * __popc(dmask);
-}
-
-// Block-wide symmetric difference (every thread of the CTA), for wide
-// columns: the rank placement of merge_xor with the common-value counts
-// carried across the CTA by per-warp ballots and a shared-memory prefix.
-// `scratch` is 2 * (blockDim.x / 32) ints of shared memory.  A, P, B may be
-// in shared or global memory; B must not alias A or P.
-__device__ __forceinline__ int merge_xor_block(const int *A, int nA, const int *P, int nP, int *B, int *scratch) {
-    const int tid = threadIdx.x, nt = blockDim.x, wid = tid >> 5, lane = tid & 31, nw = nt >> 5;
-    const unsigned lt = (1u << lane) - 1u;
-    int *wtot = scratch;  // per-warp counts of the current chunk
-    int carry = 0, common = 0;
-    for (int pass = 0; pass < 2; pass++) {
-        const int *X = pass ? P : A, *Y = pass ? A : P;
-        const int nX = pass ? nP : nA, nY = pass ? nA : nP;
-        carry = 0;
-        for (int base = 0; base < nX; base += nt) {
-            const int i = base + tid;
-            const bool v = i < nX;
-            const int x = v ? X[i] : 0;
-            const int r = v ? lower_bound(Y, nY, x) : 0;
-            const bool dup = v && r < nY && Y[r] == x;
-            const unsigned b = __ballot_sync(0xffffffffu, dup);
-            if (lane == 0) wtot[wid] = __popc(b);
-            __syncthreads();
-            int before = carry + __popc(b & lt), total = 0;
-            for (int q = 0; q < nw; q++) {
-                const int c = wtot[q];
-                if (q < wid) before += c;
-                total += c;
-            }
-            if (v && !dup) B[i + r - 2 * before] = x;
-            carry += total;
-            __syncthreads();
-        }
-        if (pass == 0) common = carry;
-    }
-    __syncthreads();
-    return nA + nP - 2 * common;
 }
 
 // Block-wide symmetric difference by merge path, for long columns.  The

@@ -75,9 +75,6 @@ __device__ __forceinline__ bool is_repeat(const PmsArgs &a, int64_t j, int lj) {
     return (pc >= 0 && pc < (int)j) || a.first[lj] != (int)j;
 }
 
-#ifndef OPH_FIRST_CHECK
-#define OPH_FIRST_CHECK 1
-#endif
 // (a) apply pending clears (clear_positives, pms_functions.cu:131-140) and
 //     record the first column of every low.
 __global__ void k_p1_first(PmsArgs a) {
@@ -106,7 +103,7 @@ __global__ void k_p1_first(PmsArgs a) {
             // many columns can share a low: skip the atomic when first[]
             // already holds a smaller column (a stale read only costs the
             // atomic that would have been issued anyway)
-            if ((pc < 0 || pc >= (int)j) && (!OPH_FIRST_CHECK || a.first[lj] > (int)j))
+            if ((pc < 0 || pc >= (int)j) && a.first[lj] > (int)j)
                 atomicMin(&a.first[lj], (int)j);
         }
     }
@@ -452,16 +449,9 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 // record carries them, with left[] for the beta check) and two otherwise;
 // reading G ints past a segment start stays in bounds through the pool's
 // tail padding.
-// Pivots of at most OPH_SEG_MAX entries are merged by runs (merge_xor_seg,
-// a loop over the pivot's entries), wider ones up to G by per-element
-// threshold search (merge_xor_thr, a loop over A's chunks).
-#ifndef OPH_SEG_MAX
-#define OPH_SEG_MAX 4
-#endif
-// The CTA tiers merge by merge path (1) or by a rank search per element (0).
-#ifndef OPH_BLOCK_PATH
-#define OPH_BLOCK_PATH 1
-#endif
+// Pivots of at most four entries are merged by runs (merge_xor_seg, a loop
+// over the pivot's entries), wider ones up to G by per-element threshold
+// search (merge_xor_thr, a loop over A's chunks).
 // Pivots of three rows read from their record are added in place
 // (merge3_inplace): only the rows above the first insertion point move.
 #ifndef OPH_INPLACE3
@@ -473,35 +463,17 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 #ifndef OPH_LAZY
 #define OPH_LAZY 2
 #endif
-// Phase II reads pivot records through L1 (1) or L2 only (0).  A record seen
-// through L1 may be stale, i.e. still unpublished (col -1) or partly
-// published; the first makes the column stop its chain for this sweep, the
-// second takes the acquire path, so a stale line costs time, not results.
-#ifndef OPH_REC_L1
-#define OPH_REC_L1 0
-#endif
 // Mark column lj positive (cleared by the next Phase I).  Every chain through
-// row lj marks it again; with OPH_CLEAR_CHECK the flag is read (alongside the
-// record) and written only while still 0, so the hot flags are not rewritten
-// by thousands of warps.
-#ifndef OPH_CLEAR_CHECK
-#define OPH_CLEAR_CHECK 1
-#endif
-template <bool CHECK = OPH_CLEAR_CHECK != 0>
+// row lj marks it again; with CHECK the flag is read (alongside the record)
+// and written only while still 0, so the hot flags are not rewritten by
+// thousands of warps (unconditional stores to a few hot L2 sectors left half
+// of the SMs at a fifth of the others' rate).
+template <bool CHECK = true>
 __device__ __forceinline__ void mark_clear(const PmsArgs &a, int lj, bool leader) {
     if (!leader) return;
     if (!CHECK || !a.clear[lj]) a.clear[lj] = 1;
 }
-__device__ __forceinline__ void rec_load_p2(const PivRec *r, int4 &h, int4 &e) {
-    if (OPH_REC_L1) {
-        const int4 *p = reinterpret_cast<const int4 *>(r);
-        h = __ldca(p);
-        e = __ldca(p + 1);
-    } else {
-        rec_load(r, h, e);
-    }
-}
-template <int G, bool SMALL_PIVOTS_ONLY, class Tile>
+template <int G, class Tile>
 __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, int *A, int *B, int *C, int cap,
                                    int32_t *out_list, int *out_cnt, long long &adds, long long &slots) {
     const int lane = tile.thread_rank();
@@ -509,7 +481,7 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
     int lj = a.low[j];
     if (lj < 0) return;
     int4 h, e;
-    rec_load_p2(&a.rec[lj], h, e);
+    rec_load(&a.rec[lj], h, e);
     if (h.x < 0 || h.x >= j) return;  // no pivot to the left of j yet
     const long long sj = a.seg[j];
     int n = a.pool[sj];
@@ -534,14 +506,14 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
             P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
             pv = P[lane];
         }
-        if (n + np > cap || (SMALL_PIVOTS_ONLY && np > G)) { handed = true; break; }
+        if (n + np > cap) { handed = true; break; }
         int nn;
         bool swap = true;
         if (OPH_INPLACE3 && np == 3 && !P) {
             // the common apparent pair: its rows are in the record
             nn = merge3_inplace<G>(tile, A, n, e.x, e.y);
             swap = false;
-        } else if (np <= OPH_SEG_MAX) {
+        } else if (np <= 4) {
             nn = merge_xor_seg<G>(tile, A, n, pv, np, B);
         } else if (np <= G) {
             nn = merge_xor_thr<G>(tile, A, n, pv, np, B);
@@ -559,7 +531,7 @@ __device__ void reduce_column_smem(const Tile &tile, const PmsArgs &a, int j, in
         }
         lj = n ? A[n - 1] : -1;
         if (lj < 0) break;
-        rec_load_p2(&a.rec[lj], h, e);
+        rec_load(&a.rec[lj], h, e);
         mark_clear(a, lj, lane == 0);
         if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
         if (h.x < 0 || h.x >= j) break;
@@ -621,7 +593,7 @@ __device__ void reduce_column_lazy(const Tile &tile, const PmsArgs &a, int j, in
     int lj = a.low[j];
     if (lj < 0) return;
     int4 h, e;
-    rec_load_p2(&a.rec[lj], h, e);
+    rec_load(&a.rec[lj], h, e);
     if (h.x < 0 || h.x >= j) return;  // no pivot to the left of j yet
     const long long sj = a.seg[j];
     int n = a.pool[sj];
@@ -725,7 +697,7 @@ __device__ void reduce_column_lazy(const Tile &tile, const PmsArgs &a, int j, in
             break;
         }
         if (lj < 0) break;
-        rec_load_p2(&a.rec[lj], h, e);
+        rec_load(&a.rec[lj], h, e);
         mark_clear(a, lj, lane == 0);
         if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
         if (h.x < 0 || h.x >= j) break;
@@ -798,7 +770,7 @@ __device__ __forceinline__ void p2_tier_body(const PmsArgs &a, int tier) {
             int *qn = &a.st->t_count[tier + 1];
             if (!LAZY) {
                 const long long before = adds;
-                reduce_column_smem<G, false>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots);
+                reduce_column_smem<G>(tile, a, in_list[idx], buf, buf + CAP, C, CAP, out_list, qn, adds, slots);
                 if (OPH_COUNTS) {  // eager tier: visits, longest chain, columns that added
                     const unsigned long long c = (unsigned long long)(adds - before);
                     dg.c[4]++;
@@ -914,8 +886,7 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
             block_copy(sC, P, np);
             P = sC;
         }
-        const int nn = OPH_BLOCK_PATH ? merge_xor_path(A, n, P, np, B, scratch)
-                                      : merge_xor_block(A, n, P, np, B, scratch);
+        const int nn = merge_xor_path(A, n, P, np, B, scratch);
         slots += n + np + nn;
         adds++;
         n = nn;
@@ -996,11 +967,8 @@ __global__ void k_count_sweep(DevStatus *st) {
 #define OPH_T1_G 32
 #endif
 constexpr int T0_G = OPH_T0_G, T0_CAP = OPH_T0_CAP, T0_BLOCK = 256;
-#ifndef OPH_T1_STAGE
-#define OPH_T1_STAGE 1
-#endif
 constexpr int T1_G = OPH_T1_G, T1_CAP = OPH_T1_CAP, T1_BLOCK = 256;
-constexpr bool T1_STAGE = OPH_T1_STAGE != 0;
+constexpr bool T1_STAGE = true;
 constexpr bool T0_LAZY = (OPH_LAZY & 1) != 0, T1_LAZY = (OPH_LAZY & 2) != 0;
 // Threads per column in the CTA tiers.
 #ifndef OPH_BLOCK_THREADS
