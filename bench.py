@@ -533,11 +533,11 @@ def run_batch(args, ws, rank, local):
     h_rows = torch.from_numpy(rows).pin_memory()
     h_low = torch.empty(total_m, dtype=torch.int32).pin_memory()
     L = api.lib()
-    info = api.Info()
+    e2e_info = api.Info()
 
     def e2e_step():
         rc = L.oph_reduce_batch(ctx._h, api.algo_id("pms"), count, h_off.numpy(), h_colptr.numpy(),
-                                C.c_void_p(h_rows.data_ptr()), h_low.numpy(), None, C.byref(info))
+                                C.c_void_p(h_rows.data_ptr()), h_low.numpy(), None, C.byref(e2e_info))
         if rc != 0:
             raise api.OphError(rc, "oph_reduce_batch")
 
