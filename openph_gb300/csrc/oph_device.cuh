@@ -53,8 +53,8 @@ struct DevStatus {
     int converged;                 // pms: no repeated low left
     int sweeps;                    // pms sweeps run
     int wl_count;                  // Phase II worklist size (tier 0 input)
-    int wl_cursor;                 // unused (tier cursors below)
-    int wide_count;                // unused
+    int s_cursor;                  // scalar tier: work-queue cursor
+    int s_out;                     //   and the columns it hands to tier 0
     int wide_cursor;               // unused
     int t_count[4];                // Phase II tier queues: columns queued per tier
     int t_cursor[4];               //   and the work-queue cursor of each tier
@@ -72,6 +72,7 @@ struct DevStatus {
     // a wider one; flushes of pending toggles before the chain's end; top
     // cancellations; columns entered; their rows on entry
     unsigned long long diag[16];
+    unsigned long long sdiag[8];   // the scalar tier's (OPH_COUNTS builds)
 #if defined(OPH_COUNTS) && OPH_COUNTS
     unsigned long long diag_sm[256];  // Phase II additions per SM
 #endif

@@ -107,7 +107,7 @@ struct Context {
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_ESSHAT, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_NSLOTS
 };
 
 }  // namespace oph

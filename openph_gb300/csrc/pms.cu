@@ -83,6 +83,8 @@ __global__ void k_p1_first(PmsArgs a) {
         a.st->reps = 0;
         a.st->wl_count = 0;
         for (int t = 0; t < 4; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
+        a.st->s_cursor = 0;
+        a.st->s_out = 0;
         if (OPH_COUNTS) a.st->diag[5] = 0;  // the eager tier's longest chain, per sweep
     }
     const int64_t n = p1_count(a);
@@ -745,6 +747,173 @@ __device__ __forceinline__ void tier_stats(const PmsArgs &a, int tier, long long
     }
 }
 
+// ------------------------------------------------------------ scalar tier
+// Short columns, one per lane: the first Phase II pass over the queue.  A
+// lane holds its column in shared memory interleaved with the other lanes'
+// (row k of the lane's column at col[32 k]; whatever rows the lanes touch,
+// their accesses fall in distinct banks) and adds pivots of at most four
+// rows, read from their records, by scalar toggles: rank the row, then
+// shift the rows above it by one.  32 columns per warp, no lane idle on
+// another's work.  A column that would outgrow TS_CAP rows, or meets a pivot
+// not held whole in its record, is written back and handed to tier 0.
+constexpr int TS_CAP = 32;
+constexpr int TS_BLOCK = 256;
+#ifndef OPH_SCALAR
+#define OPH_SCALAR 1
+#endif
+
+// Toggle row x in the lane's column of m1 rows; returns the new length.
+__device__ __forceinline__ int ts_toggle(int *col, int m1, int x) {
+    int lo = 0, len = m1;
+    while (len > 0) {
+        const int h = len >> 1;
+        if (col[(lo + h) * 32] < x) { lo += h + 1; len -= h + 1; }
+        else len = h;
+    }
+    if (lo < m1 && col[lo * 32] == x) {
+        for (int k = lo; k < m1 - 1; k++) col[k * 32] = col[(k + 1) * 32];
+        return m1 - 1;
+    }
+    for (int k = m1; k > lo; k--) col[k * 32] = col[(k - 1) * 32];
+    col[lo * 32] = x;
+    return m1 + 1;
+}
+
+#ifndef OPH_TS_MINB
+#define OPH_TS_MINB 0
+#endif
+#if OPH_TS_MINB > 0
+__global__ void __launch_bounds__(TS_BLOCK, OPH_TS_MINB) k_p2_scalar(PmsArgs a) {
+#else
+__global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
+#endif
+    if (a.st->converged) return;
+    __shared__ int sm[(TS_BLOCK / 32) * TS_CAP * 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int *col = sm + wid * TS_CAP * 32 + lane;
+    const int count = a.st->t_count[0];
+    long long adds = 0, slots = 0;
+    bool active = false, exhausted = false;
+    int j = -1, n = 0, lj = -1, capj = 0;
+    long long sj = 0;
+    int4 h = make_int4(0, 0, 0, 0), e = h;
+    LazyDiag dg{};  // OPH_COUNTS: [0] additions, [1] handed over at load, [2] mid-chain, [3] steps, [4] loads, [5] rows
+    for (;;) {
+        bool handoff = false;
+        if (OPH_COUNTS) dg.c[3]++;
+        // lanes without a column take the next ones from the queue
+        const bool need = !active && !exhausted;
+        const unsigned nm = __ballot_sync(0xffffffffu, need);
+        if (nm) {
+            const int leader = __ffs(nm) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&a.st->s_cursor, __popc(nm));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const int idx = base + __popc(nm & ((1u << lane) - 1u));
+                if (idx >= count) {
+                    exhausted = true;
+                } else {
+                    j = a.worklist[idx];
+                    lj = a.low[j];
+                    bool ok = lj >= 0 && !a.clear[j];
+                    if (ok) {
+                        rec_load(&a.rec[lj], h, e);
+                        ok = h.x >= 0 && h.x < j;  // a pivot to the left of j
+                    }
+                    if (ok) {
+                        sj = a.seg[j];
+                        n = a.pool[sj];
+                        capj = a.pool[sj + 1];
+                        // a column this tier cannot add its first pivot to goes
+                        // to tier 0 untouched
+                        if (n > TS_CAP || !rec_complete(h, e) || n + h.y - 2 > TS_CAP) {
+                            handoff = true;
+                            if (OPH_COUNTS) dg.c[1]++;
+                        } else {
+                            // 16-byte loads issued together (a segment starts on
+                            // 16 bytes and its capacity is a multiple of four)
+                            const int4 *src = reinterpret_cast<const int4 *>(a.pool + sj + SEG_HDR);
+#pragma unroll
+                            for (int q = 0; q < TS_CAP / 4; q++)
+                                if (4 * q < n) {
+                                    const int4 v = __ldcg(src + q);
+                                    col[(4 * q) * 32] = v.x;
+                                    col[(4 * q + 1) * 32] = v.y;
+                                    col[(4 * q + 2) * 32] = v.z;
+                                    col[(4 * q + 3) * 32] = v.w;
+                                }
+                            active = true;
+                            if (OPH_COUNTS) { dg.c[4]++; dg.c[5] += n; }
+                        }
+                    }
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, !active && exhausted)) break;
+        // one addition on every column that has a pivot to add
+        int fin = 0;  // 1 hand off, 2 stop (blocked or zero), 3 became a pivot
+        if (active) {
+            const int np = h.y;
+            if (!rec_complete(h, e) || n + np - 2 > TS_CAP) {
+                fin = 1;
+                if (OPH_COUNTS) dg.c[2]++;
+            } else {
+                int m1 = n - 1;  // the low cancels
+                for (int t = np - 2; t >= 0; t--) m1 = ts_toggle(col, m1, rec_entry(e, t));
+                slots += n + np + m1;
+                adds++;
+                if (OPH_COUNTS) dg.c[0]++;
+                n = m1;
+                lj = n > 0 ? col[(n - 1) * 32] : -1;
+                if (lj < 0) {
+                    fin = 2;
+                } else {
+                    rec_load(&a.rec[lj], h, e);
+                    mark_clear(a, lj, true);
+                    if (h.z == j) fin = 3;  // the beta check: row lj first appears in j
+                    else if (h.x < 0 || h.x >= j) fin = 2;
+                }
+            }
+        }
+        if (fin) {
+            active = false;
+            long long dst = sj;
+            int dcap = capj;
+            bool stored = true;
+            if (n > capj) {
+                dcap = round4(max(n + (n >> 1), 16));
+                dst = col_alloc(a, j, SEG_HDR + dcap);
+                stored = dst >= 0;  // pool exhausted: j keeps its pre-sweep state
+            }
+            if (stored) {
+                int *d = a.pool + dst + SEG_HDR;
+                for (int k = 0; k < n; k++) d[k] = col[k * 32];
+                a.pool[dst] = n;
+                a.pool[dst + 1] = dcap;
+                a.seg[j] = dst;
+                a.low[j] = lj;
+                if (fin == 3) {
+                    int first[4];
+                    for (int k = 0; k < 4; k++) first[k] = k < n ? col[k * 32] : -1;
+                    a.classes[j] = -1;
+                    rec_publish(a.rec, lj, j, n, dst, first);
+                }
+                handoff = fin == 1;
+            }
+        }
+        warp_append(handoff, j, a.slist, &a.st->s_out);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        adds += __shfl_xor_sync(0xffffffffu, adds, o);
+        slots += __shfl_xor_sync(0xffffffffu, slots, o);
+    }
+    if (lane == 0) tier_stats(a, 0, adds, slots);
+    if (OPH_COUNTS)
+        for (int q = 0; q < 6; q++)
+            if (dg.c[q]) atomicAdd(&a.st->sdiag[q], dg.c[q]);
+}
+
 // Tiers 0 and 1: groups of G lanes, each group with A/B buffers of CAP ints
 // and, with STAGE, a C buffer into which a pivot wider than the group is
 // staged; without it (tier 0) such a pivot is searched in the store.
@@ -1039,7 +1208,8 @@ int t0_candidate(int v, int *lanes, int *cap) {
 }
 
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
-    static int done1[64], done2[64];
+    static int done1[64], done2[64], dones[64];
+    g->gs = fill_grid(ctx, k_p2_scalar, TS_BLOCK, 0, dones);
     g->v0 = (ctx->tier0 >= 0 && ctx->tier0 < T0_CANDIDATES) ? ctx->tier0 : 0;
     g->s1 = (size_t)(T1_BLOCK / T1_G) * (T1_STAGE ? 3 : 2) * T1_CAP * sizeof(int);
     g->s2 = (size_t)3 * T2_CAP * sizeof(int);
@@ -1049,7 +1219,7 @@ int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     g->g3 = ctx->sm_count * 2;
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
     g->t = (int)std::max<int64_t>(1, ntiles);
-    if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0) {
+    if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0 || g->gs < 0) {
         fprintf(stderr, "openph_gb300: Phase II kernel set-up failed: %s\n", cudaGetErrorString(cudaGetLastError()));
         return OPH_ERR_CUDA;
     }
@@ -1124,7 +1294,11 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
         a.ucur = C[parity & 1];
         a.unext = C[(parity + 1) & 1];
     }
-    {
+    if (a.slist) {
+        // the scalar tier takes the queue first and hands tier 0 the rest
+        a.t0_list = a.slist;
+        a.t0_count = &a0.st->s_out;
+    } else {
         a.t0_list = a.worklist;
         a.t0_count = &a0.st->t_count[0];
     }
@@ -1140,6 +1314,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
         k_p1_worklist<<<g.m, 256, 0, s>>>(a);
     }
     if (ev) cudaEventRecord(ev[1], s);
+    if (a.slist) k_p2_scalar<<<g.gs, TS_BLOCK, 0, s>>>(a);
     launch_t0(a, g, s);
     if (ev) cudaEventRecord(ev[2], s);
     k_p2_tier1<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
@@ -1176,6 +1351,10 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
 #ifndef OPH_PHASE1_LIST
 #define OPH_PHASE1_LIST 1
 #endif
+    if (OPH_SCALAR) {
+        a.slist = (int32_t *)ctx_alloc(ctx, S_SLIST, sizeof(int32_t) * (m > 0 ? m : 1));
+        if (!a.slist) return OPH_ERR_OOM;
+    }
     if (OPH_PHASE1_LIST) {
         a.ulist = (int32_t *)ctx_alloc(ctx, S_ULIST, sizeof(int32_t) * 2 * (m > 0 ? m : 1));
         a.kagg = (int32_t *)ctx_alloc(ctx, S_KAGG, sizeof(int32_t) * (w.ntiles + 1));
@@ -1268,6 +1447,12 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
                 fprintf(stderr, "\n");
             }
 #endif
+            if (trace > 1 && worked && a.slist) {
+                const unsigned long long *d = hs.sdiag, *e = before.sdiag;
+                fprintf(stderr, "  scalar tier: additions %llu, handed at load %llu / mid-chain %llu, lane-steps %llu, "
+                                "columns loaded %llu (rows %llu)\n", d[0] - e[0], d[1] - e[1], d[2] - e[2],
+                        d[3] - e[3], d[4] - e[4], d[5] - e[5]);
+            }
             if (trace > 1 && worked && !T0_LAZY) {
                 const unsigned long long *d = hs.diag, *e = before.diag;
                 fprintf(stderr, "  tier 0 (eager): visits %llu, columns that added %llu, longest chain %llu\n",

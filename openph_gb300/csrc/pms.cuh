@@ -37,6 +37,8 @@ struct PmsArgs {
     // Phase II tier-0 queue (the compacted list, or the worklist)
     int32_t *t0_list;
     int *t0_count;
+    // the scalar tier's hand-off list to tier 0 (nullptr: no scalar tier)
+    int32_t *slist;
     // exact |P| + |T| + |T xor P| counters in the lazy tiers (profiling)
     int stats;
 };
@@ -50,6 +52,7 @@ struct SweepGrids {
     int v0;                 // tier-0 candidate in use
     int m, t;               // grid of the per-column passes, Phase I tiles
     int g0, g1, g2, g3;     // Phase II tier grids
+    int gs;                 //   and the scalar tier's
     size_t s0, s1, s2;      // their dynamic shared memory
 };
 
