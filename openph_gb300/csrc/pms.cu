@@ -779,6 +779,10 @@ __device__ __forceinline__ int ts_toggle(int *col, int m1, int x) {
     return m1 + 1;
 }
 
+#ifndef OPH_TS_REFILL
+#define OPH_TS_REFILL 24
+#endif
+constexpr int TS_REFILL = OPH_TS_REFILL;
 #ifndef OPH_TS_MINB
 #define OPH_TS_MINB 0
 #endif
@@ -798,61 +802,97 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
     long long sj = 0;
     int4 h = make_int4(0, 0, 0, 0), e = h;
     LazyDiag dg{};  // OPH_COUNTS: [0] additions, [1] handed over at load, [2] mid-chain, [3] steps, [4] loads, [5] rows
+    int fin = 0;  // a finished column awaiting write-back: 1 hand off, 2 stop, 3 became a pivot
     for (;;) {
-        bool handoff = false;
         if (OPH_COUNTS) dg.c[3]++;
-        // lanes without a column take the next ones from the queue
-        const bool need = !active && !exhausted;
-        const unsigned nm = __ballot_sync(0xffffffffu, need);
-        if (nm) {
-            const int leader = __ffs(nm) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(&a.st->s_cursor, __popc(nm));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (need) {
-                const int idx = base + __popc(nm & ((1u << lane) - 1u));
-                if (idx >= count) {
-                    exhausted = true;
-                } else {
-                    j = a.worklist[idx];
-                    lj = a.low[j];
-                    bool ok = lj >= 0 && !a.clear[j];
-                    if (ok) {
-                        rec_load(&a.rec[lj], h, e);
-                        ok = h.x >= 0 && h.x < j;  // a pivot to the left of j
+        // Book-keeping (write-backs and refills) diverges from the additions,
+        // so it waits until at least TS_REFILL lanes have no column to add to
+        // (or none has): finished lanes keep their column in shared memory
+        // until then, and the long paths run with many lanes at once.
+        const unsigned waiting = __ballot_sync(0xffffffffu, !active);
+        if (__popc(waiting) >= TS_REFILL || waiting == 0xffffffffu) {
+            bool handoff = false;
+            if (fin) {
+                long long dst = sj;
+                int dcap = capj;
+                bool stored = true;
+                if (n > capj) {
+                    dcap = round4(max(n + (n >> 1), 16));
+                    dst = col_alloc(a, j, SEG_HDR + dcap);
+                    stored = dst >= 0;  // pool exhausted: j keeps its pre-sweep state
+                }
+                if (stored) {
+                    int *d = a.pool + dst + SEG_HDR;
+                    for (int k = 0; k < n; k++) d[k] = col[k * 32];
+                    a.pool[dst] = n;
+                    a.pool[dst + 1] = dcap;
+                    a.seg[j] = dst;
+                    a.low[j] = lj;
+                    if (fin == 3) {
+                        int first[4];
+                        for (int k = 0; k < 4; k++) first[k] = k < n ? col[k * 32] : -1;
+                        a.classes[j] = -1;
+                        rec_publish(a.rec, lj, j, n, dst, first);
                     }
-                    if (ok) {
-                        sj = a.seg[j];
-                        n = a.pool[sj];
-                        capj = a.pool[sj + 1];
-                        // a column this tier cannot add its first pivot to goes
-                        // to tier 0 untouched
-                        if (n > TS_CAP || !rec_complete(h, e) || n + h.y - 2 > TS_CAP) {
-                            handoff = true;
-                            if (OPH_COUNTS) dg.c[1]++;
-                        } else {
-                            // 16-byte loads issued together (a segment starts on
-                            // 16 bytes and its capacity is a multiple of four)
-                            const int4 *src = reinterpret_cast<const int4 *>(a.pool + sj + SEG_HDR);
+                    handoff = fin == 1;
+                }
+                fin = 0;
+            }
+            warp_append(handoff, j, a.slist, &a.st->s_out);
+            handoff = false;
+            // lanes without a column take the next ones from the queue
+            const bool need = !active && !exhausted;
+            const unsigned nm = __ballot_sync(0xffffffffu, need);
+            if (nm) {
+                const int leader = __ffs(nm) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(&a.st->s_cursor, __popc(nm));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (need) {
+                    const int idx = base + __popc(nm & ((1u << lane) - 1u));
+                    if (idx >= count) {
+                        exhausted = true;
+                    } else {
+                        j = a.worklist[idx];
+                        lj = a.low[j];
+                        bool ok = lj >= 0 && !a.clear[j];
+                        if (ok) {
+                            rec_load(&a.rec[lj], h, e);
+                            ok = h.x >= 0 && h.x < j;  // a pivot to the left of j
+                        }
+                        if (ok) {
+                            sj = a.seg[j];
+                            n = a.pool[sj];
+                            capj = a.pool[sj + 1];
+                            // a column this tier cannot add its first pivot to
+                            // goes to tier 0 untouched
+                            if (n > TS_CAP || !rec_complete(h, e) || n + h.y - 2 > TS_CAP) {
+                                handoff = true;
+                                if (OPH_COUNTS) dg.c[1]++;
+                            } else {
+                                // 16-byte loads issued together (a segment starts
+                                // on 16 bytes, its capacity a multiple of four)
+                                const int4 *src = reinterpret_cast<const int4 *>(a.pool + sj + SEG_HDR);
 #pragma unroll
-                            for (int q = 0; q < TS_CAP / 4; q++)
-                                if (4 * q < n) {
-                                    const int4 v = __ldcg(src + q);
-                                    col[(4 * q) * 32] = v.x;
-                                    col[(4 * q + 1) * 32] = v.y;
-                                    col[(4 * q + 2) * 32] = v.z;
-                                    col[(4 * q + 3) * 32] = v.w;
-                                }
-                            active = true;
-                            if (OPH_COUNTS) { dg.c[4]++; dg.c[5] += n; }
+                                for (int q = 0; q < TS_CAP / 4; q++)
+                                    if (4 * q < n) {
+                                        const int4 v = __ldcg(src + q);
+                                        col[(4 * q) * 32] = v.x;
+                                        col[(4 * q + 1) * 32] = v.y;
+                                        col[(4 * q + 2) * 32] = v.z;
+                                        col[(4 * q + 3) * 32] = v.w;
+                                    }
+                                active = true;
+                                if (OPH_COUNTS) { dg.c[4]++; dg.c[5] += n; }
+                            }
                         }
                     }
                 }
             }
+            warp_append(handoff, j, a.slist, &a.st->s_out);
+            if (__all_sync(0xffffffffu, !active && exhausted)) break;
         }
-        if (__all_sync(0xffffffffu, !active && exhausted)) break;
         // one addition on every column that has a pivot to add
-        int fin = 0;  // 1 hand off, 2 stop (blocked or zero), 3 became a pivot
         if (active) {
             const int np = h.y;
             if (!rec_complete(h, e) || n + np - 2 > TS_CAP) {
@@ -875,34 +915,8 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
                     else if (h.x < 0 || h.x >= j) fin = 2;
                 }
             }
+            if (fin) active = false;
         }
-        if (fin) {
-            active = false;
-            long long dst = sj;
-            int dcap = capj;
-            bool stored = true;
-            if (n > capj) {
-                dcap = round4(max(n + (n >> 1), 16));
-                dst = col_alloc(a, j, SEG_HDR + dcap);
-                stored = dst >= 0;  // pool exhausted: j keeps its pre-sweep state
-            }
-            if (stored) {
-                int *d = a.pool + dst + SEG_HDR;
-                for (int k = 0; k < n; k++) d[k] = col[k * 32];
-                a.pool[dst] = n;
-                a.pool[dst + 1] = dcap;
-                a.seg[j] = dst;
-                a.low[j] = lj;
-                if (fin == 3) {
-                    int first[4];
-                    for (int k = 0; k < 4; k++) first[k] = k < n ? col[k * 32] : -1;
-                    a.classes[j] = -1;
-                    rec_publish(a.rec, lj, j, n, dst, first);
-                }
-                handoff = fin == 1;
-            }
-        }
-        warp_append(handoff, j, a.slist, &a.st->s_out);
     }
     for (int o = 16; o > 0; o >>= 1) {
         adds += __shfl_xor_sync(0xffffffffu, adds, o);
