@@ -756,7 +756,10 @@ __device__ __forceinline__ void tier_stats(const PmsArgs &a, int tier, long long
 // shift the rows above it by one.  32 columns per warp, no lane idle on
 // another's work.  A column that would outgrow TS_CAP rows, or meets a pivot
 // not held whole in its record, is written back and handed to tier 0.
-constexpr int TS_CAP = 32;
+#ifndef OPH_TS_CAP
+#define OPH_TS_CAP 48
+#endif
+constexpr int TS_CAP = OPH_TS_CAP;
 constexpr int TS_BLOCK = 256;
 #ifndef OPH_SCALAR
 #define OPH_SCALAR 1
