@@ -124,6 +124,7 @@ extern "C" __attribute__((visibility("default"))) int oph_reduce_pms_noalloc(int
     a.beta = beta;
     a.worklist = c.take<int32_t>(m);
     a.widelist = c.take<int32_t>(m);
+    a.slist = c.take<int32_t>(m);
     a.seg = c.take<int64_t>(m);
     a.rec = c.take<PivRec>(m);
     a.ntiles = (m + 2047) / 2048;

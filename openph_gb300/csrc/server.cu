@@ -453,7 +453,7 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     // the arena: per-column arrays for mcap columns (a tenth of the budget)
     // and a segment pool for the rest (at most what 32-bit segment fields
     // address)
-    const int64_t per_col = 4 + 1 + 1 + 1 + 4 + 4 + 4 + 4 + 8 + (int64_t)sizeof(PivRec) + 4;
+    const int64_t per_col = 4 + 1 + 1 + 1 + 4 + 4 + 4 + 4 + 4 + 8 + (int64_t)sizeof(PivRec) + 4;
     sv->mcap = std::min<int64_t>(budget_bytes / 10 / per_col, (1ll << 29) - 1);
     int64_t pool_bytes = budget_bytes - sv->mcap * per_col - budget_bytes / 16;
     sv->pool_ints = std::min<int64_t>(pool_bytes / 4 - POOL_PAD, MAX_POOL_INTS - 1);
@@ -467,6 +467,7 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     a.beta = (int32_t *)ctx_alloc(ctx, S_BETA, 4 * mc);
     a.worklist = (int32_t *)ctx_alloc(ctx, S_WORK, 4 * mc);
     a.widelist = (int32_t *)ctx_alloc(ctx, S_WIDE, 4 * mc);
+    a.slist = (int32_t *)ctx_alloc(ctx, S_SLIST, 4 * mc);
     a.seg = (int64_t *)ctx_alloc(ctx, S_SEG, 8 * mc);
     a.rec = (PivRec *)ctx_alloc(ctx, S_ROWPIV, sizeof(PivRec) * mc);
     a.inst = (int *)ctx_alloc(ctx, S_LOWTRUE, 4 * mc);
@@ -476,8 +477,8 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     a.iover = (int *)ctx_alloc(ctx, S_TMP, 4 * (size_t)max_active);
     a.st = (DevStatus *)ctx_alloc(ctx, S_STATUS, sizeof(DevStatus));
     a.pool = (int *)ctx_alloc(ctx, S_POOL, sizeof(int) * (sv->pool_ints + POOL_PAD));
-    bool ok = a.low && a.classes && a.clear && a.dim && a.first && a.beta && a.worklist && a.widelist && a.seg &&
-              a.rec && a.inst && a.agg && a.ipool && a.ireps && a.iover && a.st && a.pool;
+    bool ok = a.low && a.classes && a.clear && a.dim && a.first && a.beta && a.worklist && a.widelist &&
+              a.slist && a.seg && a.rec && a.inst && a.agg && a.ipool && a.ireps && a.iover && a.st && a.pool;
     if (ok) ok = cudaMallocHost((void **)&sv->h_ireps, 4 * (size_t)max_active) == cudaSuccess &&
                  cudaMallocHost((void **)&sv->h_iover, 4 * (size_t)max_active) == cudaSuccess;
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
