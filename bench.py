@@ -347,10 +347,12 @@ def run_ours(args, ws, rank, local):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     ab = algorithmic_bytes(bm, st)
-    # dominant kernel: Phase II tier 0.  Its algorithmic bytes are the
-    # per-addition figure 4 (|P| + |T| + |T xor P|) summed over the additions
-    # it performed (counted on the device), per launch; divided by its mean
-    # launch time (CUDA events around each launch on the library's stream)
+    # dominant kernels: the Phase II narrow tiers (the scalar tier and tier 0,
+    # launched back to back and timed together each sweep).  Their
+    # algorithmic bytes are the per-addition figure 4 (|P| + |T| + |T xor P|)
+    # summed over the additions they performed (counted on the device), per
+    # sweep; divided by their mean time per sweep (CUDA events around the
+    # pair on the library's stream)
     per_red_narrow_s = narrow_ms / 1e3 / args.steps
     t0_bytes = 4 * tier0_slots
     achieved = t0_bytes / per_red_narrow_s / 1e9 if per_red_narrow_s > 0 else None
@@ -367,7 +369,9 @@ def run_ours(args, ws, rank, local):
         "complexes_per_s": ws * args.steps / total_s,
         "e2e": {"value": ws * m * args.steps / e2e_s, "unit": "cols/s", "h2d_bytes_per_step": 8 * nnz,
                 "d2h_bytes_per_step": 8 * m, "ms_per_step": 1e3 * e2e_s / args.steps, "api": "openph() C ABI"},
-        "roofline": {"bound": "hbm", "kernel": "k_p2_tier<8,128,256> (Phase II tier 0: column additions)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "Phase II narrow tiers, one launch each per sweep: k_p2_scalar (a column per lane) "
+                               "then k_p2_tier<8,128,256> (8 lanes per column)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback",
