@@ -44,6 +44,24 @@ def random_complex(n_vertices, p_edge, p_tri, seed):
     return BoundaryMatrix.from_columns(cols)
 
 
+def simplex_skeleton(n_vertices, seed, max_dim=None):
+    """Every face of the (n_vertices - 1)-simplex up to max_dim (all of them by
+    default), in a lower-star order: a random value per vertex, a simplex
+    valued by its largest vertex, ties by dimension then vertex tuple.
+    Columns have up to max_dim + 1 rows."""
+    from itertools import combinations
+    rng = np.random.default_rng(seed)
+    vv = rng.random(n_vertices)
+    top = n_vertices if max_dim is None else max_dim + 1
+    simplices = [c for k in range(1, top + 1) for c in combinations(range(n_vertices), k)]
+    simplices.sort(key=lambda s: (max(vv[list(s)]), len(s), s))
+    pos = {s: i for i, s in enumerate(simplices)}
+    cols = []
+    for s in simplices:
+        cols.append([] if len(s) == 1 else sorted(pos[s[:y] + s[y + 1:]] for y in range(len(s))))
+    return BoundaryMatrix.from_columns(cols)
+
+
 def small_cases():
     out = {
         "triangle": triangle(),
@@ -54,4 +72,6 @@ def small_cases():
     }
     for s in range(3):
         out[f"random_{s}"] = random_complex(14, 0.5, 0.6, seed=100 + s)
+    out["simplex_6d"] = simplex_skeleton(7, seed=11)          # columns of up to 7 rows
+    out["skeleton_4d_of_9"] = simplex_skeleton(9, seed=12, max_dim=4)
     return out

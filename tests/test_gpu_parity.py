@@ -273,3 +273,19 @@ def test_pms_trackers_per_sweep(cuda_lib):
     assert np.all(redu[:n] <= 1.0) and np.all((eerr[:n] > 0) & (eerr[:n] <= 1.0))
     assert np.all(tt[1:n] > 0) and tt[0] == 0
     assert np.all(lone[n:] == -1)
+
+
+def test_columns_wider_than_pms_handles(cuda_lib):
+    """The 7-simplex has a column of 8 rows: pms (whose Phase I keeps one
+    running maximum per dimension -1..6) refuses it with an error; the other
+    algorithms reduce it exactly."""
+    from cases import simplex_skeleton
+    bm = simplex_skeleton(8, seed=13)
+    assert np.diff(bm.colptr).max() == 8
+    r, c = bm.to_coo1()
+    with pytest.raises(OphError):
+        ph("pms", r, c, bm.m, 3, np.zeros(bm.m, np.int32))
+    want, _, _ = oracle.twist(bm)
+    for algo in ("standard", "twist", "standard_parallel", "twist_parallel", "ph_row", "ph_row_parallel"):
+        low, *_ = ph(algo, r, c, bm.m, 3, np.zeros(bm.m, np.int32))
+        np.testing.assert_array_equal(low, want + 1, err_msg=algo)
