@@ -289,3 +289,20 @@ def test_columns_wider_than_pms_handles(cuda_lib):
     for algo in ("standard", "twist", "standard_parallel", "twist_parallel", "ph_row", "ph_row_parallel"):
         low, *_ = ph(algo, r, c, bm.m, 3, np.zeros(bm.m, np.int32))
         np.testing.assert_array_equal(low, want + 1, err_msg=algo)
+
+
+def test_batch_ragged_with_empty_instances(ctx):
+    """Instances of 0, 1 and 5 columns, a triangle, a 6-simplex and a small
+    Rips complex in one batch: each equals the oracle."""
+    from cases import empty_columns, simplex_skeleton, triangle
+    from openph_gb300.complexes import BoundaryMatrix
+    mats = [BoundaryMatrix.from_columns([]), triangle(), BoundaryMatrix.from_columns([[]]), empty_columns(5),
+            simplex_skeleton(7, seed=21), cx.rips_mixed(10, seed=3), BoundaryMatrix.from_columns([])]
+    lows, esss, _ = ctx.reduce_batch(mats, "pms")
+    for bm, low, ess in zip(mats, lows, esss):
+        assert len(low) == bm.m
+        if bm.m == 0:
+            continue
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
