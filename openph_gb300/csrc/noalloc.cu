@@ -169,7 +169,7 @@ extern "C" __attribute__((visibility("default"))) int oph_reduce_pms_noalloc(int
     ctx.device = dev;
     ctx.sm_count = sm;
     ctx.stream = s;
-    SweepGrids g;
+    SweepGrids g{};
     if ((rc = sweep_grids(&ctx, m, a.ntiles, &g))) return rc;
     launch_phase0(a, 0, m, g.m, s);
     for (int sweeps = 0;;) {

@@ -101,6 +101,11 @@ struct Context {
     int launches = 0;               // kernels launched by the current reduction
     int tier0 = 0;                  // Phase II tier-0 candidate (autotuned)
     Tracking *track = nullptr;      // per-sweep trackers for the current reduction
+    // two pms sweeps (the list ping-pong's two parities) captured as one CUDA
+    // graph and replayed instead of 2 x 11 launches; sweep_key holds the
+    // launch arguments it was captured with
+    cudaGraphExec_t sweep_graph = nullptr;
+    std::vector<unsigned char> sweep_key;
 };
 
 // buffer slots of Context::bufs

@@ -25,6 +25,7 @@
 //     Phase I); kernels of a converged sweep return at once, so the host reads
 //     one status word per batch of sweeps instead of one per sweep.
 #include <algorithm>
+#include <cstring>
 
 #include "oph_host.h"
 #include "pms.cuh"
@@ -1356,6 +1357,44 @@ void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int par
 
 constexpr int KERNELS_PER_SWEEP = 11;
 
+// Sweeps replayed from a captured CUDA graph (0: launched one by one).
+#ifndef OPH_GRAPHS
+#define OPH_GRAPHS 1
+#endif
+
+// The graph of two sweeps (parities 0 and 1) for these arguments, captured on
+// first use and again whenever an argument changes (a regrown store moves the
+// pool).  Returns false, with nothing left captured, when capture fails; the
+// caller then launches the sweeps directly.
+static bool sweep_pair_graph(Context *ctx, const PmsArgs &a, const SweepGrids &g) {
+    std::vector<unsigned char> key(sizeof(PmsArgs) + sizeof(SweepGrids));
+    memcpy(key.data(), &a, sizeof(PmsArgs));
+    memcpy(key.data() + sizeof(PmsArgs), &g, sizeof(SweepGrids));
+    if (ctx->sweep_graph && key == ctx->sweep_key) return true;
+    if (ctx->sweep_graph) {
+        cudaGraphExecDestroy(ctx->sweep_graph);
+        ctx->sweep_graph = nullptr;
+    }
+    cudaStream_t s = ctx->stream;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    launch_sweep_ev(a, g, s, nullptr, 0);
+    launch_sweep_ev(a, g, s, nullptr, 1);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&ctx->sweep_graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ctx->sweep_graph = nullptr;
+        return false;
+    }
+    ctx->sweep_key = std::move(key);
+    return true;
+}
+
 int run_pms(Context *ctx, Work &w, oph_info *info) {
     const int64_t m = w.m;
     PmsArgs a{};
@@ -1379,7 +1418,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         a.ulist_next = a.ulist + m;
     }
     cudaStream_t s = ctx->stream;
-    SweepGrids g;
+    SweepGrids g{};
     int rc = sweep_grids(ctx, m, w.ntiles, &g);
     if (rc) return rc;
     if (a.ulist) {
@@ -1428,7 +1467,14 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     for (;;) {
         const int nb = std::min(batch, max_sweeps - sweeps_launched);
         DevStatus before = hs;
-        for (int b = 0; b < nb; b++) {
+        int b = 0;
+        if (OPH_GRAPHS && !timed && (sweeps_launched & 1) == 0 && nb >= 2 && sweep_pair_graph(ctx, a, g)) {
+            for (; b + 2 <= nb; b += 2) {
+                OPH_CUDA_TRY(cudaGraphLaunch(ctx->sweep_graph, s));
+                ctx->launches += 2 * KERNELS_PER_SWEEP;
+            }
+        }
+        for (; b < nb; b++) {
             launch_sweep_ev(a, g, s, timed ? ctx->pev + 6 * b : nullptr, sweeps_launched + b);
             launch_track(a, g, s, tr, sweeps_launched + b + 1);
             ctx->launches += KERNELS_PER_SWEEP;
