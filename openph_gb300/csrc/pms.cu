@@ -15,15 +15,19 @@
 //     dimension bucket (a tiled scan); j is a pivot iff it is first for its
 //     low, unclassified, and low > ceil(j).  Identical marks to the serial walk
 //     on graded matrices (rows of distinct buckets are disjoint).
-//   * Phase II runs a compacted worklist of unresolved columns through a
-//     persistent work queue; the column being reduced stays in shared memory
-//     across its whole chain of additions and is written back once; pivots are
-//     staged into shared memory; columns wider than the narrow tier go to a
-//     wide tier (one warp per column, larger shared buffers), and beyond that
-//     to a global-memory tier.
+//   * Phase II takes the unresolved columns that can add this sweep from a
+//     work queue, each column on chip for its whole chain of additions and
+//     written back once, through tiers by column length: a column per lane
+//     (the scalar tier, <= 48 rows), 8 lanes per column (tier 0, <= 128 rows,
+//     three-row pivots added in place), a warp per column (tier 1, <= 512
+//     rows, pending toggles in registers), a CTA per column (tiers 2 and 3,
+//     merge path, shared memory or pool buffers).  A pivot of at most four
+//     rows comes with the one 32-byte record read that also gives the beta
+//     check; the flags every chain would rewrite are written only on change.
 //   * Convergence is tested on the device (the count of repeated lows from
 //     Phase I); kernels of a converged sweep return at once, so the host reads
-//     one status word per batch of sweeps instead of one per sweep.
+//     one status word per batch of sweeps, and the sweeps of a batch are
+//     replayed from a captured CUDA graph.
 #include <algorithm>
 #include <cstring>
 
