@@ -440,27 +440,26 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
     return (long long)off;
 }
 
-// Phase II tiers.  A column is reduced with its rows in shared memory across
-// its whole chain of additions; a column that would outgrow its tier is
-// written back and queued for the next tier:
+// Phase II tiers.  A column is reduced with its rows on chip across its whole
+// chain of additions; a column that would outgrow its tier is written back
+// and queued for the next tier:
+//   scalar  a lane per column,  48 rows      (32 columns per warp; k_p2_scalar)
 //   tier 0  8 lanes per column, CAP 128      (4 columns per warp)
 //   tier 1  a warp per column,  CAP 512      (pivot staged in shared memory
 //                                             when wider than the warp)
-//   tier 2  a CTA per column,   CAP 8192     (block-wide merge)
+//   tier 2  a CTA per column,   CAP 8192     (block-wide merge path)
 //   tier 3  a CTA per column,   buffers in the pool (no limit)
-// Pivots of at most G entries (most are apparent pairs of 3 entries) are held
-// one per lane and merged without staging, by runs or thresholds
-// (merge_xor_seg / merge_xor_thr).  The queues ping-pong between the worklist
-// and widelist arrays.  Each addition costs
-// one dependent round trip when the pivot has at most four entries (its
-// record carries them, with left[] for the beta check) and two otherwise;
-// reading G ints past a segment start stays in bounds through the pool's
-// tail padding.
-// Pivots of at most four entries are merged by runs (merge_xor_seg, a loop
-// over the pivot's entries), wider ones up to G by per-element threshold
-// search (merge_xor_thr, a loop over A's chunks).
-// Pivots of three rows read from their record are added in place
-// (merge3_inplace): only the rows above the first insertion point move.
+// The queues ping-pong between the worklist and widelist arrays (the scalar
+// tier hands on through slist).  Each addition costs one dependent round trip
+// when the pivot has at most four entries (its record carries them, with
+// left[] for the beta check) and two otherwise; reading G ints past a segment
+// start stays in bounds through the pool's tail padding.
+// In the lane groups, pivots of at most G entries are held one per lane and
+// merged without staging: three rows read from their record in place
+// (merge3_inplace: only the rows above the first insertion point move), other
+// pivots of at most four entries by runs (merge_xor_seg, a loop over the
+// pivot's entries), wider ones up to G by per-element threshold search
+// (merge_xor_thr, a loop over A's chunks).
 #ifndef OPH_INPLACE3
 #define OPH_INPLACE3 1
 #endif
