@@ -172,6 +172,14 @@ int oph_server_create(int device, int64_t budget_bytes, int32_t max_active, oph_
 /* Queue a 0-based CSC matrix (copied); returns a ticket.  OPH_ERR_OOM if it
  * can never fit the arena, OPH_ERR_BAD_INPUT if malformed. */
 int oph_server_submit(oph_server *srv, int64_t m, const int64_t *colptr, const int32_t *rows, int64_t *ticket);
+/* The same for a 0-based CSC already in device memory on the server's device
+ * (d_colptr[m + 1] with d_colptr[0] == 0, d_rows[nnz]): the server copies it
+ * device to device and checks it there before returning (the caller's
+ * buffers may be freed then), and its admission reads that copy in place —
+ * no host copy and no host-to-device transfer of the input.  Pairs with
+ * oph_rips_device / oph_lower_star_device.  No counterpart in the reference. */
+int oph_server_submit_device(oph_server *srv, int64_t m, const int64_t *d_colptr, const int32_t *d_rows,
+                             int64_t *ticket);
 /* Wait for a ticket (timeout_ms < 0: forever); copies low/ess (0-based,
  * -1 = none; either may be NULL) and frees the ticket. */
 int oph_server_wait(oph_server *srv, int64_t ticket, int32_t *low, int32_t *ess, oph_request_info *info,

@@ -113,6 +113,7 @@ def lib():
                                               C.POINTER(Info)]
         L.oph_server_create.argtypes = [C.c_int, C.c_int64, C.c_int32, C.POINTER(vp)]
         L.oph_server_submit.argtypes = [vp, C.c_int64, i64, vp, C.POINTER(C.c_int64)]
+        L.oph_server_submit_device.argtypes = [vp, C.c_int64, vp, vp, C.POINTER(C.c_int64)]
         L.oph_server_wait.argtypes = [vp, C.c_int64, vp, vp, C.POINTER(RequestInfo), C.c_int64]
         L.oph_server_stats.argtypes = [vp, C.POINTER(ServerCounters)]
         L.oph_server_destroy.argtypes = [vp]
@@ -388,6 +389,21 @@ class Server:
         if rc != OPH_OK:
             raise OphError(rc, "oph_server_submit")
         self._m[t.value] = bm.m
+        return t.value
+
+    def submit_device(self, dm) -> int:
+        """Queue a matrix already in device memory (a complexes.DeviceMatrix,
+        or anything with torch ``colptr``/``rows`` on this server's device);
+        the server copies it on the device before returning."""
+        import torch
+        torch.cuda.current_stream(dm.colptr.device).synchronize()
+        t = C.c_int64()
+        m = int(dm.colptr.shape[0]) - 1
+        rc = lib().oph_server_submit_device(self._h, m, C.c_void_p(dm.colptr.data_ptr()),
+                                            C.c_void_p(dm.rows.data_ptr()), C.byref(t))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_server_submit_device")
+        self._m[t.value] = m
         return t.value
 
     def wait(self, ticket: int, timeout_ms: int = -1):

@@ -89,6 +89,9 @@ struct Request {
     int64_t ticket = 0, m = 0, nnz = 0;
     std::vector<int64_t> colptr;
     std::vector<int32_t> rows;
+    // a request submitted from device memory: its own copy of the CSC
+    // (colptr then rows, server-owned), read in place at admission
+    void *d_buf = nullptr;
     std::vector<int32_t> low, ess;
     double t_submit = 0, t_admit = 0, t_done = 0;
     int sweeps = 0, status = OPH_OK, slot = -1;
@@ -97,6 +100,19 @@ struct Request {
 };
 
 // ------------------------------------------------------------------ kernels
+// The structural checks of oph_server_submit on a CSC in device memory:
+// columns of at most MAXC - 1 rows, rows strictly ascending and < m.
+__global__ void k_srv_check(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                            int64_t nnz, int *bad) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t lo = colptr[j], hi = colptr[j + 1];
+        // the bounds first: no row is read outside [0, nnz)
+        bool ok = lo >= 0 && hi >= lo && hi <= nnz && hi - lo <= MAXC - 1;
+        for (int64_t k = lo; ok && k < hi; k++) ok = rows[k] >= 0 && rows[k] < m && (k == lo || rows[k] > rows[k - 1]);
+        if (!ok) atomicExch(bad, 1);
+    }
+}
+
 // Admission: columns [c0, c0+m) of request slot `b`, input staged at
 // colptr/rows (local), segments packed from pool offset `base`.
 __global__ void k_srv_init(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
@@ -194,6 +210,7 @@ __global__ void k_srv_sweep_reset(DevStatus *st) {
 // ------------------------------------------------------------------ server
 struct Server {
     Context *ctx = nullptr;  // owns the stream and the device buffers
+    cudaStream_t sub_stream = nullptr;  // device submissions: copy and check
     int64_t budget = 0, mcap = 0, pool_ints = 0;
     int max_slots = 0;
     PmsArgs a{};
@@ -240,8 +257,15 @@ struct Server {
         r->c0 = c0; r->reg = reg; r->reg_ints = reg_ints; r->slot = b;
         int64_t *d_colptr = reinterpret_cast<int64_t *>(a.pool + stg);
         int32_t *d_rows = a.pool + stg + 2 * (r->m + 1);
-        cudaMemcpyAsync(d_colptr, r->colptr.data(), sizeof(int64_t) * (r->m + 1), cudaMemcpyHostToDevice, s);
-        if (r->nnz) cudaMemcpyAsync(d_rows, r->rows.data(), sizeof(int32_t) * r->nnz, cudaMemcpyHostToDevice, s);
+        if (r->d_buf) {
+            // submitted from device memory: read in place, freed after the
+            // kernels below (in stream order)
+            d_colptr = static_cast<int64_t *>(r->d_buf);
+            d_rows = reinterpret_cast<int32_t *>(d_colptr + r->m + 1);
+        } else {
+            cudaMemcpyAsync(d_colptr, r->colptr.data(), sizeof(int64_t) * (r->m + 1), cudaMemcpyHostToDevice, s);
+            if (r->nnz) cudaMemcpyAsync(d_rows, r->rows.data(), sizeof(int32_t) * r->nnz, cudaMemcpyHostToDevice, s);
+        }
         if (r->m > 0) {
             k_srv_init<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, b, reg, a);
             k_srv_left<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, a);
@@ -251,6 +275,10 @@ struct Server {
                                          (unsigned long long)(reg + packed_ints(r->m, r->nnz)),
                                          (unsigned long long)(reg + reg_ints));
         if (r->m > 0) launch_phase0(a, c0, c0 + r->m, grid(r->m), s);
+        if (r->d_buf) {
+            cudaFreeAsync(r->d_buf, s);
+            r->d_buf = nullptr;
+        }
         // the staged input is read by the kernels above: its region is
         // released after the sweep's synchronisation
         staged.emplace_back(stg, stage_ints);
@@ -482,9 +510,11 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     if (ok) ok = cudaMallocHost((void **)&sv->h_ireps, 4 * (size_t)max_active) == cudaSuccess &&
                  cudaMallocHost((void **)&sv->h_iover, 4 * (size_t)max_active) == cudaSuccess;
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
+    if (ok) ok = cudaStreamCreateWithFlags(&sv->sub_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
         if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
         if (sv->h_iover) cudaFreeHost(sv->h_iover);
+        if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
         oph_context_destroy(raw);
         delete sv;
         return OPH_ERR_OOM;
@@ -552,6 +582,63 @@ __attribute__((visibility("default"))) int oph_server_submit(oph_server *sv, int
     return OPH_OK;
 }
 
+__attribute__((visibility("default"))) int oph_server_submit_device(oph_server *sv, int64_t m,
+                                                                    const int64_t *d_colptr, const int32_t *d_rows,
+                                                                    int64_t *ticket) {
+    if (!sv || m < 0 || !d_colptr || !ticket) return OPH_ERR_BAD_INPUT;
+    OPH_CUDA_TRY(cudaSetDevice(sv->ctx->device));
+    cudaStream_t s = sv->sub_stream;
+    int64_t ends[2] = {0, 0};
+    OPH_CUDA_TRY(cudaMemcpyAsync(&ends[0], d_colptr, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaMemcpyAsync(&ends[1], d_colptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    const int64_t nnz = ends[1];
+    if (ends[0] != 0 || nnz < 0 || (nnz > 0 && !d_rows)) return OPH_ERR_BAD_INPUT;
+    if (m > sv->mcap || sv->region_ints(m, nnz) + 2 * (m + 1) + nnz > sv->pool_ints) return OPH_ERR_OOM;
+    // the server's own copy (the caller may free its buffers on return), and
+    // the same structural checks as oph_server_submit, on the device
+    const size_t bytes = sizeof(int64_t) * (m + 1) + sizeof(int32_t) * nnz + sizeof(int);
+    void *buf = nullptr;
+    if (cudaMallocAsync(&buf, bytes, s) != cudaSuccess) {
+        cudaGetLastError();
+        return OPH_ERR_OOM;
+    }
+    int64_t *cp = static_cast<int64_t *>(buf);
+    int32_t *rw = reinterpret_cast<int32_t *>(cp + m + 1);
+    int *bad = reinterpret_cast<int *>(rw + nnz);
+    int h_bad = 0;
+    cudaMemcpyAsync(cp, d_colptr, sizeof(int64_t) * (m + 1), cudaMemcpyDeviceToDevice, s);
+    if (nnz) cudaMemcpyAsync(rw, d_rows, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(bad, 0, sizeof(int), s);
+    if (m > 0) k_srv_check<<<sv->grid(m), 256, 0, s>>>(cp, rw, m, nnz, bad);
+    cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess || h_bad) {
+        cudaFreeAsync(buf, s);
+        cudaStreamSynchronize(s);
+        return e != cudaSuccess ? OPH_ERR_CUDA : OPH_ERR_BAD_INPUT;
+    }
+    Request *r = new Request();
+    r->m = m;
+    r->nnz = nnz;
+    r->d_buf = buf;
+    r->t_submit = now_ms();
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        if (sv->error) {
+            cudaFreeAsync(buf, s);
+            delete r;
+            return sv->error;
+        }
+        r->ticket = sv->next_ticket++;
+        sv->all[r->ticket] = r;
+        sv->pending.push_back(r);
+        *ticket = r->ticket;
+    }
+    sv->cv_work.notify_one();
+    return OPH_OK;
+}
+
 __attribute__((visibility("default"))) int oph_server_wait(oph_server *sv, int64_t ticket, int32_t *low,
                                                            int32_t *ess, oph_request_info *info, int64_t timeout_ms) {
     if (!sv) return OPH_ERR_BAD_INPUT;
@@ -606,7 +693,12 @@ __attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
     }
     sv->cv_work.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
-    for (auto &kv : sv->all) delete kv.second;
+    cudaSetDevice(sv->ctx->device);
+    for (auto &kv : sv->all) {
+        if (kv.second->d_buf) cudaFree(kv.second->d_buf);
+        delete kv.second;
+    }
+    if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
     if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
     if (sv->h_iover) cudaFreeHost(sv->h_iover);
     oph_context_destroy(reinterpret_cast<oph_context *>(sv->ctx));

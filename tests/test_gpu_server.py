@@ -78,3 +78,60 @@ def test_tight_arena_regrows(cuda_lib):
     want, want_ess, _ = oracle.twist(bm)
     np.testing.assert_array_equal(low, want)
     np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_device_submissions_mixed_with_host(cuda_lib):
+    """Matrices built on the GPU and submitted from device memory run in the
+    same batch as host submissions; each result equals the oracle's, and the
+    device buffers may be freed as soon as submission returns."""
+    import torch
+    host = [cx.rips_cube(14, seed=5), cx.lower_star_image(20, 20, seed=6, sigma=2.0)]
+    pts = cx.points_torus(200, 3)
+    thr = cx.rips_threshold(pts, 40_000)
+    img = cx.image_smoothed(48, 40, 7)
+    with Server(0, budget_bytes=1 << 30, max_active=16) as srv:
+        dev = [cx.rips_device(pts, thr), cx.lower_star_device(img), cx.rips_device(cx.points_cube(9, 2))]
+        want_dev = [cx.rips(pts, thr), cx.lower_star(img), cx.rips(cx.points_cube(9, 2))]
+        tickets = []
+        for k in range(3):
+            tickets.append(("d", k, srv.submit_device(dev[k])))
+            if k < len(host):
+                tickets.append(("h", k, srv.submit(host[k])))
+        del dev
+        torch.cuda.empty_cache()
+        res = {(kind, k): srv.wait(t) for kind, k, t in tickets}
+        assert srv.stats()["completed"] == len(tickets)
+    for k, bm in enumerate(want_dev):
+        low, ess, _ = res[("d", k)]
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
+    for k, bm in enumerate(host):
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(res[("h", k)][0], want)
+        np.testing.assert_array_equal(res[("h", k)][1], want_ess)
+
+
+def test_device_submission_rejects_malformed(cuda_lib):
+    """A device colptr that decreases, or a row index out of range, is
+    refused at submission with BAD_INPUT; the server keeps working."""
+    import torch
+    from openph_gb300.api import OPH_ERR_BAD_INPUT
+    from openph_gb300.complexes import DeviceMatrix
+    bm = cx.rips_cube(6, seed=1)
+    with Server(0, budget_bytes=256 << 20, max_active=4) as srv:
+        cp = torch.as_tensor(bm.colptr, device="cuda")
+        rows = torch.as_tensor(bm.rows, device="cuda").clone()
+        last = int(bm.colptr[-1]) - 1
+        rows[last] = bm.m  # a row past the last column
+        with pytest.raises(OphError) as e:
+            srv.submit_device(DeviceMatrix(cp, rows, None))
+        assert e.value.status == OPH_ERR_BAD_INPUT
+        cp_bad = cp.clone()
+        cp_bad[2] = cp_bad[3] + 1
+        with pytest.raises(OphError) as e:
+            srv.submit_device(DeviceMatrix(cp_bad, torch.as_tensor(bm.rows, device="cuda"), None))
+        assert e.value.status == OPH_ERR_BAD_INPUT
+        good = DeviceMatrix(cp, torch.as_tensor(bm.rows, device="cuda"), None)
+        low, _, _ = srv.wait(srv.submit_device(good))
+    np.testing.assert_array_equal(low, oracle.twist(bm)[0])
