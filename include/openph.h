@@ -94,6 +94,7 @@ typedef struct {
     int64_t pool_bytes;      /* column-store bytes in use at the end           */
     int32_t regrows;         /* times the column store had to grow             */
     float device_ms;         /* device time of the reduction (CUDA events)     */
+    int32_t dual;            /* 1 when pms reduced the anti-transpose          */
 } oph_info;
 
 /* A context owns one CUDA stream on one device plus cached device buffers;
@@ -244,6 +245,25 @@ int oph_context_autotune_batch(oph_context *ctx, int32_t count, const int64_t *c
                                const int32_t *rows, int32_t *lanes, int32_t *cap, float *best_ms);
 /* Set the narrow-tier configuration directly (must be a candidate). */
 int oph_context_set_tier0(oph_context *ctx, int32_t lanes, int32_t cap);
+
+/* Which matrix pms reduces (no counterpart in the reference, whose pms
+ * always reduces D).  The low pairs of D and of its anti-transpose D'
+ * (entry (i, j) of D at (m-1-j, m-1-i)) determine each other, so reducing
+ * D' gives the same low and ess; it moves the work from the top dimension,
+ * which twist and pms on D must reduce column by column, to the bottom one.
+ *   OPH_DUAL_AUTO    D' when the input is graded (every column's rows from
+ *                    one dimension bucket, distinct buckets from distinct
+ *                    ones), has at least 2^17 columns and its top bucket
+ *                    holds at least 8 times the columns of the bottom one
+ *                    (Rips complexes), else D
+ *   OPH_DUAL_NEVER   always D
+ *   OPH_DUAL_ALWAYS  D' whenever the input is graded
+ * Reductions with per-sweep trackers (oph_openph with tracker outputs)
+ * always reduce D, whose progress the trackers describe.  Default AUTO. */
+#define OPH_DUAL_AUTO 0
+#define OPH_DUAL_NEVER 1
+#define OPH_DUAL_ALWAYS 2
+int oph_context_set_dual(oph_context *ctx, int32_t mode);
 
 /* Testing hooks: cap the sweep count (0 = default) and the initial column
  * store size in bytes (0 = default), to exercise the timeout and regrow

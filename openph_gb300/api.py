@@ -23,6 +23,7 @@ from . import _build
 ALGORITHMS = ("standard", "twist", "ph_row", "standard_parallel", "twist_parallel", "ph_row_parallel", "pms")
 
 OPH_OK, OPH_ERR_BAD_INPUT, OPH_ERR_OOM, OPH_ERR_OVERFLOW, OPH_ERR_TIMEOUT, OPH_ERR_CUDA, OPH_ERR_ALGO = range(7)
+OPH_DUAL_AUTO, OPH_DUAL_NEVER, OPH_DUAL_ALWAYS = range(3)
 
 
 class OphError(RuntimeError):
@@ -34,7 +35,7 @@ class OphError(RuntimeError):
 class Info(C.Structure):
     _fields_ = [("num_iters", C.c_int32), ("sweeps", C.c_int32), ("additions", C.c_int64),
                 ("slots_moved", C.c_int64), ("pool_bytes", C.c_int64), ("regrows", C.c_int32),
-                ("device_ms", C.c_float)]
+                ("device_ms", C.c_float), ("dual", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -123,6 +124,7 @@ def lib():
         L.oph_context_autotune_batch.argtypes = [vp, C.c_int32, i64, i64, vp, C.POINTER(C.c_int32),
                                                  C.POINTER(C.c_int32), C.POINTER(C.c_float)]
         L.oph_context_set_tier0.argtypes = [vp, C.c_int32, C.c_int32]
+        L.oph_context_set_dual.argtypes = [vp, C.c_int32]
         L.oph_last_profile.argtypes = [vp, C.POINTER(Profile)]
         _lib = L
     return _lib
@@ -357,6 +359,16 @@ class Context:
         rc = lib().oph_context_set_tier0(self._h, int(lanes), int(cap))
         if rc != OPH_OK:
             raise OphError(rc, "oph_context_set_tier0")
+
+    def set_dual(self, mode):
+        """Which matrix pms reduces: "auto" (the anti-transpose for graded
+        inputs of >= 2^17 columns whose top dimension bucket holds >= 8x the
+        columns of the bottom one), "never" or "always" (the anti-transpose
+        when graded)."""
+        code = {"auto": OPH_DUAL_AUTO, "never": OPH_DUAL_NEVER, "always": OPH_DUAL_ALWAYS}.get(mode, mode)
+        rc = lib().oph_context_set_dual(self._h, int(code))
+        if rc != OPH_OK:
+            raise OphError(rc, "oph_context_set_dual")
 
     def set_profile(self, on: bool = True, slots: bool = False):
         """Per-phase event timing (``on``); ``slots`` also tracks the exact

@@ -214,25 +214,40 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
     ctx->launches = 0;
     ctx->prof = oph_profile{};
     if (ctx->profile) cudaEventRecord(ctx->ev[2], s);
-    int rc = setup_store(ctx, w, pms);
+    // pms on the anti-transpose where that moves the work to a far smaller
+    // dimension bucket (not with per-sweep trackers, which follow D's own
+    // reduction); wr is the matrix reduced
+    int rc;
+    bool dual = false;
+    if (pms && !ctx->track) {
+        bool bad = false;
+        if ((rc = dual_choose(ctx, w, ctx->dual, &dual, &bad))) return rc;
+        if (bad) return OPH_ERR_BAD_INPUT;
+    }
+    Work wd;
+    if (dual && (rc = dual_build(ctx, w, wd))) return rc;
+    Work &wr = dual ? wd : w;
+    rc = setup_store(ctx, wr, pms);
     if (rc) return rc;
     ctx->launches += pms ? 3 : 1;
+    if (dual) dual_dims(ctx, w, wd);
     if (ctx->profile) {
         cudaEventRecord(ctx->ev[3], s);
         cudaEventSynchronize(ctx->ev[3]);
         cudaEventElapsedTime(&ctx->prof.setup_ms, ctx->ev[2], ctx->ev[3]);
     }
     DevStatus hs;
-    if ((rc = ctx_sync_status(ctx, w, &hs))) return rc;
+    if ((rc = ctx_sync_status(ctx, wr, &hs))) return rc;
     if (hs.error) return OPH_ERR_BAD_INPUT;
-    // the Phase I scan keeps one running maximum per dimension bucket -1 .. MAXC-2
-    if (pms && hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;
+    // the Phase I scan keeps one running maximum per dimension bucket -1 ..
+    // MAXC-2 (D's buckets, checked by dual_choose when D' is reduced)
+    if (pms && !dual && hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;
     const int row_quirk = algo == OPH_ALGO_PH_ROW;
     if (row_quirk && o.ess) k_fill_i32<<<grid_for(ctx, m), 256, 0, s>>>(o.ess, m, 1);
     oph_info local{};
     if (m > 0) {
         if (pms) {
-            rc = run_pms(ctx, w, &local);
+            rc = run_pms(ctx, wr, &local);
         } else {
             rc = run_sequential(ctx, w, algo, row_quirk ? o.ess : nullptr, &local);
         }
@@ -241,6 +256,13 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
         local.num_iters = 1;
     }
     const int ess_mode = algo == OPH_ALGO_PH_ROW_PARALLEL ? ESS_ROW_PARALLEL : (row_quirk ? ESS_RUNNING : ESS_PAIRS);
+    if (dual && m > 0) {
+        // D's lows, back in w.low for the outputs and the trackers
+        int32_t *mapped = nullptr;
+        if ((rc = dual_lows(ctx, wd, &mapped))) return rc;
+        OPH_CUDA_TRY(cudaMemcpyAsync(w.low, mapped, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
+    }
+    local.dual = dual ? 1 : 0;
     if (m > 0) {
         k_finalize1<<<grid_for(ctx, m), 256, 0, s>>>(w.low, m, o.one_based, ess_mode, o.inst_off, o.count, o.low,
                                                      o.ess, o.arglow);
@@ -678,6 +700,12 @@ struct TuneOne { int64_t m; const int64_t *colptr; const int32_t *rows; int32_t 
 struct TuneBatch { int32_t count; const int64_t *col_off, *colptr; const int32_t *rows; int32_t *low; };
 
 extern "C" {
+
+__attribute__((visibility("default"))) int oph_context_set_dual(oph_context *ctx, int32_t mode) {
+    if (!ctx || mode < OPH_DUAL_AUTO || mode > OPH_DUAL_ALWAYS) return OPH_ERR_BAD_INPUT;
+    ctx->dual = mode;
+    return OPH_OK;
+}
 
 __attribute__((visibility("default"))) int oph_context_set_tier0(oph_context *ctx, int32_t lanes, int32_t cap) {
     if (!ctx) return OPH_ERR_BAD_INPUT;

@@ -55,7 +55,6 @@ struct DevStatus {
     int wl_count;                  // Phase II worklist size (tier 0 input)
     int s_cursor;                  // scalar tier: work-queue cursor
     int s_out;                     //   and the columns it hands to tier 0
-    int wide_cursor;               // unused
     int t_count[4];                // Phase II tier queues: columns queued per tier
     int t_cursor[4];               //   and the work-queue cursor of each tier
     int reps;                      // repeated lows seen by the last Phase I
@@ -66,6 +65,9 @@ struct DevStatus {
     int ucount[2];                     // compacted Phase I: list sizes (ping-pong)
     unsigned long long tier_adds[4];   // additions performed by each Phase II tier
     unsigned long long tier_slots[4];  // |P| + |T| + |T xor P| summed per tier
+    unsigned long long s_adds;         // the scalar tier's share of tier_adds[0]
+    int bucket_open;                   // ascending order: highest bucket (dim + 1) Phase II takes
+    int bucket_unres[MAXC];            //   and the unresolved columns per bucket (this sweep)
     // diagnostics of the lazy tiers 0 and 1 (filled only in OPH_COUNTS builds),
     // per tier t at [8t ..]: additions by a pivot held in its record, by a
     // pivot of <= 4 rows read from its segment, by one of 5 .. G + 1 rows, by

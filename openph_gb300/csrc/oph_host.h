@@ -48,6 +48,7 @@ struct Work {
     int64_t ntiles = 0;
     int *pool = nullptr;              // column store
     DevStatus *st = nullptr;
+    bool ascending = false;           // pms: buckets in ascending order (the anti-transpose)
 };
 
 struct Context;
@@ -63,6 +64,20 @@ int run_pms(Context *ctx, Work &w, oph_info *info);
 
 // variants.cu
 int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *info);
+
+// dual.cu: pms on the anti-transpose.  dual_choose grades w's buckets and
+// decides (*bad_input: malformed CSC); dual_build writes the anti-transpose
+// into wd (wd shares w's per-column arrays); dual_dims gives wd D's buckets
+// after the set-up; dual_lows maps wd's lows back to D's.
+// The automatic choice: D' for matrices of at least DUAL_MIN_M columns whose
+// top bucket holds DUAL_RATIO times the bottom one's columns (below that
+// size the few more sweeps and the transpose cost more than D's additions).
+constexpr unsigned long long DUAL_RATIO = 8;
+constexpr int64_t DUAL_MIN_M = 1 << 17;
+int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input);
+int dual_build(Context *ctx, const Work &w, Work &wd);
+void dual_dims(Context *ctx, const Work &w, Work &wd);
+int dual_lows(Context *ctx, const Work &wd, int32_t **low);
 
 // capi.cu
 void *ctx_alloc(Context *ctx, int slot, size_t bytes);
@@ -87,7 +102,7 @@ struct Context {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
-    DevBuf bufs[32];
+    DevBuf bufs[48];
     DevStatus *h_status = nullptr;  // pinned mirror
     int max_sweeps = 0;             // 0 = default
     int64_t initial_pool_bytes = 0; // 0 = default
@@ -100,6 +115,7 @@ struct Context {
     oph_profile prof{};             // last reduction
     int launches = 0;               // kernels launched by the current reduction
     int tier0 = 0;                  // Phase II tier-0 candidate (autotuned)
+    int dual = OPH_DUAL_AUTO;       // which matrix pms reduces
     Tracking *track = nullptr;      // per-sweep trackers for the current reduction
     // two pms sweeps (the list ping-pong's two parities) captured as one CUDA
     // graph and replayed instead of 2 x 11 launches; sweep_key holds the
@@ -112,7 +128,7 @@ struct Context {
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_NSLOTS
 };
 
 }  // namespace oph

@@ -218,7 +218,9 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
     if ((int64_t)blockIdx.x * P1_TILE >= n) return;
     __shared__ int sm[P1_THREADS / 32][MAXC];
     __shared__ int skeep;
+    __shared__ int sunres[MAXC];
     if (threadIdx.x == 0) skeep = 0;
+    if (threadIdx.x < MAXC) sunres[threadIdx.x] = 0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
     int lows[P1_ITEMS], bkt[P1_ITEMS];
@@ -277,24 +279,29 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
         for (int d = 0; d < MAXC; d++)
             if (d == bkt[t]) ceil = pre[d];
         const int cls = a.classes[j];
+        bool kept = false;
         if (rep[t]) {
 #pragma unroll
             for (int d = 0; d < MAXC; d++)
                 if (d == bkt[t]) pre[d] = max(pre[d], lj);
-            keep += cls == 0;
+            kept = cls == 0;
         } else if (cls == 0 && lj > ceil) {
             a.classes[j] = -1;
             const long long sj = a.seg[j];
             rec_publish<false>(a.rec, lj, (int)j, a.pool[sj], sj, a.pool + sj + SEG_HDR);
             a.clear[lj] = 1;
         } else {
-            keep += cls == 0;
+            kept = cls == 0;
         }
+        keep += kept;
+        if (kept && a.ascending) atomicAdd(&sunres[bkt[t]], 1);
     }
     if (a.ulist) {
         if (keep) atomicAdd(&skeep, keep);
         __syncthreads();
         if (threadIdx.x == 0) a.kagg[blockIdx.x] = skeep;
+        if (a.ascending && threadIdx.x < MAXC && sunres[threadIdx.x])
+            atomicAdd(&a.st->bucket_unres[threadIdx.x], sunres[threadIdx.x]);
     }
 }
 
@@ -325,7 +332,19 @@ __global__ void k_p1_kscan(PmsArgs a) {
         carry += total;
         __syncthreads();
     }
-    if (threadIdx.x == 0) *a.unext = carry;
+    if (threadIdx.x == 0) {
+        *a.unext = carry;
+        if (a.ascending) {
+            // the lowest bucket with unresolved columns opens (counts of
+            // this sweep's k_p1_mark, cleared for the next one)
+            int open = MAXC;
+            for (int d = MAXC - 1; d >= 0; d--) {
+                if (a.st->bucket_unres[d] > 0) open = d;
+                a.st->bucket_unres[d] = 0;
+            }
+            a.st->bucket_open = open;
+        }
+    }
 }
 
 // (f) compacted list: the columns that stay unresolved, in order, into the
@@ -393,10 +412,13 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
     // Phase II takes these columns from a queue filled by warp-aggregated
     // appends: concurrently reduced columns then come from all over the
     // matrix instead of one neighbourhood (which contends on shared pivots).
-    // Only columns that can add this sweep are queued (p2_ready).
+    // Only columns that can add this sweep are queued (p2_ready), and in
+    // ascending order only those of the open buckets.
+    const int open = a.ascending ? __ldcg(&a.st->bucket_open) : MAXC;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
-        const bool want = ((keepmask >> t) & 1u) && (!OPH_P2_FILTER || p2_ready(a, cols[t]));
+        const bool want = ((keepmask >> t) & 1u) && a.dim[cols[t]] + 1 <= open &&
+                          (!OPH_P2_FILTER || p2_ready(a, cols[t]));
         warp_append(want, cols[t], a.worklist, &a.st->t_count[0]);
     }
 }
@@ -790,19 +812,23 @@ __device__ __forceinline__ int ts_toggle(int *col, int m1, int x) {
 #define OPH_TS_REFILL 24
 #endif
 constexpr int TS_REFILL = OPH_TS_REFILL;
-#ifndef OPH_TS_MINB
-#define OPH_TS_MINB 0
-#endif
-#if OPH_TS_MINB > 0
-__global__ void __launch_bounds__(TS_BLOCK, OPH_TS_MINB) k_p2_scalar(PmsArgs a) {
-#else
-__global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
-#endif
+// The queue a scalar pass takes its columns from, and the list it hands on to.
+struct ScalarQ {
+    const int32_t *in;
+    const int *in_count;
+    int *cursor;
+    int32_t *out;
+    int *out_count;
+};
+
+// CAP rows per lane in BLOCK * CAP ints of dynamic shared memory.
+template <int CAP, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_p2_scalar(PmsArgs a, ScalarQ sq) {
     if (a.st->converged) return;
-    __shared__ int sm[(TS_BLOCK / 32) * TS_CAP * 32];
+    extern __shared__ int sm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int *col = sm + wid * TS_CAP * 32 + lane;
-    const int count = a.st->t_count[0];
+    int *col = sm + wid * CAP * 32 + lane;
+    const int count = *sq.in_count;
     long long adds = 0, slots = 0;
     bool active = false, exhausted = false;
     int j = -1, n = 0, lj = -1, capj = 0;
@@ -845,7 +871,7 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
                 }
                 fin = 0;
             }
-            warp_append(handoff, j, a.slist, &a.st->s_out);
+            warp_append(handoff, j, sq.out, sq.out_count);
             handoff = false;
             // lanes without a column take the next ones from the queue
             const bool need = !active && !exhausted;
@@ -853,14 +879,14 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
             if (nm) {
                 const int leader = __ffs(nm) - 1;
                 int base = 0;
-                if (lane == leader) base = atomicAdd(&a.st->s_cursor, __popc(nm));
+                if (lane == leader) base = atomicAdd(sq.cursor, __popc(nm));
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (need) {
                     const int idx = base + __popc(nm & ((1u << lane) - 1u));
                     if (idx >= count) {
                         exhausted = true;
                     } else {
-                        j = a.worklist[idx];
+                        j = sq.in[idx];
                         lj = a.low[j];
                         bool ok = lj >= 0 && !a.clear[j];
                         if (ok) {
@@ -873,15 +899,15 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
                             capj = a.pool[sj + 1];
                             // a column this tier cannot add its first pivot to
                             // goes to tier 0 untouched
-                            if (n > TS_CAP || !rec_complete(h, e) || n + h.y - 2 > TS_CAP) {
+                            if (n > CAP || !rec_complete(h, e) || n + h.y - 2 > CAP) {
                                 handoff = true;
                                 if (OPH_COUNTS) dg.c[1]++;
                             } else {
                                 // 16-byte loads issued together (a segment starts
                                 // on 16 bytes, its capacity a multiple of four)
                                 const int4 *src = reinterpret_cast<const int4 *>(a.pool + sj + SEG_HDR);
-#pragma unroll
-                                for (int q = 0; q < TS_CAP / 4; q++)
+#pragma unroll 12
+                                for (int q = 0; q < CAP / 4; q++)
                                     if (4 * q < n) {
                                         const int4 v = __ldcg(src + q);
                                         col[(4 * q) * 32] = v.x;
@@ -896,13 +922,13 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
                     }
                 }
             }
-            warp_append(handoff, j, a.slist, &a.st->s_out);
+            warp_append(handoff, j, sq.out, sq.out_count);
             if (__all_sync(0xffffffffu, !active && exhausted)) break;
         }
         // one addition on every column that has a pivot to add
         if (active) {
             const int np = h.y;
-            if (!rec_complete(h, e) || n + np - 2 > TS_CAP) {
+            if (!rec_complete(h, e) || n + np - 2 > CAP) {
                 fin = 1;
                 if (OPH_COUNTS) dg.c[2]++;
             } else {
@@ -929,7 +955,10 @@ __global__ void __launch_bounds__(TS_BLOCK) k_p2_scalar(PmsArgs a) {
         adds += __shfl_xor_sync(0xffffffffu, adds, o);
         slots += __shfl_xor_sync(0xffffffffu, slots, o);
     }
-    if (lane == 0) tier_stats(a, 0, adds, slots);
+    if (lane == 0) {
+        tier_stats(a, 0, adds, slots);
+        if (adds) atomicAdd(&a.st->s_adds, (unsigned long long)adds);
+    }
     if (OPH_COUNTS)
         for (int q = 0; q < 6; q++)
             if (dg.c[q]) atomicAdd(&a.st->sdiag[q], dg.c[q]);
@@ -1139,6 +1168,210 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
     if (threadIdx.x == 0) tier_stats(a, tier, adds, slots);
 }
 
+// ------------------------------------------------------------ bitmap tier
+// Tier 3's columns (longer than tier 2's shared buffers) as a bitmap over
+// rows [w0, w0 + 32 * bm_words) in a per-CTA scratch in global memory: an
+// addition toggles the pivot's bits, O(|P|) work where a merge rewrites all
+// of T (the reduced cochains of a Rips complex's anti-transpose run to ~10^5
+// rows against pivots of a few hundred); the next low is the highest set bit
+// below the old one; the rows are written back in order, and the words
+// cleared, once, when the chain ends.  A row below w0 (a window smaller than
+// the matrix) sends the column to the merge path instead.
+constexpr int64_t BM_MAX_WORDS = 1 << 18;
+
+template <class Op>
+__device__ __forceinline__ int block_reduce(int v, int *red, Op op) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    int r = red[0];
+    for (int w = 1; w < nw; w++) r = op(r, red[w]);
+    __syncthreads();
+    return r;
+}
+struct OpSum {
+    __device__ int operator()(int x, int y) const { return x + y; }
+};
+struct OpMax {
+    __device__ int operator()(int x, int y) const { return max(x, y); }
+};
+
+// Highest set bit at or below word wl (window-relative), -1 if none.
+__device__ int bitmap_top(const uint32_t *bm, int wl, int *red) {
+    for (int base = wl; base >= 0; base -= (int)blockDim.x) {
+        const int w = base - (int)threadIdx.x;
+        const uint32_t v = w >= 0 ? __ldcg(bm + w) : 0u;
+        const int best = block_reduce(v ? w : -1, red, OpMax{});
+        if (best >= 0) return best * 32 + 31 - __clz(__ldcg(bm + best));
+    }
+    return -1;
+}
+
+// Rows of words [0, top] in ascending order into dst (when not null), the
+// words zeroed.  Returns the number of rows.
+__device__ int bitmap_extract(uint32_t *bm, int top, int w0, int *dst, int *red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int out = 0;
+    for (int base = 0; base <= top; base += (int)blockDim.x) {
+        const int w = base + (int)threadIdx.x;
+        uint32_t v = w <= top ? __ldcg(bm + w) : 0u;
+        const int c = __popc(v);
+        int incl = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) red[wid] = incl;
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int q = 0; q < nw; q++) {
+            if (q < wid) before += red[q];
+            total += red[q];
+        }
+        __syncthreads();
+        if (v) {
+            int pos = out + before + incl - c;
+            if (dst)
+                while (v) {
+                    dst[pos++] = w0 + w * 32 + (__ffs(v) - 1);
+                    v &= v - 1;
+                }
+            bm[w] = 0u;
+        }
+        out += total;
+    }
+    __syncthreads();
+    return out;
+}
+
+// Returns true when the column needs the merge path (its state written back
+// first).
+__device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long long &adds, long long &slots) {
+    __shared__ int s_red[32];
+    __shared__ int s_small[4];
+    __shared__ long long s_off;
+    const int tid = threadIdx.x;
+    if (a.clear[j]) return false;
+    int lj = a.low[j];
+    if (lj < 0) return false;
+    int4 h, e;
+    rec_load(&a.rec[lj], h, e);
+    if (h.x < 0 || h.x >= j) return false;
+    const long long sj = a.seg[j];
+    int n = a.pool[sj];
+    const int capj = a.pool[sj + 1];
+    const int *T = a.pool + sj + SEG_HDR;
+    const long long nbits = 32ll * a.bm_words;
+    // the window's first row: a multiple of 32 with lj - w0 < nbits
+    const int w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 31) & ~31ll) : 0;
+    if (n > 0 && T[0] < w0) return true;
+    for (int k = tid; k < n; k += blockDim.x) {
+        const int r = T[k] - w0;
+        atomicOr(bm + (r >> 5), 1u << (r & 31));
+    }
+    __syncthreads();
+    bool made_pivot = false, fell_back = false;
+    for (;;) {
+        int np;
+        const int *P;
+        if (rec_complete(h, e)) {
+            np = h.y;
+            if (tid < np) s_small[tid] = rec_entry(e, tid);
+            __syncthreads();
+            P = s_small;
+        } else {
+            const int4 h2 = rec_header(&a.rec[lj], h);
+            np = h2.y;
+            P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
+        }
+        if (P[0] < w0) {  // the pivot reaches below the window
+            fell_back = true;
+            break;
+        }
+        int d = 0;
+        for (int k = tid; k < np; k += blockDim.x) {
+            const int r = P[k] - w0;
+            const uint32_t bit = 1u << (r & 31);
+            d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
+        }
+        d = block_reduce(d, s_red, OpSum{});
+        slots += n + np + (n + d);
+        adds++;
+        n += d;
+        if (n == 0) {
+            lj = -1;
+            break;
+        }
+        // lj's bit went with the pivot's top: the next low lies below it
+        const int tb = bitmap_top(bm, (lj - w0) >> 5, s_red);
+        if (tb < 0) {  // cannot happen while n > 0; never index rec[-1]
+            n = 0;
+            lj = -1;
+            break;
+        }
+        lj = w0 + tb;
+        rec_load(&a.rec[lj], h, e);
+        mark_clear<false>(a, lj, tid == 0);
+        if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
+        if (h.x < 0 || h.x >= j) break;
+    }
+    long long dst = sj;
+    int dcap = capj;
+    bool stored = true;
+    if (n > capj) {
+        dcap = round4(max(n + (n >> 1), 16));
+        if (tid == 0) s_off = col_alloc(a, j, SEG_HDR + dcap);
+        __syncthreads();
+        stored = s_off >= 0;  // pool exhausted: j keeps its pre-sweep state
+        dst = s_off;
+    }
+    const int top = n > 0 ? (lj - w0) >> 5 : -1;
+    bitmap_extract(bm, top, w0, stored ? a.pool + dst + SEG_HDR : nullptr, s_red);
+    if (!stored) return false;
+    if (tid == 0) {
+        a.pool[dst] = n;
+        a.pool[dst + 1] = dcap;
+        a.seg[j] = dst;
+        a.low[j] = lj;
+    }
+    if (made_pivot) {
+        fence_acq_rel();
+        __syncthreads();
+        if (tid == 0) {
+            a.classes[j] = -1;
+            rec_publish(a.rec, lj, j, n, dst, a.pool + dst + SEG_HDR);
+        }
+    }
+    __syncthreads();
+    return fell_back;
+}
+
+// Tier 3: the bitmap path (per-CTA scratch at bm + blockIdx.x * bm_words),
+// or the merge path in pool buffers when there is no scratch or the window
+// does not reach a column's rows.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_p2_bitmap(PmsArgs a, int tier) {
+    if (a.st->converged) return;
+    __shared__ int scratch[2 * (BLOCK / 32)];
+    __shared__ int s_idx;
+    const int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
+    const int count = a.st->t_count[tier];
+    uint32_t *bm = a.bm ? a.bm + (size_t)blockIdx.x * a.bm_words : nullptr;
+    long long adds = 0, slots = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(&a.st->t_cursor[tier], 1);
+        __syncthreads();
+        const int idx = s_idx;
+        __syncthreads();
+        if (idx >= count) break;
+        const int j = in_list[idx];
+        if (!bm || reduce_column_bitmap(a, j, bm, adds, slots))
+            reduce_column_block(a, j, nullptr, nullptr, nullptr, 0, scratch, nullptr, nullptr, adds, slots);
+    }
+    if (threadIdx.x == 0) tier_stats(a, tier, adds, slots);
+}
+
 __global__ void k_count_sweep(DevStatus *st) {
     if (!st->converged) st->sweeps++;
 }
@@ -1230,7 +1463,9 @@ int t0_candidate(int v, int *lanes, int *cap) {
 
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     static int done1[64], done2[64], dones[64];
-    g->gs = fill_grid(ctx, k_p2_scalar, TS_BLOCK, 0, dones);
+    g->ss = (size_t)TS_BLOCK * TS_CAP * sizeof(int);
+    g->gs = fill_grid(ctx, k_p2_scalar<TS_CAP, TS_BLOCK>, TS_BLOCK, g->ss, dones);
+
     g->v0 = (ctx->tier0 >= 0 && ctx->tier0 < T0_CANDIDATES) ? ctx->tier0 : 0;
     g->s1 = (size_t)(T1_BLOCK / T1_G) * (T1_STAGE ? 3 : 2) * T1_CAP * sizeof(int);
     g->s2 = (size_t)3 * T2_CAP * sizeof(int);
@@ -1335,14 +1570,18 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
         k_p1_worklist<<<g.m, 256, 0, s>>>(a);
     }
     if (ev) cudaEventRecord(ev[1], s);
-    if (a.slist) k_p2_scalar<<<g.gs, TS_BLOCK, 0, s>>>(a);
+    if (a.slist) {
+        DevStatus *st = a0.st;
+        k_p2_scalar<TS_CAP, TS_BLOCK><<<g.gs, TS_BLOCK, g.ss, s>>>(
+            a, ScalarQ{a.worklist, &st->t_count[0], &st->s_cursor, a.slist, &st->s_out});
+    }
     launch_t0(a, g, s);
     if (ev) cudaEventRecord(ev[2], s);
     k_p2_tier1<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY><<<g.g1, T1_BLOCK, g.s1, s>>>(a, 1);
     if (ev) cudaEventRecord(ev[3], s);
     k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
     if (ev) cudaEventRecord(ev[4], s);
-    k_p2_block<0, T3_BLOCK><<<g.g3, T3_BLOCK, 0, s>>>(a, 3);
+    k_p2_bitmap<T3_BLOCK><<<g.g3, T3_BLOCK, 0, s>>>(a, 3);
     k_count_sweep<<<1, 1, 0, s>>>(a.st);
     if (ev) cudaEventRecord(ev[5], s);
 }
@@ -1358,7 +1597,11 @@ void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int par
     launch_sweep_ev(a, g, s, nullptr, parity);
 }
 
-constexpr int KERNELS_PER_SWEEP = 11;
+// Kernels one sweep launches (launch_sweep_ev): Phase I (six with the
+// compacted list, else five), the scalar tier, tiers 0-3, the counter.
+static int kernels_per_sweep(const PmsArgs &a) {
+    return (a.ulist ? 6 : 5) + (a.slist ? 1 : 0) + 4 + 1;
+}
 
 // Sweeps replayed from a captured CUDA graph (0: launched one by one).
 #ifndef OPH_GRAPHS
@@ -1419,11 +1662,18 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         a.kagg = (int32_t *)ctx_alloc(ctx, S_KAGG, sizeof(int32_t) * (w.ntiles + 1));
         if (!a.ulist || !a.kagg) return OPH_ERR_OOM;
         a.ulist_next = a.ulist + m;
+        a.ascending = w.ascending ? 1 : 0;
     }
     cudaStream_t s = ctx->stream;
     SweepGrids g{};
     int rc = sweep_grids(ctx, m, w.ntiles, &g);
     if (rc) return rc;
+    // tier 3's bitmaps: a window of the whole matrix up to 2^23 rows per CTA,
+    // zeroed here (each column leaves its words zeroed)
+    a.bm_words = std::min<int64_t>((m + 32) / 32, BM_MAX_WORDS);
+    a.bm = (uint32_t *)ctx_alloc(ctx, S_BITMAP, sizeof(uint32_t) * (size_t)a.bm_words * g.g3);
+    if (!a.bm) return OPH_ERR_OOM;
+    OPH_CUDA_TRY(cudaMemsetAsync(a.bm, 0, sizeof(uint32_t) * (size_t)a.bm_words * g.g3, s));
     if (a.ulist) {
         k_iota<<<g.m, 256, 0, s>>>(a.ulist, m);
         const int mi = (int)m;
@@ -1474,13 +1724,13 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         if (OPH_GRAPHS && !timed && (sweeps_launched & 1) == 0 && nb >= 2 && sweep_pair_graph(ctx, a, g)) {
             for (; b + 2 <= nb; b += 2) {
                 OPH_CUDA_TRY(cudaGraphLaunch(ctx->sweep_graph, s));
-                ctx->launches += 2 * KERNELS_PER_SWEEP;
+                ctx->launches += 2 * kernels_per_sweep(a);
             }
         }
         for (; b < nb; b++) {
             launch_sweep_ev(a, g, s, timed ? ctx->pev + 6 * b : nullptr, sweeps_launched + b);
             launch_track(a, g, s, tr, sweeps_launched + b + 1);
-            ctx->launches += KERNELS_PER_SWEEP;
+            ctx->launches += kernels_per_sweep(a);
         }
         sweeps_launched += nb;
         OPH_CUDA_TRY(cudaGetLastError());
@@ -1497,12 +1747,15 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
                 p2w_ms += t[2] + t[3] + t[4];
                 if (tr && b < worked) tr->sweep_ms.push_back(t[0] + t[1] + t[2] + t[3] + t[4]);
                 if (trace && b < worked)
-                    fprintf(stderr, "sweep %d: unresolved %d queued t0=%d t1=%d t2=%d t3=%d | adds t0=%llu t1=%llu t2=%llu "
-                                    "t3=%llu | ms p1=%.3f t0=%.3f t1=%.3f t2=%.3f t3=%.3f\n", hs.sweeps,
-                            a.ulist ? hs.ucount[hs.sweeps & 1] : -1, hs.t_count[0],
-                            hs.t_count[1], hs.t_count[2], hs.t_count[3], hs.tier_adds[0] - before.tier_adds[0],
+                    fprintf(stderr, "sweep %d: unresolved %d queued t0=%d (to tier 0: %d) t1=%d t2=%d t3=%d | adds "
+                                    "scalar=%llu t0=%llu t1=%llu t2=%llu t3=%llu | ms p1=%.3f t0=%.3f t1=%.3f t2=%.3f "
+                                    "t3=%.3f | open %d\n", hs.sweeps,
+                            a.ulist ? hs.ucount[hs.sweeps & 1] : -1, hs.t_count[0], a.slist ? hs.s_out : -1,
+                            hs.t_count[1], hs.t_count[2], hs.t_count[3], hs.s_adds - before.s_adds,
+                            hs.tier_adds[0] - before.tier_adds[0] - (hs.s_adds - before.s_adds),
                             hs.tier_adds[1] - before.tier_adds[1], hs.tier_adds[2] - before.tier_adds[2],
-                            hs.tier_adds[3] - before.tier_adds[3], t[0], t[1], t[2], t[3], t[4]);
+                            hs.tier_adds[3] - before.tier_adds[3], t[0], t[1], t[2], t[3], t[4],
+                            a.ascending ? hs.bucket_open - 1 : -2);
             }
             p2_launches += worked;
 #if OPH_COUNTS

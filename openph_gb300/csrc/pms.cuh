@@ -41,6 +41,15 @@ struct PmsArgs {
     int32_t *slist;
     // exact |P| + |T| + |T xor P| counters in the lazy tiers (profiling)
     int stats;
+    // buckets in ascending order (with the compacted list): Phase II takes
+    // columns of the lowest bucket that has unresolved ones and of those
+    // below, so that the pivots of a bucket clear the next one's columns
+    // before they are reduced (twist's order; for the anti-transpose)
+    int ascending;
+    // tier 3's bitmaps: bm_words 32-bit words per CTA of its grid (nullptr:
+    // tier 3 merges)
+    uint32_t *bm;
+    int64_t bm_words;
 };
 
 // Launch geometry of the Phase II tiers (occupancy-derived, per device).
@@ -53,7 +62,7 @@ struct SweepGrids {
     int m, t;               // grid of the per-column passes, Phase I tiles
     int g0, g1, g2, g3;     // Phase II tier grids
     int gs;                 //   and the scalar tier's
-    size_t s0, s1, s2;      // their dynamic shared memory
+    size_t s0, s1, s2, ss;  // their dynamic shared memory
 };
 
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g);

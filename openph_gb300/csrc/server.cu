@@ -242,27 +242,27 @@ struct Server {
     // Admission of one request into slot b; called by the worker only.
     int admit(Request *r, int b) {
         cudaStream_t s = ctx->stream;
-        const int64_t stage_ints = 2 * (r->m + 1) + r->nnz + 4;
+        // a host submission is staged in the pool; a device one was copied
+        // to its own buffer at submission
+        const bool host = r->d_buf == nullptr;
+        const int64_t stage_ints = host ? 2 * (r->m + 1) + r->nnz + 4 : 0;
         const int64_t reg_ints = region_ints(r->m, r->nnz);
         const int64_t c0 = cols.alloc(std::max<int64_t>(r->m, 1), 1);
         if (c0 < 0) return 1;
         const int64_t reg = pool.alloc(reg_ints, 64);
         if (reg < 0) { cols.release(c0, std::max<int64_t>(r->m, 1)); return 1; }
-        const int64_t stg = pool.alloc(stage_ints, 64);
+        const int64_t stg = host ? pool.alloc(stage_ints, 64) : 0;
         if (stg < 0) {
             cols.release(c0, std::max<int64_t>(r->m, 1));
             pool.release(reg, reg_ints);
             return 1;
         }
         r->c0 = c0; r->reg = reg; r->reg_ints = reg_ints; r->slot = b;
-        int64_t *d_colptr = reinterpret_cast<int64_t *>(a.pool + stg);
-        int32_t *d_rows = a.pool + stg + 2 * (r->m + 1);
-        if (r->d_buf) {
-            // submitted from device memory: read in place, freed after the
-            // kernels below (in stream order)
-            d_colptr = static_cast<int64_t *>(r->d_buf);
-            d_rows = reinterpret_cast<int32_t *>(d_colptr + r->m + 1);
-        } else {
+        int64_t *d_colptr = static_cast<int64_t *>(r->d_buf);
+        int32_t *d_rows = reinterpret_cast<int32_t *>(d_colptr + r->m + 1);
+        if (host) {
+            d_colptr = reinterpret_cast<int64_t *>(a.pool + stg);
+            d_rows = a.pool + stg + 2 * (r->m + 1);
             cudaMemcpyAsync(d_colptr, r->colptr.data(), sizeof(int64_t) * (r->m + 1), cudaMemcpyHostToDevice, s);
             if (r->nnz) cudaMemcpyAsync(d_rows, r->rows.data(), sizeof(int32_t) * r->nnz, cudaMemcpyHostToDevice, s);
         }
@@ -275,13 +275,15 @@ struct Server {
                                          (unsigned long long)(reg + packed_ints(r->m, r->nnz)),
                                          (unsigned long long)(reg + reg_ints));
         if (r->m > 0) launch_phase0(a, c0, c0 + r->m, grid(r->m), s);
-        if (r->d_buf) {
+        if (host) {
+            // the staged input is read by the kernels above: its region is
+            // released after the sweep's synchronisation
+            staged.emplace_back(stg, stage_ints);
+        } else {
+            // the device copy is freed in stream order after those kernels
             cudaFreeAsync(r->d_buf, s);
             r->d_buf = nullptr;
         }
-        // the staged input is read by the kernels above: its region is
-        // released after the sweep's synchronisation
-        staged.emplace_back(stg, stage_ints);
         r->t_admit = now_ms();
         slots[b] = r;
         admitted++;

@@ -2,7 +2,7 @@
 
     python -m openph_gb300.run_case [--workload rips_torus|lower_star|rips_cube|batch]
                                     [--target-m M] [--algo pms] [--steps K]
-                                    [--tier0 LANES,CAP] [--profile]
+                                    [--tier0 LANES,CAP] [--profile] [--dual MODE]
 
 Prints one JSON line with the device time per reduction and the library's
 counters.  The matrix is device-resident before the first reduction.
@@ -45,6 +45,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--tier0", default="", help="tier-0 lanes,capacity (default: the library's choice)")
     ap.add_argument("--profile", action="store_true", help="print per-phase times of the last step")
+    ap.add_argument("--dual", default="auto", help="pms on the anti-transpose: auto, never or always")
     args = ap.parse_args()
 
     import torch
@@ -56,6 +57,7 @@ def main():
     if args.tier0:
         ctx.set_tier0(*map(int, args.tier0.split(",")))
     ctx.set_profile(args.profile)
+    ctx.set_dual(args.dual)
     if args.workload == "batch":
         # --target-m is the number of complexes; one segmented pass each step
         col_off, colptr, rows = (torch.from_numpy(x).to(dev) for x in bm[:3])
@@ -66,7 +68,7 @@ def main():
                                        nnz, d_low.data_ptr(), None, args.algo) for _ in range(args.steps)]
         print(json.dumps({"workload": "batch", "count": len(bm[0]) - 1, "m": m, "nnz": nnz,
                           "device_ms": [o["device_ms"] for o in out], "sweeps": out[-1]["sweeps"],
-                          "additions": out[-1]["additions"], **_prof(ctx, args)}))
+                          "additions": out[-1]["additions"], "dual": out[-1]["dual"], **_prof(ctx, args)}))
         ctx.close()
         return
     d_colptr = torch.from_numpy(bm.colptr).to(dev)
@@ -79,7 +81,7 @@ def main():
                                      args.algo))
     print(json.dumps({"workload": args.workload, "m": bm.m, "nnz": bm.nnz, "algo": args.algo,
                       "device_ms": [o["device_ms"] for o in out], "sweeps": out[-1]["sweeps"],
-                      "additions": out[-1]["additions"], "pivots": int((d_low.cpu().numpy() >= 0).sum()),
+                      "additions": out[-1]["additions"], "dual": out[-1]["dual"], "pivots": int((d_low.cpu().numpy() >= 0).sum()),
                       **_prof(ctx, args)}))
     ctx.close()
 

@@ -75,3 +75,20 @@ def small_cases():
     out["simplex_6d"] = simplex_skeleton(7, seed=11)          # columns of up to 7 rows
     out["skeleton_4d_of_9"] = simplex_skeleton(9, seed=12, max_dim=4)
     return out
+
+
+def anti_transpose(bm):
+    """D' with entry (m-1-j, m-1-i) for every entry (i, j) of D, rows
+    ascending (column m-1-i of D' lists the columns of D holding row i)."""
+    m = bm.m
+    cols = [[] for _ in range(m)]
+    for j in range(m - 1, -1, -1):
+        for i in bm.column(j):
+            cols[m - 1 - int(i)].append(m - 1 - j)
+    return BoundaryMatrix.from_columns(cols)
+
+
+def mixed_buckets():
+    """A matrix whose columns of three rows take them from two buckets (the
+    triangle's edges, and three vertices), so its buckets are not graded."""
+    return BoundaryMatrix.from_columns([[], [], [], [0, 1], [0, 2], [1, 2], [3, 4, 5], [0, 1, 2]])

@@ -1,0 +1,144 @@
+"""pms on the anti-transpose (OPH_DUAL_*): every output equal to the oracle's
+twist on D, the automatic choice per matrix, the fall-back to D for inputs
+whose buckets are not graded, batches, and the drop-in call."""
+import numpy as np
+import pytest
+
+import oracle
+from openph_gb300 import complexes as cx
+from openph_gb300.api import Context
+
+from cases import mixed_buckets, random_complex, simplex_skeleton, small_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = small_cases()
+
+
+@pytest.fixture(scope="module")
+def dctx(cuda_lib):
+    c = Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("mode", ["always", "never", "auto"])
+def test_small_cases(dctx, name, mode):
+    bm = CASES[name]
+    dctx.set_dual(mode)
+    low, ess, arglow, info = dctx.reduce(bm, "pms", with_arglow=True)
+    dctx.set_dual("auto")
+    want, want_ess, _ = oracle.twist(bm)
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+    want_arg = np.full(bm.m, -1, np.int32)
+    j = np.nonzero(want >= 0)[0]
+    want_arg[want[j]] = j
+    np.testing.assert_array_equal(arglow, want_arg)
+    if mode != "auto":  # every small case is graded
+        assert info["dual"] == (1 if mode == "always" else 0)
+
+
+@pytest.mark.parametrize("seed", range(3))
+def test_larger_complexes_both_ways(dctx, seed):
+    mats = [cx.rips_cube(40 + 5 * seed, seed=seed), cx.rips_mixed(45, seed=seed),
+            cx.lower_star_image(40, 56, seed=seed, sigma=2.0), random_complex(30, 0.4, 0.5, seed=300 + seed),
+            simplex_skeleton(8, seed=40 + seed, max_dim=4)]
+    for bm in mats:
+        want, want_ess, _ = oracle.twist(bm)
+        for mode in ("always", "never"):
+            dctx.set_dual(mode)
+            low, ess, info = dctx.reduce(bm, "pms")
+            np.testing.assert_array_equal(low, want, err_msg=f"{mode} m={bm.m}")
+            np.testing.assert_array_equal(ess, want_ess, err_msg=f"{mode} m={bm.m}")
+            assert info["dual"] == (1 if mode == "always" else 0)
+    dctx.set_dual("auto")
+
+
+def test_auto_choice(dctx):
+    """Rips complexes of 2^17 columns or more (top bucket >= 8x the bottom
+    one) go to D'; a smaller one, and a lower-star image (triangles about
+    twice the vertices) of any size, stay on D."""
+    dctx.set_dual("auto")
+    _, _, info = dctx.reduce(cx.rips_cube(100, seed=1), "pms")  # 166,750 columns
+    assert info["dual"] == 1
+    _, _, info = dctx.reduce(cx.rips_cube(30, seed=1), "pms")
+    assert info["dual"] == 0
+    _, _, info = dctx.reduce(cx.lower_star_image(256, 256, seed=2), "pms")
+    assert info["dual"] == 0
+    _, _, info = dctx.reduce(CASES["empty5"], "pms")
+    assert info["dual"] == 0
+
+
+def test_ungraded_input_stays_on_d(dctx):
+    """Columns of three rows from two buckets: 'always' falls back to D and
+    gives the same result as 'never'."""
+    bm = mixed_buckets()
+    dctx.set_dual("never")
+    low_n, ess_n, info_n = dctx.reduce(bm, "pms")
+    dctx.set_dual("always")
+    low_a, ess_a, info_a = dctx.reduce(bm, "pms")
+    dctx.set_dual("auto")
+    assert info_a["dual"] == 0 and info_n["dual"] == 0
+    np.testing.assert_array_equal(low_a, low_n)
+    np.testing.assert_array_equal(ess_a, ess_n)
+
+
+def test_dual_does_few_additions_on_rips(dctx):
+    bm = cx.rips_torus(400, 200_000, seed=5)
+    want, want_ess, st = oracle.twist(bm)
+    dctx.set_dual("auto")
+    low, ess, info = dctx.reduce(bm, "pms")
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+    assert info["dual"] == 1
+    assert info["additions"] * 100 < st["additions"]
+
+
+@pytest.mark.parametrize("mode", ["always", "auto", "never"])
+def test_batch(dctx, mode):
+    from cases import empty_columns, triangle
+    from openph_gb300.complexes import BoundaryMatrix
+    mats = [cx.rips_mixed(n, seed=60 + n) for n in (9, 21, 14)] + [
+        BoundaryMatrix.from_columns([]), triangle(), empty_columns(3), cx.lower_star_image(9, 7, seed=5),
+        simplex_skeleton(6, seed=2)]
+    dctx.set_dual(mode)
+    lows, esss, info = dctx.reduce_batch(mats, "pms")
+    dctx.set_dual("auto")
+    for bm, low, ess in zip(mats, lows, esss):
+        if bm.m == 0:
+            continue
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_drop_in_call_without_trackers(cuda_lib):
+    """openph() with no tracker outputs takes D' on a large Rips complex
+    (1-based COO in, 1-based lows out); with trackers it reduces D."""
+    from openph_gb300.api import ph
+    bm = cx.rips_cube(100, seed=8)
+    want, want_ess, _ = oracle.twist(bm)
+    r, c = bm.to_coo1()
+    low, ess, *_ = ph("pms", r, c, bm.m, 0)
+    np.testing.assert_array_equal(low, want + 1)
+    np.testing.assert_array_equal(ess, want_ess)
+    low, ess, linf, *_ , it = ph("pms", r, c, bm.m, 0, (want + 1).astype(np.int32))
+    np.testing.assert_array_equal(low, want + 1)
+    assert linf[int(it[0]) - 1] == 0.0
+
+
+def test_rips_torus_1m_device_input(dctx):
+    """The torus family through oph_reduce_device, D' chosen automatically."""
+    import torch
+    bm = cx.rips_torus(400, 1_000_000, seed=2)
+    want, want_ess, _ = oracle.twist(bm)
+    cp = torch.as_tensor(bm.colptr, device="cuda")
+    rw = torch.as_tensor(bm.rows, device="cuda")
+    low = torch.empty(bm.m, dtype=torch.int32, device="cuda")
+    ess = torch.empty(bm.m, dtype=torch.int32, device="cuda")
+    info = dctx.reduce_device(bm.m, cp.data_ptr(), rw.data_ptr(), low.data_ptr(), ess.data_ptr())
+    assert info["dual"] == 1
+    np.testing.assert_array_equal(low.cpu().numpy(), want)
+    np.testing.assert_array_equal(ess.cpu().numpy(), want_ess)

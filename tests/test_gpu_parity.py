@@ -106,6 +106,7 @@ def test_sweep_cap_times_out(cuda_lib):
     from openph_gb300.api import Context, OPH_ERR_TIMEOUT
     bm = cx.rips_cube(40, seed=1)
     with Context(0) as c:
+        c.set_dual("never")  # D itself needs several sweeps
         c.set_limits(max_sweeps=1)
         with pytest.raises(OphError) as e:
             c.reduce(bm, "pms")
@@ -165,14 +166,26 @@ def test_lower_star_512_full_size(ctx, algo):
     np.testing.assert_array_equal(ess, want_ess)
 
 
-def test_rips_torus_1m(ctx):
-    """A 1M-column torus Rips complex (the 5M configuration's family)."""
+@pytest.fixture(scope="module")
+def torus_1m():
     bm = cx.rips_torus(400, 1_000_000, seed=2)
     want, want_ess, _ = oracle.twist(bm)
-    low, ess, info = ctx.reduce(bm, "pms")
+    return bm, want, want_ess
+
+
+@pytest.mark.parametrize("mode", ["never", "auto"])
+def test_rips_torus_1m(cuda_lib, torus_1m, mode):
+    """A 1M-column torus Rips complex (the 5M configuration's family), on D
+    and on its anti-transpose."""
+    from openph_gb300.api import Context
+    bm, want, want_ess = torus_1m
+    with Context(0) as c:
+        c.set_dual(mode)
+        low, ess, info = c.reduce(bm, "pms")
     np.testing.assert_array_equal(low, want)
     np.testing.assert_array_equal(ess, want_ess)
     assert info["regrows"] == 0
+    assert info["dual"] == (0 if mode == "never" else 1)
 
 
 @pytest.mark.parametrize("lanes,cap", [(8, 128), (4, 128), (8, 64), (8, 256), (16, 128), (16, 256), (32, 128)])
@@ -213,6 +226,7 @@ def test_long_chains_every_tier0_candidate(cuda_lib, torus_200k, lanes, cap):
     from openph_gb300.api import Context
     bm, want, want_ess, _ = torus_200k
     with Context(0) as c:
+        c.set_dual("never")  # the chains of D's triangle columns
         c.set_tier0(lanes, cap)
         low, ess, _ = c.reduce(bm, "pms")
     np.testing.assert_array_equal(low, want)
@@ -227,6 +241,7 @@ def test_slot_counters_match_twist(cuda_lib, torus_200k):
     from openph_gb300.api import Context
     bm, want, want_ess, st = torus_200k
     with Context(0) as c:
+        c.set_dual("never")  # the additions twist makes are those of D
         c.set_profile(True, slots=True)
         low, ess, info = c.reduce(bm, "pms")
         prof = c.last_profile()
