@@ -1,15 +1,17 @@
 #!/usr/bin/env python
-"""Benchmark: plain pms on one Rips complex of a noisy torus (~5M columns).
+"""Benchmark: pms on one Rips complex of a noisy torus (~5M columns).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-One step = one full pms reduction of the complex (set-up, sweeps, outputs).
+One step = one full pms reduction of the complex (set-up, sweeps, outputs),
+by the library's own choice of matrix (the anti-transpose, for this complex).
 ``value`` is columns/s with the boundary matrix already resident in HBM;
 ``e2e`` is the same metric through the drop-in ``openph()`` C call with host
 (pinned) COO input and host outputs, copies included.  The roofline is the
-Phase II narrow-tier kernel (the additions), timed with CUDA events on the
-library's stream during the timed steps.  ``cpu_baseline`` is the fixed-slot
-port of the reference's CPU twist on a bounded prefix of the same reduction.
+Phase II kernel that takes the most time, timed with CUDA events on the
+library's stream in a second pass of the same steps.  ``cpu_baseline`` is the
+fixed-slot port of the reference's CPU twist on a bounded prefix of the same
+reduction.
 
 ``--impl reference`` times the reference's CPU twist (its port; the
 reference's own build needs its source tree) on the host cores, on the same
@@ -287,7 +289,8 @@ def run_ours(args, ws, rank, local):
     # library's stream (kernels launched one by one): the per-phase split,
     # the Phase II launch durations for the roofline and the launch count
     ctx.set_profile(True)
-    narrow_ms, wide_ms, p1_ms, launches, p2_launches = 0.0, 0.0, 0.0, 0, 0
+    narrow_ms, p1_ms, setup_ms, launches, p2_launches = 0.0, 0.0, 0.0, 0, 0
+    tier_ms = [0.0, 0.0, 0.0]
     ev_prof = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for k in range(args.steps):
         flush.fill_(k)
@@ -297,18 +300,18 @@ def run_ours(args, ws, rank, local):
         ev_prof[k][1].record(stream)
         prof = ctx.last_profile()
         narrow_ms += prof["phase2_narrow_ms"]
-        wide_ms += prof["phase2_wide_ms"]
+        tier_ms = [x + y for x, y in zip(tier_ms, prof["tier_ms"])]
         p1_ms += prof["phase1_ms"]
+        setup_ms += prof["setup_ms"]
         launches += prof["kernel_launches"]
         p2_launches += prof["phase2_launches"]
     torch.cuda.synchronize()
     profiled_ms = sum(a.elapsed_time(b) for a, b in ev_prof) / args.steps
-    # the exact |P| + |T| + |T xor P| of every tier-0 addition, from one more
-    # (untimed) reduction of the same matrix with slot tracking on
+    # the exact |P| + |T| + |T xor P| of every addition per tier, from one
+    # more (untimed) reduction of the same matrix with slot tracking on
     ctx.set_profile(True, slots=True)
     step()
-    prof = ctx.last_profile()
-    tier0_slots = prof["tier_slots"][0]
+    slot_prof = ctx.last_profile()
     ctx.set_profile(False)
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_s = max_over_ranks(sum(step_ms) / 1e3, dist, device)
@@ -362,17 +365,25 @@ def run_ours(args, ws, rank, local):
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
     ab = algorithmic_bytes(bm, st)
-    # dominant kernels: the Phase II narrow tiers (the scalar tier and tier 0,
-    # launched back to back and timed together each sweep).  Their
-    # algorithmic bytes are the per-addition figure 4 (|P| + |T| + |T xor P|)
-    # summed over the additions they performed (counted on the device), per
-    # sweep; divided by their mean time per sweep (CUDA events around the
-    # pair on the library's stream)
-    per_red_narrow_s = narrow_ms / 1e3 / args.steps
-    t0_bytes = 4 * tier0_slots
-    achieved = t0_bytes / per_red_narrow_s / 1e9 if per_red_narrow_s > 0 else None
-    traffic = load_traffic()
+    # the dominant Phase II kernel (one launch per sweep, CUDA events around
+    # each tier on the library's stream): its algorithmic bytes are the
+    # per-addition figure 4 (|P| + |T| + |T xor P|) summed over the additions
+    # it performed (counted on the device), per launch, over its mean launch
+    # time.  On the anti-transpose that is tier 3's bitmap kernel.
+    comps = {"narrow": (narrow_ms, slot_prof["tier_slots"][0],
+                        "k_p2_scalar + k_p2_tier<8,128,256> (scalar tier and tier 0, a pair per sweep)"),
+             "tier1": (tier_ms[0], slot_prof["tier_slots"][1], "k_p2_tier1<32,512,256> (tier 1)"),
+             "tier2": (tier_ms[1], slot_prof["tier_slots"][2], "k_p2_block<8192,256> (tier 2)"),
+             "tier3": (tier_ms[2], slot_prof["tier_slots"][3], "k_p2_bitmap<256> (tier 3, bitmap columns)")}
+    dom = max(comps, key=lambda k: comps[k][0])
+    dom_ms, dom_slots, dom_name = comps[dom]
+    per_red_dom_s = dom_ms / 1e3 / args.steps
     launches_per_red = p2_launches / args.steps
+    dom_bytes = 4 * dom_slots
+    achieved = dom_bytes / per_red_dom_s / 1e9 if per_red_dom_s > 0 else None
+    traffic = load_traffic()
+    if traffic and traffic.get("component") != dom:
+        traffic = None
     line = {
         "metric": "cols/s", "value": ws * m * args.steps / total_s, "unit": "cols/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps,
@@ -384,23 +395,26 @@ def run_ours(args, ws, rank, local):
         "complexes_per_s": ws * args.steps / total_s,
         "e2e": {"value": ws * m * args.steps / e2e_s, "unit": "cols/s", "h2d_bytes_per_step": 8 * nnz,
                 "d2h_bytes_per_step": 8 * m, "ms_per_step": 1e3 * e2e_s / args.steps, "api": "openph() C ABI"},
-        "roofline": {"bound": "hbm",
-                     "kernel": "Phase II narrow tiers, one launch each per sweep: k_p2_scalar (a column per lane) "
-                               "then k_p2_tier<8,128,256> (8 lanes per column)",
+        "roofline": {"bound": "hbm", "kernel": dom_name,
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak if achieved else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if peaks else "fallback",
-                     "algorithmic_bytes_per_launch": t0_bytes / launches_per_red if launches_per_red else None,
-                     "algorithmic_bytes_per_reduction_all_tiers_twist": ab["additions"],
-                     "mean_launch_ms": narrow_ms / max(1, p2_launches),
+                     "algorithmic_bytes_per_launch": dom_bytes / launches_per_red if launches_per_red else None,
+                     "mean_launch_ms": dom_ms / max(1, p2_launches),
+                     "launches_per_reduction": launches_per_red,
+                     "twist_on_d_algorithmic_bytes_per_reduction": ab["additions"],
                      "traffic": (traffic or {}).get("bytes_per_launch"),
                      "traffic_source": (traffic or {}).get("source")},
-        "phases_ms_per_step": {"phase2_narrow": narrow_ms / args.steps, "phase2_wide_global": wide_ms / args.steps,
-                               "phase1": p1_ms / args.steps, "total_launched_one_by_one": profiled_ms,
+        "phases_ms_per_step": {"setup_and_transpose": setup_ms / args.steps, "phase1": p1_ms / args.steps,
+                               "phase2_narrow": narrow_ms / args.steps, "tier1": tier_ms[0] / args.steps,
+                               "tier2": tier_ms[1] / args.steps, "tier3": tier_ms[2] / args.steps,
+                               "total_launched_one_by_one": profiled_ms,
                                "note": "a second pass of the same steps with events around every phase "
                                        "(no CUDA graph); the headline pass replays the captured sweeps"},
+        "matrix_reduced": "anti-transpose D' (OPH_DUAL_AUTO)" if infos[-1]["dual"] else "D",
         "sweeps": infos[-1]["sweeps"], "device_additions": infos[-1]["additions"],
-        "twist_additions": st["additions"],
+        "device_slots_per_tier": slot_prof["tier_slots"],
+        "twist_additions_on_d": st["additions"],
         "cpu_baseline": {"value": cpu_rate, "unit": "cols/s", "cores": 1, "kind": "port",
                          "sample": f"fixed-slot twist port, first {cpu_st['columns_done']} columns of the twist "
                                    f"order of the same matrix ({cpu_st['seconds']:.1f} s)"},
@@ -599,6 +613,7 @@ def run_batch(args, ws, rank, local):
                     "api": "oph_reduce_batch C ABI", "equal_to_device_run": e2e_equal},
             "cpu_baseline": cpu_batch_sample(col_off, colptr, rows, CPU_SAMPLE_SECONDS),
             "cols_per_s": ws * total_m * args.steps / batch_s,
+            "matrix_reduced": "anti-transpose D' (OPH_DUAL_AUTO)" if info["dual"] else "D",
             "sweeps": info["sweeps"], "device_additions": info["additions"], "regrows": info["regrows"],
             "pool_bytes": info["pool_bytes"],
             "parity": {"batched_equals_one_at_a_time": mismatches == 0, "mismatched_instances": mismatches,

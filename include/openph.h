@@ -200,6 +200,8 @@ typedef struct {
     int64_t tier_additions[4];/* column additions done by each Phase II tier       */
     int64_t tier_slots[4];    /* sum of |P| + |T| + |T xor P| per tier (tiers 0-1:
                                  only with OPH_PROFILE_SLOTS)                      */
+    float tier_ms[3];         /* tiers 1, 2 and 3 apart (their sum is
+                                 phase2_wide_ms)                                   */
 } oph_profile;
 
 #define OPH_PROFILE_EVENTS 1  /* per-phase CUDA-event timing                     */

@@ -60,12 +60,13 @@ class ServerCounters(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("phase2_narrow_ms", C.c_float), ("phase2_wide_ms", C.c_float), ("phase1_ms", C.c_float),
                 ("setup_ms", C.c_float), ("phase2_launches", C.c_int32), ("kernel_launches", C.c_int32),
-                ("tier_additions", C.c_int64 * 4), ("tier_slots", C.c_int64 * 4)]
+                ("tier_additions", C.c_int64 * 4), ("tier_slots", C.c_int64 * 4), ("tier_ms", C.c_float * 3)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["tier_additions"] = list(self.tier_additions)
         d["tier_slots"] = list(self.tier_slots)
+        d["tier_ms"] = list(self.tier_ms)
         return d
 
 

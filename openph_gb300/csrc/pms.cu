@@ -1715,7 +1715,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     int sweeps_launched = 0;
     int batch = trace ? 1 : 2;
     DevStatus hs{};
-    float p2_ms = 0, p2w_ms = 0, p1_ms = 0;
+    float p2_ms = 0, p2w_ms = 0, p1_ms = 0, wt_ms[3] = {0, 0, 0};
     int p2_launches = 0, regrows = 0;
     for (;;) {
         const int nb = std::min(batch, max_sweeps - sweeps_launched);
@@ -1745,6 +1745,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
                 p1_ms += t[0];
                 p2_ms += t[1];
                 p2w_ms += t[2] + t[3] + t[4];
+                for (int q = 0; q < 3; q++) wt_ms[q] += t[2 + q];
                 if (tr && b < worked) tr->sweep_ms.push_back(t[0] + t[1] + t[2] + t[3] + t[4]);
                 if (trace && b < worked)
                     fprintf(stderr, "sweep %d: unresolved %d queued t0=%d (to tier 0: %d) t1=%d t2=%d t3=%d | adds "
@@ -1810,6 +1811,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
         cudaEventElapsedTime(&p0, ctx->ev[0], ctx->pev[6 * MAX_BATCH]);
         ctx->prof.phase2_narrow_ms = p2_ms;
         ctx->prof.phase2_wide_ms = p2w_ms;
+        for (int q = 0; q < 3; q++) ctx->prof.tier_ms[q] = wt_ms[q];
         ctx->prof.phase1_ms = p1_ms;
         ctx->prof.setup_ms += p0;
         ctx->prof.phase2_launches = p2_launches;
