@@ -220,6 +220,7 @@ int dual_build(Context *ctx, const Work &w, Work &wd) {
     ctx->launches += 3 + (bits + 7) / 8;
     OPH_CUDA_TRY(cudaGetLastError());
     wd.rows = dv.Current();
+    wd.entry_col = dk.Current();
     return OPH_OK;
 }
 

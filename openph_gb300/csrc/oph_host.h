@@ -49,6 +49,7 @@ struct Work {
     int *pool = nullptr;              // column store
     DevStatus *st = nullptr;
     bool ascending = false;           // pms: buckets in ascending order (the anti-transpose)
+    const uint32_t *entry_col = nullptr;  // nnz: column of each entry, when known (the anti-transpose)
 };
 
 struct Context;

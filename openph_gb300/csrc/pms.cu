@@ -1178,6 +1178,7 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
 // cleared, once, when the chain ends.  A row below w0 (a window smaller than
 // the matrix) sends the column to the merge path instead.
 constexpr int64_t BM_MAX_WORDS = 1 << 18;
+constexpr int BM_BLOCK = 1024;
 
 template <class Op>
 __device__ __forceinline__ int block_reduce(int v, int *red, Op op) {
@@ -1208,15 +1209,18 @@ __device__ int bitmap_top(const uint32_t *bm, int wl, int *red) {
     return -1;
 }
 
-// Rows of words [0, top] in ascending order into dst (when not null), the
-// words zeroed.  Returns the number of rows.
-__device__ int bitmap_extract(uint32_t *bm, int top, int w0, int *dst, int *red) {
+// Rows of words [lo, top] in ascending order into dst (when not null), the
+// words zeroed; every set bit lies in that range.  Four words per thread
+// (lo rounded down to a multiple of 4, the per-CTA scratch a multiple of 4
+// words long).  Returns the number of rows.
+__device__ int bitmap_extract(uint32_t *bm, int lo, int top, int w0, int *dst, int *red) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int out = 0;
-    for (int base = 0; base <= top; base += (int)blockDim.x) {
-        const int w = base + (int)threadIdx.x;
-        uint32_t v = w <= top ? __ldcg(bm + w) : 0u;
-        const int c = __popc(v);
+    for (int base = lo & ~3; base <= top; base += 4 * (int)blockDim.x) {
+        const int w = base + 4 * (int)threadIdx.x;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (w <= top) v = __ldcg(reinterpret_cast<const uint4 *>(bm + w));
+        const int c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
         int incl = c;
         for (int o = 1; o < 32; o <<= 1) {
             const int u = __shfl_up_sync(0xffffffffu, incl, o);
@@ -1230,14 +1234,14 @@ __device__ int bitmap_extract(uint32_t *bm, int top, int w0, int *dst, int *red)
             total += red[q];
         }
         __syncthreads();
-        if (v) {
+        if (c) {
             int pos = out + before + incl - c;
-            if (dst)
-                while (v) {
-                    dst[pos++] = w0 + w * 32 + (__ffs(v) - 1);
-                    v &= v - 1;
-                }
-            bm[w] = 0u;
+            if (dst) {
+                const uint32_t words[4] = {v.x, v.y, v.z, v.w};
+                for (int q = 0; q < 4; q++)
+                    for (uint32_t b = words[q]; b; b &= b - 1) dst[pos++] = w0 + (w + q) * 32 + (__ffs(b) - 1);
+            }
+            *reinterpret_cast<uint4 *>(bm + w) = make_uint4(0u, 0u, 0u, 0u);
         }
         out += total;
     }
@@ -1266,6 +1270,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
     // the window's first row: a multiple of 32 with lj - w0 < nbits
     const int w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 31) & ~31ll) : 0;
     if (n > 0 && T[0] < w0) return true;
+    int lo_row = n > 0 ? T[0] : lj;  // no set bit below it
     for (int k = tid; k < n; k += blockDim.x) {
         const int r = T[k] - w0;
         atomicOr(bm + (r >> 5), 1u << (r & 31));
@@ -1289,6 +1294,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
             fell_back = true;
             break;
         }
+        lo_row = min(lo_row, P[0]);
         int d = 0;
         for (int k = tid; k < np; k += blockDim.x) {
             const int r = P[k] - w0;
@@ -1327,7 +1333,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
         dst = s_off;
     }
     const int top = n > 0 ? (lj - w0) >> 5 : -1;
-    bitmap_extract(bm, top, w0, stored ? a.pool + dst + SEG_HDR : nullptr, s_red);
+    bitmap_extract(bm, (lo_row - w0) >> 5, top, w0, stored ? a.pool + dst + SEG_HDR : nullptr, s_red);
     if (!stored) return false;
     if (tid == 0) {
         a.pool[dst] = n;
@@ -1398,7 +1404,6 @@ constexpr bool T0_LAZY = (OPH_LAZY & 1) != 0, T1_LAZY = (OPH_LAZY & 2) != 0;
 #define OPH_BLOCK_THREADS 256
 #endif
 constexpr int T2_CAP = 8192, T2_BLOCK = OPH_BLOCK_THREADS;
-constexpr int T3_BLOCK = OPH_BLOCK_THREADS;
 
 // Occupancy-filling grid for a kernel with `smem` bytes of dynamic shared
 // memory (attribute set once per device).
@@ -1472,7 +1477,7 @@ int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     g->g0 = t0_grid_of(ctx, g->v0, &g->s0);
     g->g1 = fill_grid(ctx, k_p2_tier1<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY>, T1_BLOCK, g->s1, done1);
     g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
-    g->g3 = ctx->sm_count * 2;
+    g->g3 = ctx->sm_count;  // tier 3: one 1024-thread CTA per SM
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
     g->t = (int)std::max<int64_t>(1, ntiles);
     if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0 || g->gs < 0) {
@@ -1581,7 +1586,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
     if (ev) cudaEventRecord(ev[3], s);
     k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
     if (ev) cudaEventRecord(ev[4], s);
-    k_p2_bitmap<T3_BLOCK><<<g.g3, T3_BLOCK, 0, s>>>(a, 3);
+    k_p2_bitmap<BM_BLOCK><<<g.g3, BM_BLOCK, 0, s>>>(a, 3);
     k_count_sweep<<<1, 1, 0, s>>>(a.st);
     if (ev) cudaEventRecord(ev[5], s);
 }
@@ -1670,7 +1675,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     if (rc) return rc;
     // tier 3's bitmaps: a window of the whole matrix up to 2^23 rows per CTA,
     // zeroed here (each column leaves its words zeroed)
-    a.bm_words = std::min<int64_t>((m + 32) / 32, BM_MAX_WORDS);
+    a.bm_words = std::min<int64_t>(((m + 32) / 32 + 3) & ~3ll, BM_MAX_WORDS);
     a.bm = (uint32_t *)ctx_alloc(ctx, S_BITMAP, sizeof(uint32_t) * (size_t)a.bm_words * g.g3);
     if (!a.bm) return OPH_ERR_OOM;
     OPH_CUDA_TRY(cudaMemsetAsync(a.bm, 0, sizeof(uint32_t) * (size_t)a.bm_words * g.g3, s));
