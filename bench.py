@@ -374,7 +374,7 @@ def run_ours(args, ws, rank, local):
                         "k_p2_scalar + k_p2_tier<8,128,256> (scalar tier and tier 0, a pair per sweep)"),
              "tier1": (tier_ms[0], slot_prof["tier_slots"][1], "k_p2_tier1<32,512,256> (tier 1)"),
              "tier2": (tier_ms[1], slot_prof["tier_slots"][2], "k_p2_block<8192,256> (tier 2)"),
-             "tier3": (tier_ms[2], slot_prof["tier_slots"][3], "k_p2_bitmap<256> (tier 3, bitmap columns)")}
+             "tier3": (tier_ms[2], slot_prof["tier_slots"][3], "k_p2_bitmap<1024> (tier 3, bitmap columns)")}
     dom = max(comps, key=lambda k: comps[k][0])
     dom_ms, dom_slots, dom_name = comps[dom]
     per_red_dom_s = dom_ms / 1e3 / args.steps

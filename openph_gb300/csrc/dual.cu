@@ -41,7 +41,8 @@ __device__ __forceinline__ int bucket_of(int64_t n) { return (int)(n - 1 > 126 ?
 // and the structural checks (colptr monotone within [0, nnz], rows strictly
 // ascending and < m: *bad).
 __global__ void k_dual_grade(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                             int64_t nnz, unsigned long long *count, int *tab, int *mixed, int *bad) {
+                             int64_t nnz, const int8_t *__restrict__ bucket, unsigned long long *count, int *tab,
+                             int *mixed, int *bad) {
     __shared__ unsigned long long s_count[MAXC];
     __shared__ int s_tab[MAXC];
     __shared__ int s_flags[2];
@@ -71,7 +72,7 @@ __global__ void k_dual_grade(const int64_t *__restrict__ colptr, const int32_t *
                 break;
             }
             prev = r;
-            const int br = bucket_of(colptr[r + 1] - colptr[r]);
+            const int br = bucket[r];
             if (k == lo) rb = br;
             else if (br != rb) s_flags[0] = 1;
         }
@@ -94,6 +95,24 @@ __global__ void k_dual_grade(const int64_t *__restrict__ colptr, const int32_t *
         if (s_flags[1]) atomicExch(bad, 1);
     }
 }
+
+// Each column's bucket, one byte, for k_dual_grade's row lookups (a column
+// whose colptr is out of bounds gets any value: k_dual_grade rejects it).
+__global__ void k_dual_buckets(const int64_t *__restrict__ colptr, int64_t m, int8_t *__restrict__ bucket) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
+        bucket[j] = (int8_t)bucket_of(colptr[j + 1] - colptr[j]);
+}
+
+// left of D' without atomics: row m-1-j of D' first appears in column
+// m-1-low_D(j) (the largest row of D's column j), for every nonempty j.
+__global__ void k_dual_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                            PivRec *__restrict__ rec) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = colptr[j + 1];
+        if (b > colptr[j]) rec[m - 1 - j].left = (int)(m - 1 - rows[b - 1]);
+    }
+}
+
 
 // Sort keys of D': entry k of D (row r, column j) becomes key m-1-r (its
 // column in D'), value m-1-j (its row), written at nnz-1-k so that a stable
@@ -147,6 +166,11 @@ static int grid_of(Context *ctx, int64_t n) {
     return (int)std::max<int64_t>(1, std::min(g, cap));
 }
 
+void dual_left(Context *ctx, const Work &wd) {
+    k_dual_left<<<grid_of(ctx, wd.m), 256, 0, ctx->stream>>>(wd.src_colptr, wd.src_rows, wd.m, wd.rec);
+    ctx->launches++;
+}
+
 int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input) {
     *use = false;
     *bad_input = false;
@@ -162,9 +186,11 @@ int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_inpu
     Grade init{};
     for (int b = 0; b < MAXC; b++) init.tab[b] = TAB_NONE;
     OPH_CUDA_TRY(cudaMemcpyAsync(d, &init, sizeof(Grade), cudaMemcpyHostToDevice, s));
-    k_dual_grade<<<grid_of(ctx, w.m), 256, 0, s>>>(w.colptr, w.rows, w.m, w.nnz, d->count, d->tab, &d->mixed,
-                                                    &d->bad);
-    ctx->launches++;
+    // the buckets go through w.dim, which the set-up rewrites afterwards
+    k_dual_buckets<<<grid_of(ctx, w.m), 256, 0, s>>>(w.colptr, w.m, w.dim);
+    k_dual_grade<<<grid_of(ctx, w.m), 256, 0, s>>>(w.colptr, w.rows, w.m, w.nnz, w.dim, d->count, d->tab,
+                                                    &d->mixed, &d->bad);
+    ctx->launches += 2;
     OPH_CUDA_TRY(cudaGetLastError());
     Grade g;
     OPH_CUDA_TRY(cudaMemcpyAsync(&g, d, sizeof(Grade), cudaMemcpyDeviceToHost, s));
@@ -201,6 +227,8 @@ int dual_build(Context *ctx, const Work &w, Work &wd) {
     wd = w;
     wd.colptr = colptr;
     wd.ascending = true;
+    wd.src_colptr = w.colptr;
+    wd.src_rows = w.rows;
     if (nnz == 0) {
         OPH_CUDA_TRY(cudaMemsetAsync(colptr, 0, sizeof(int64_t) * (m + 1), s));
         wd.rows = v0;

@@ -50,6 +50,8 @@ struct Work {
     DevStatus *st = nullptr;
     bool ascending = false;           // pms: buckets in ascending order (the anti-transpose)
     const uint32_t *entry_col = nullptr;  // nnz: column of each entry, when known (the anti-transpose)
+    const int64_t *src_colptr = nullptr;  // the anti-transpose: D's CSC, from which left[] follows
+    const int32_t *src_rows = nullptr;
 };
 
 struct Context;
@@ -78,6 +80,7 @@ constexpr int64_t DUAL_MIN_M = 1 << 17;
 int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input);
 int dual_build(Context *ctx, const Work &w, Work &wd);
 void dual_dims(Context *ctx, const Work &w, Work &wd);
+void dual_left(Context *ctx, const Work &wd);
 int dual_lows(Context *ctx, const Work &wd, int32_t **low);
 
 // capi.cu

@@ -172,7 +172,8 @@ int setup_store(Context *ctx, Work &w, bool need_beta) {
                                                                         w.dim);
         if (w.nnz > 0)
             k_setup_entries<<<grid_for(ctx, w.nnz, 256), 256, 0, ctx->stream>>>(
-                w.colptr, w.rows, w.entry_col, w.nnz, w.pool, need_beta ? w.rec : nullptr);
+                w.colptr, w.rows, w.entry_col, w.nnz, w.pool, need_beta && !w.src_colptr ? w.rec : nullptr);
+        if (need_beta && w.src_colptr) dual_left(ctx, w);
     } else {
         k_setup_columns<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.pool, w.seg, w.low,
                                                                         w.dim, w.st);
