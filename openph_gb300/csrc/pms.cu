@@ -1703,7 +1703,9 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     OPH_CUDA_TRY(cudaGetLastError());
 
     // per-phase events: 6 per sweep, reused batch after batch
-    constexpr int MAX_BATCH = 16;
+    // sweeps launched between two reads of the status (doubling from 2): a
+    // batch that overshoots convergence launches sweeps that return at once
+    constexpr int MAX_BATCH = 4;
     const int nev = 6 * MAX_BATCH + 1;
     if ((ctx->profile || ctx->track || getenv("OPH_TRACE")) && ctx->pev_n < nev) {
         ctx->pev = (cudaEvent_t *)realloc(ctx->pev, sizeof(cudaEvent_t) * nev);
