@@ -216,6 +216,15 @@ def run_reference(args, ws, rank):
     return 0
 
 
+# What bounds each Phase II kernel, from its ncu captures (profiles/).
+ROOFLINE_NOTES = {
+    "tier3": "latency-bound: chains of dependent additions on a few long columns of the anti-transpose "
+             "(ncu: 0.4% SM throughput, DRAM idle, the bitmaps in L2); the merge-equivalent bytes are "
+             "what a merge would move, ~58x the kernel's DRAM traffic",
+    "narrow": "instruction-issue-bound (ncu: 60-89% issue active, DRAM 1-2%); T stays on chip per chain",
+}
+
+
 def load_traffic():
     p = ROOT / "profiles" / "traffic.json"
     if p.exists():
@@ -404,7 +413,8 @@ def run_ours(args, ws, rank, local):
                      "launches_per_reduction": launches_per_red,
                      "twist_on_d_algorithmic_bytes_per_reduction": ab["additions"],
                      "traffic": (traffic or {}).get("bytes_per_launch"),
-                     "traffic_source": (traffic or {}).get("source")},
+                     "traffic_source": (traffic or {}).get("source"),
+                     "note": ROOFLINE_NOTES.get(dom)},
         "phases_ms_per_step": {"setup_and_transpose": setup_ms / args.steps, "phase1": p1_ms / args.steps,
                                "phase2_narrow": narrow_ms / args.steps, "tier1": tier_ms[0] / args.steps,
                                "tier2": tier_ms[1] / args.steps, "tier3": tier_ms[2] / args.steps,
