@@ -1180,35 +1180,6 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
 constexpr int64_t BM_MAX_WORDS = 1 << 18;
 constexpr int BM_BLOCK = 1024;
 
-template <class Op>
-__device__ __forceinline__ int block_reduce(int v, int *red, Op op) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    int r = red[0];
-    for (int w = 1; w < nw; w++) r = op(r, red[w]);
-    __syncthreads();
-    return r;
-}
-struct OpSum {
-    __device__ int operator()(int x, int y) const { return x + y; }
-};
-struct OpMax {
-    __device__ int operator()(int x, int y) const { return max(x, y); }
-};
-
-// Highest set bit at or below word wl (window-relative), -1 if none.
-__device__ int bitmap_top(const uint32_t *bm, int wl, int *red) {
-    for (int base = wl; base >= 0; base -= (int)blockDim.x) {
-        const int w = base - (int)threadIdx.x;
-        const uint32_t v = w >= 0 ? __ldcg(bm + w) : 0u;
-        const int best = block_reduce(v ? w : -1, red, OpMax{});
-        if (best >= 0) return best * 32 + 31 - __clz(__ldcg(bm + best));
-    }
-    return -1;
-}
-
 // Rows of words [lo, top] in ascending order into dst (when not null), the
 // words zeroed; every set bit lies in that range.  Four words per thread
 // (lo rounded down to a multiple of 4, the per-CTA scratch a multiple of 4
@@ -1277,46 +1248,71 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
     }
     __syncthreads();
     bool made_pivot = false, fell_back = false;
+    // Two CTA barriers per addition: the whole CTA toggles the pivot's bits
+    // and leaves per-warp counts; warp 0 totals them and finds the next low
+    // (128 words a step, 16-byte loads) for everyone.
+    const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
     for (;;) {
         int np;
-        const int *P;
+        const int *P = nullptr;
         if (rec_complete(h, e)) {
-            np = h.y;
-            if (tid < np) s_small[tid] = rec_entry(e, tid);
-            __syncthreads();
-            P = s_small;
+            np = h.y;  // rows in the record, which every thread holds
         } else {
             const int4 h2 = rec_header(&a.rec[lj], h);
             np = h2.y;
             P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
         }
-        if (P[0] < w0) {  // the pivot reaches below the window
+        const int p0 = P ? P[0] : rec_entry(e, 0);
+        if (p0 < w0) {  // the pivot reaches below the window
             fell_back = true;
             break;
         }
-        lo_row = min(lo_row, P[0]);
+        lo_row = min(lo_row, p0);
         int d = 0;
         for (int k = tid; k < np; k += blockDim.x) {
-            const int r = P[k] - w0;
+            const int r = (P ? P[k] : rec_entry(e, k & 3)) - w0;
             const uint32_t bit = 1u << (r & 31);
             d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
         }
-        d = block_reduce(d, s_red, OpSum{});
-        slots += n + np + (n + d);
-        adds++;
-        n += d;
-        if (n == 0) {
-            lj = -1;
-            break;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0) s_red[wid] = d;
+        __syncthreads();
+        if (wid == 0) {
+            int t = lane < nw ? s_red[lane] : 0;
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            const int nn = n + t;
+            int next = -1;
+            if (nn > 0) {
+                // lj's bit went with the pivot's top: the next low lies below it
+                for (int c0 = ((lj - w0) >> 5) & ~3; c0 >= 0 && next < 0; c0 -= 128) {
+                    const int w = c0 - 4 * lane;
+                    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                    if (w >= 0) v = __ldcg(reinterpret_cast<const uint4 *>(bm + w));
+                    const int hi = v.w ? w + 3 : v.z ? w + 2 : v.y ? w + 1 : v.x ? w : -1;
+                    const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
+                    if (nz) {
+                        const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
+                        const int hw = __shfl_sync(0xffffffffu, hi, src);
+                        next = hw * 32 + 31 - __clz(__ldcg(bm + hw));
+                    }
+                }
+            }
+            if (lane == 0) {
+                s_small[0] = nn;
+                s_small[1] = next;  // -1: zero column (or, never, no bit left)
+            }
         }
-        // lj's bit went with the pivot's top: the next low lies below it
-        const int tb = bitmap_top(bm, (lj - w0) >> 5, s_red);
-        if (tb < 0) {  // cannot happen while n > 0; never index rec[-1]
+        __syncthreads();
+        const int nn = s_small[0], next = s_small[1];
+        slots += n + np + nn;
+        adds++;
+        n = nn;
+        if (next < 0) {
             n = 0;
             lj = -1;
             break;
         }
-        lj = w0 + tb;
+        lj = w0 + next;
         rec_load(&a.rec[lj], h, e);
         mark_clear<false>(a, lj, tid == 0);
         if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
