@@ -20,10 +20,14 @@
 //     written back once, through tiers by column length: a column per lane
 //     (the scalar tier, <= 48 rows), 8 lanes per column (tier 0, <= 128 rows,
 //     three-row pivots added in place), a warp per column (tier 1, <= 512
-//     rows, pending toggles in registers), a CTA per column (tiers 2 and 3,
-//     merge path, shared memory or pool buffers).  A pivot of at most four
-//     rows comes with the one 32-byte record read that also gives the beta
-//     check; the flags every chain would rewrite are written only on change.
+//     rows, pending toggles in registers), a CTA per column (tier 2, merge
+//     path in shared memory; tier 3, the column as a bitmap of its rows).  A
+//     pivot of at most four rows comes with the one 32-byte record read that
+//     also gives the beta check; the flags every chain would rewrite are
+//     written only on change.
+//   * On the anti-transpose (dual.cu) Phase II takes the dimension buckets in
+//     ascending order, so that each bucket's pivots clear the next bucket's
+//     columns before they are reduced (twist's order).
 //   * Convergence is tested on the device (the count of repeated lows from
 //     Phase I); kernels of a converged sweep return at once, so the host reads
 //     one status word per batch of sweeps, and the sweeps of a batch are
