@@ -474,7 +474,9 @@ __device__ __forceinline__ long long col_alloc(const PmsArgs &a, int j, long lon
 //   tier 1  a warp per column,  CAP 512      (pivot staged in shared memory
 //                                             when wider than the warp)
 //   tier 2  a CTA per column,   CAP 8192     (block-wide merge path)
-//   tier 3  a CTA per column,   buffers in the pool (no limit)
+//   tier 3  a CTA per column,   a bitmap of its rows (no limit; the merge
+//                               path in pool buffers when the bitmap's window
+//                               cannot hold a row)
 // The queues ping-pong between the worklist and widelist arrays (the scalar
 // tier hands on through slist).  Each addition costs one dependent round trip
 // when the pivot has at most four entries (its record carries them, with
