@@ -415,6 +415,14 @@ def run_ours(args, ws, rank, local):
                      "traffic": (traffic or {}).get("bytes_per_launch"),
                      "traffic_source": (traffic or {}).get("source"),
                      "note": ROOFLINE_NOTES.get(dom)},
+        # the reduction-level figure of the algorithmic byte count: D's twist
+        # work (the reference's) over the time this library takes for the
+        # whole reduction; above 1 on the anti-transpose, which skips that work
+        "reduction_bytes": {"bytes_per_reduction": ab["total"],
+                            "per_s_gbs": ab["total"] / (total_s / args.steps) / 1e9,
+                            "frac_of_peak": ab["total"] / (total_s / args.steps) / 1e9 / peak,
+                            "definition": "4 (nnz + m + 1) + 4 m + 4 (|P| + |T| + |T xor P|) over the CPU "
+                                          "twist's additions on D, per reduction"},
         "phases_ms_per_step": {"setup_and_transpose": setup_ms / args.steps, "phase1": p1_ms / args.steps,
                                "phase2_narrow": narrow_ms / args.steps, "tier1": tier_ms[0] / args.steps,
                                "tier2": tier_ms[1] / args.steps, "tier3": tier_ms[2] / args.steps,
