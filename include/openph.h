@@ -217,21 +217,23 @@ int oph_last_profile(oph_context *ctx, oph_profile *out);
  * oph_reduce_pms_noalloc — pms on device buffers WITHOUT allocating any
  * device memory.  No counterpart in the reference: it exists for callers that
  * cannot call cudaMalloc — a host framework whose caching allocator owns the
- * GPU's memory (MATLAB GPU arrays, PyTorch), a real-time pipeline that cannot
- * afford cudaMalloc's implicit synchronisation, code running while a stream
- * is being captured.  Every working array comes from one fixed 32 MiB device
- * array inside the library, held by every GPU that loads it until exit; a
- * matrix whose working set does not fit (roughly 200,000 columns of a
- * 2-complex) is rejected with OPH_ERR_OOM, and a column store that would have
- * to grow returns OPH_ERR_OVERFLOW (use oph_reduce_device for those).
+ * GPU's memory (MATLAB GPU arrays, PyTorch), or a real-time pipeline that
+ * cannot afford cudaMalloc's implicit synchronisation.  Every working array
+ * comes from one fixed 32 MiB device array inside the library, held by every
+ * GPU that loads it until exit; a matrix whose working set does not fit
+ * (roughly 200,000 columns of a 2-complex) is rejected with OPH_ERR_OOM, and
+ * a column store that would have to grow returns OPH_ERR_OVERFLOW (use
+ * oph_reduce_device for those).  A malformed CSC is rejected with
+ * OPH_ERR_BAD_INPUT before anything is written.
  * d_colptr (int64[m+1]) and d_rows are the 0-based CSC on the device; d_low
  * and d_ess (may be NULL) receive 0-based lows (-1 = none) and the essential
  * flags, as oph_reduce_device produces them.  `stream` is a cudaStream_t
- * (NULL = the legacy default stream); the call returns when the results are
- * in place.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race, so serialise
- * them.
+ * (NULL = the legacy default stream).  The call is synchronous (it returns
+ * when the results are in place, and reads sizes and status back to the
+ * host), so it must not be issued on a stream under capture.  The first call
+ * on a device looks up the array's address (cudaGetSymbolAddress) and keeps
+ * it for the process: not for use after a cudaDeviceReset.  All calls share
+ * the array: calls that overlap on the GPU race, so serialise them.
  */
 int oph_reduce_pms_noalloc(int64_t m, const int64_t *d_colptr, const int32_t *d_rows, int32_t *d_low,
                            int32_t *d_ess, void *stream);

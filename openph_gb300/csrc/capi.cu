@@ -218,6 +218,11 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
     // dimension bucket (not with per-sweep trackers, which follow D's own
     // reduction); wr is the matrix reduced
     int rc;
+    // nothing indexes through colptr / rows before they pass the structural
+    // check: here, or in the grading of dual_choose, which makes the same
+    // checks (bounds first) whenever it runs
+    const bool grades = pms && !ctx->track && ctx->dual != OPH_DUAL_NEVER && m > 0;
+    if (!w.checked && !grades && (rc = check_csc(ctx, w.colptr, w.rows, m, w.nnz, nullptr, 0))) return rc;
     bool dual = false;
     if (pms && !ctx->track) {
         bool bad = false;
@@ -439,6 +444,11 @@ static int batch_core(oph_context *ctx, int algo, int32_t count, const int64_t *
                       const int32_t *d_rows_local, int64_t total_m, int64_t total_nnz, int32_t *d_low, int32_t *d_ess,
                       oph_info *info) {
     cudaStream_t s = ctx->stream;
+    ctx->launches = 0;
+    // instance offsets, colptr and local rows checked before the shift reads
+    // through them
+    int rc = check_csc(ctx, d_colptr, d_rows_local, total_m, total_nnz, d_col_off, count);
+    if (rc) return rc;
     int32_t *d_rows_g = (int32_t *)ctx_alloc(ctx, S_COO_R, sizeof(int32_t) * (total_nnz > 0 ? total_nnz : 1));
     if (!d_rows_g) return OPH_ERR_OOM;
     if (total_m > 0)
@@ -446,11 +456,12 @@ static int batch_core(oph_context *ctx, int algo, int32_t count, const int64_t *
                                                             d_rows_g);
     OPH_CUDA_TRY(cudaGetLastError());
     Work w;
-    int rc = alloc_work(ctx, w, total_m);
+    rc = alloc_work(ctx, w, total_m);
     if (rc) return rc;
     w.nnz = total_nnz;
     w.colptr = d_colptr;
     w.rows = d_rows_g;
+    w.checked = true;
     Outputs o;
     o.low = d_low;
     o.ess = d_ess;
@@ -568,6 +579,7 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
     w.nnz = nnz;
     w.colptr = d_colptr;
     w.rows = d_rows;
+    w.checked = true;  // the COO conversion validated every entry
     const bool track = h_low_true && (err_linf || err_lone || err_redu || err_ess);
     int32_t *lt0 = d_lt, *esst = d_lt + mm;
     if (track && m > 0) {

@@ -3,21 +3,26 @@
 //
 // Some callers own all of the device's memory, or must not call cudaMalloc
 // at all: a host framework whose caching allocator holds the GPU (MATLAB's
-// GPU arrays, PyTorch's caching allocator), a real-time pipeline where
-// cudaMalloc's implicit device synchronisation is not acceptable, or code
-// that runs while a stream is being captured into a CUDA graph.  For them this
-// entry point reduces a small matrix with every working array carved out of
-// one fixed file-scope device array (NOALLOC_SCRATCH_BYTES, held by every GPU
-// that loads the library until the process exits).  The caller passes the
-// device input and output buffers and a stream; nothing here calls
+// GPU arrays, PyTorch's caching allocator), or a real-time pipeline where
+// cudaMalloc's implicit device synchronisation is not acceptable.  For them
+// this entry point reduces a small matrix with every working array carved out
+// of one fixed file-scope device array (NOALLOC_SCRATCH_BYTES, held by every
+// GPU that loads the library until the process exits).  The caller passes
+// the device input and output buffers and a stream; nothing here calls
 // cudaMalloc, cudaFree, cudaMallocHost or any allocating library routine.
 //
+// The call is synchronous: it reads the input's size and the convergence
+// status back to the host and waits on the stream, so it must not be issued
+// on a stream that is being captured into a CUDA graph.
+//
 // Set-up: the first call on a device looks up the array's device address
-// with cudaGetSymbolAddress (once per device, with that device current); make
-// that first call before any stream capture.  All calls share the one array:
-// calls that overlap on the GPU (two streams, two threads) race and corrupt
-// each other, so serialise them.  Each call re-initialises every part of the
-// array it reads, so nothing from the previous call leaks into the next.
+// with cudaGetSymbolAddress (once per device, with that device current) and
+// keeps it for the life of the process; a cudaDeviceReset invalidates it, so
+// the entry point is not for use after a device reset.  All calls share the
+// one array: calls that overlap on the GPU (two streams, two threads) race
+// and corrupt each other, so serialise them.  Each call re-initialises every
+// part of the array it reads, so nothing from the previous call leaks into
+// the next.
 #include <algorithm>
 #include <mutex>
 
@@ -29,6 +34,8 @@ namespace oph {
 __global__ void k_setup_columns(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                                 int *__restrict__ pool, int64_t *__restrict__ seg, int32_t *__restrict__ low,
                                 int8_t *__restrict__ dim, DevStatus *st);
+__global__ void k_check_csc(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                            int64_t nnz, const int64_t *__restrict__ inst_off, int count, int *bad);
 __global__ void k_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                        PivRec *__restrict__ rec);
 __global__ void k_beta(PivRec *__restrict__ rec, int64_t m, int32_t *__restrict__ beta);
@@ -150,13 +157,20 @@ extern "C" __attribute__((visibility("default"))) int oph_reduce_pms_noalloc(int
     init.max_dim = -1;
     OPH_CUDA_TRY(cudaMemcpyAsync(st, &init, sizeof(init), cudaMemcpyHostToDevice, s));
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)sm * 16));
+    // the caller's CSC is checked (read only) before any kernel writes
+    // through its offsets or rows
+    DevStatus hs;
+    k_check_csc<<<grid, 256, 0, s>>>(d_colptr, d_rows, m, nnz, nullptr, 0, &st->error);
+    OPH_CUDA_TRY(cudaGetLastError());
+    OPH_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs.error) return OPH_ERR_BAD_INPUT;
     k_setup_columns<<<grid, 256, 0, s>>>(d_colptr, d_rows, m, a.pool, a.seg, a.low, dim, st);
     OPH_CUDA_TRY(cudaMemsetAsync(a.rec, 0x7f, sizeof(PivRec) * m, s));
     OPH_CUDA_TRY(cudaMemsetAsync(beta, 0xff, sizeof(int32_t) * m, s));
     k_left<<<grid, 256, 0, s>>>(d_colptr, d_rows, m, a.rec);
     k_beta<<<grid, 256, 0, s>>>(a.rec, m, beta);
     OPH_CUDA_TRY(cudaGetLastError());
-    DevStatus hs;
     OPH_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
     OPH_CUDA_TRY(cudaStreamSynchronize(s));
     if (hs.error || hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;

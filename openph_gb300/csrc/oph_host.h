@@ -52,6 +52,7 @@ struct Work {
     const uint32_t *entry_col = nullptr;  // nnz: column of each entry, when known (the anti-transpose)
     const int64_t *src_colptr = nullptr;  // the anti-transpose: D's CSC, from which left[] follows
     const int32_t *src_rows = nullptr;
+    bool checked = false;             // colptr/rows already passed the structural check
 };
 
 struct Context;
@@ -60,6 +61,10 @@ struct Context;
 int setup_store(Context *ctx, Work &w, bool need_beta);
 int coo1_to_csc(Context *ctx, const int *d_rows1, const int *d_cols1, int64_t nnz, int64_t m, int64_t *d_colptr,
                 int32_t *d_rows0);
+// Structural check of a device CSC (k_check_csc), synchronous: OPH_OK or
+// OPH_ERR_BAD_INPUT.  With d_inst_off, rows are local to their instance.
+int check_csc(Context *ctx, const int64_t *d_colptr, const int32_t *d_rows, int64_t m, int64_t nnz,
+              const int64_t *d_inst_off, int count);
 int grow_pool(Context *ctx, Work &w);
 
 // pms.cu
@@ -106,7 +111,7 @@ struct Context {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev[8] = {};
-    DevBuf bufs[48];
+    DevBuf bufs[48];  // indexed by Slot
     DevStatus *h_status = nullptr;  // pinned mirror
     int max_sweeps = 0;             // 0 = default
     int64_t initial_pool_bytes = 0; // 0 = default
@@ -132,7 +137,7 @@ struct Context {
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_NSLOTS
 };
 
 }  // namespace oph

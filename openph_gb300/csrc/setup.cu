@@ -7,6 +7,8 @@
 //   compute_simplex_dimensions_h  src/cuda/dimensions.cu:54-104 (host, single thread)
 //   create_beta_h / create_beta   src/cuda/algorithms/pms/beta.cu:2-26 (host, single thread)
 //   assert_col_order              src/cuda/functions.cu:27-35 (warning only)
+#include <algorithm>
+
 #include "oph_host.h"
 
 namespace oph {
@@ -30,6 +32,50 @@ __global__ void k_coo1_to_csc(const int *__restrict__ r1, const int *__restrict_
             for (int64_t q = (k == 0 ? 0 : pc); q < c; q++) colptr[q] = k;  // columns pc+1 .. c (1-based)
         if (k == nnz - 1)
             for (int64_t q = c; q <= m; q++) colptr[q] = nnz;
+    }
+}
+
+// Structural check of a 0-based CSC before any kernel indexes through it:
+// colptr[0] == 0, colptr non-decreasing within [0, nnz], rows strictly
+// ascending inside a column and below the column count of their matrix —
+// m, or, for a batch (inst_off != nullptr), the size of the column's
+// instance, whose offsets must run from 0 to m without decreasing.  Only
+// reads; any violation sets *bad.  Bounds come first: no row is read
+// outside [0, nnz) and no offset outside [0, count].
+__global__ void k_check_csc(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                            int64_t nnz, const int64_t *__restrict__ inst_off, int count, int *bad) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    if (tid == 0 && (colptr[0] != 0 || colptr[m] != nnz)) atomicExch(bad, 1);
+    if (inst_off) {
+        for (int64_t b = tid; b < count; b += stride)
+            if (inst_off[b] > inst_off[b + 1] || (b == 0 && inst_off[0] != 0) ||
+                (b == count - 1 && inst_off[count] != m))
+                atomicExch(bad, 1);
+    }
+    for (int64_t j = tid; j < m; j += stride) {
+        const int64_t lo = colptr[j], hi = colptr[j + 1];
+        if (lo < 0 || hi < lo || hi > nnz) {
+            atomicExch(bad, 1);
+            continue;
+        }
+        int64_t lim = m;
+        if (inst_off) {
+            int a = 0, z = count;  // last b with inst_off[b] <= j (bounded steps whatever the offsets)
+            while (z - a > 1) {
+                const int mid = (a + z) >> 1;
+                if (inst_off[mid] <= j) a = mid; else z = mid;
+            }
+            lim = inst_off[a + 1] - inst_off[a];
+        }
+        int prev = -1;
+        for (int64_t k = lo; k < hi; k++) {
+            const int r = rows[k];
+            if (r <= prev || r >= lim) {
+                atomicExch(bad, 1);
+                break;
+            }
+            prev = r;
+        }
     }
 }
 
@@ -124,6 +170,22 @@ static int grid_for(Context *ctx, int64_t n, int block) {
     int64_t cap = (int64_t)ctx->sm_count * 16;
     if (g > cap) g = cap;
     return g < 1 ? 1 : (int)g;
+}
+
+int check_csc(Context *ctx, const int64_t *d_colptr, const int32_t *d_rows, int64_t m, int64_t nnz,
+              const int64_t *d_inst_off, int count) {
+    int *d_bad = (int *)ctx_alloc(ctx, S_CHECK, sizeof(int));
+    if (!d_bad) return OPH_ERR_OOM;
+    cudaStream_t s = ctx->stream;
+    OPH_CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(int), s));
+    k_check_csc<<<grid_for(ctx, std::max<int64_t>(m, count), 256), 256, 0, s>>>(d_colptr, d_rows, m, nnz,
+                                                                                d_inst_off, count, d_bad);
+    ctx->launches++;
+    OPH_CUDA_TRY(cudaGetLastError());
+    int bad = 0;
+    OPH_CUDA_TRY(cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    return bad ? OPH_ERR_BAD_INPUT : OPH_OK;
 }
 
 int coo1_to_csc(Context *ctx, const int *d_rows1, const int *d_cols1, int64_t nnz, int64_t m, int64_t *d_colptr,

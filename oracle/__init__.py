@@ -24,7 +24,6 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboph_oracle.so"
 REF_BIN = HERE / "_ref" / "ref_ph"
-REFERENCE_SRC = Path("/root/reference/src/cuda")
 
 
 class Stats(C.Structure):
@@ -41,8 +40,9 @@ def build(force: bool = False) -> None:
     src = HERE / "oracle.c"
     if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
         subprocess.run(["make", "-s", "-C", str(HERE), "liboph_oracle.so"], check=True)
-    if REFERENCE_SRC.exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+    # the reference's own CPU code, where its checkout exists (the recipe
+    # takes the checkout from OPENPH_REFERENCE)
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref-if-present"], check=True)
 
 
 _lib = None
@@ -83,6 +83,33 @@ def _run(name, bm):
 def twist(bm):
     """CPU twist (src/cuda/algorithms/twist/twist.cu:10-87)."""
     return _run("oracle_twist", bm)
+
+
+class _Csc:
+    """The fields of a boundary matrix that the oracle reads."""
+
+    def __init__(self, colptr, rows):
+        self.colptr = np.ascontiguousarray(colptr, dtype=np.int64)
+        self.rows = np.ascontiguousarray(rows, dtype=np.int32)
+        self.m = int(self.colptr.shape[0] - 1)
+
+
+def _twist_job(job):
+    low, ess, _ = twist(_Csc(*job))
+    return low, ess
+
+
+def twist_many(jobs, processes: int | None = None):
+    """The CPU twist over many matrices, each a (colptr, rows) pair, in
+    worker processes started with ``spawn`` (safe in a parent that has
+    already initialised CUDA).  Returns [(low, ess), ...] in job order."""
+    import multiprocessing as mp
+    jobs = list(jobs)
+    if not jobs:
+        return []
+    n = max(1, min(processes or os.cpu_count() or 1, len(jobs)))
+    with mp.get_context("spawn").Pool(n) as pool:
+        return pool.map(_twist_job, jobs, chunksize=max(1, len(jobs) // (8 * n)))
 
 
 def standard(bm):

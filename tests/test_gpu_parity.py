@@ -321,3 +321,31 @@ def test_batch_ragged_with_empty_instances(ctx):
         want, want_ess, _ = oracle.twist(bm)
         np.testing.assert_array_equal(low, want)
         np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_void_openph_drop_in_symbol(cuda_lib):
+    """The reference's own symbol, void openph(...) (src/cuda/openph.cu:29-35),
+    called with the arguments the MEX gateway passes (src/matlab/ph/ph.cu:
+    71-74): the outputs land in the caller's arrays; an unknown algorithm
+    string prints and leaves low all zeros, as the drop-in contract says."""
+    from cases import triangle
+    for bm, algo in ((cx.rips_cube(24, seed=8), "pms"), (cx.rips_cube(24, seed=8), "twist"), (triangle(), "pms")):
+        r, c = bm.to_coo1()
+        m = bm.m
+        low = np.full(m, -9, np.int32)
+        ess = np.full(m, -9, np.int32)
+        trk = [np.zeros(m + 1, np.float32) for _ in range(5)]
+        it = np.zeros(1, np.int32)
+        low_true = np.zeros(m, np.int32)
+        cuda_lib.openph(algo.encode(), r, c, m, 4, low_true.ctypes.data, len(r), low, ess, *trk, it, 0)
+        want_low, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want_low + 1, err_msg=algo)
+        np.testing.assert_array_equal(ess, want_ess, err_msg=algo)
+        assert it[0] >= 1
+    bm = triangle()
+    r, c = bm.to_coo1()
+    low = np.full(bm.m, 5, np.int32)
+    ess = np.zeros(bm.m, np.int32)
+    trk = [np.zeros(bm.m + 1, np.float32) for _ in range(5)]
+    cuda_lib.openph(b"not_an_algorithm", r, c, bm.m, 4, None, len(r), low, ess, *trk, np.zeros(1, np.int32), 0)
+    np.testing.assert_array_equal(low, np.zeros(bm.m, np.int32))
