@@ -1,22 +1,43 @@
 #!/usr/bin/env python
-"""Benchmark: pms on one Rips complex of a noisy torus (~5M columns).
+"""Benchmark of the pms reduction on one GB300: a large complex, a batch of
+complexes in one pass, and a served request stream.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload all|torus|batch|serve]
 
-One step = one full pms reduction of the complex (set-up, sweeps, outputs),
-by the library's own choice of matrix (the anti-transpose, for this complex).
-``value`` is columns/s with the boundary matrix already resident in HBM;
-``e2e`` is the same metric through the drop-in ``openph()`` C call with host
-(pinned) COO input and host outputs, copies included.  The roofline is the
-Phase II kernel that takes the most time, timed with CUDA events on the
-library's stream in a second pass of the same steps.  ``cpu_baseline`` is the
-fixed-slot port of the reference's CPU twist on a bounded prefix of the same
-reduction.
+The default run (``--workload all``) prints ONE JSON line whose headline is
+columns/s on one Rips complex of a noisy torus (400 points, 5,000,179
+columns), with two more objects beside it:
 
-``--impl reference`` times the reference's CPU twist (its port; the
-reference's own build needs its source tree) on the host cores, on the same
-matrix and metric.  For N > 1 every rank reduces its own replica (no
-collective on the data path); rank 0 prints.
+* ``batch``: 4096 Rips complexes (n ~ U[20, 120], half cube, half noisy
+  circle) reduced in one segmented pass, complexes/s against plain pms one
+  complex at a time on the same GPU; every instance is checked against its
+  one-at-a-time result and against the oracle's twist.
+* ``serve``: a Poisson stream of requests (m log-uniform in [10^3, 2*10^6],
+  the three generator families, fresh seeds) through the continuous-batching
+  server, served complexes/s and p50/p99 latency at saturation, against plain
+  sequential pms on the same GPU; every request is checked against plain pms
+  and against the oracle's twist.
+
+For the headline, one step = one full reduction of the complex (set-up,
+sweeps, outputs) by the library's own choice of matrix.  ``value`` is
+columns/s with the boundary matrix already in HBM; ``e2e`` is the same metric
+through the drop-in ``openph()`` C call with pinned host COO in and host
+outputs, copies included.  The roofline is the Phase II kernel that takes the
+most time, timed with CUDA events on the library's stream in a second pass of
+the same steps.  ``cpu_baseline`` is one whole reduction of the same complex
+by the fixed-slot port of the reference's CPU twist on one host core.
+
+``--impl reference`` times that fixed-slot port of the reference's CPU twist
+(the reference's own build needs its source tree) on the host cores: each
+step is one whole reduction of the same complex, and the steps run side by
+side in one process per core.  For N > 1 every rank reduces its own replica
+of the torus (no collective on the data path); rank 0 prints.
+
+CPU work (the oracle checks, the CPU baselines, request generation) runs in
+a pool of worker processes started with ``spawn`` before any CUDA use, and
+never beside a timed GPU region that it could slow down except for the two
+single-core torus jobs, which overlap the torus timing on 2 of the cores.
 """
 from __future__ import annotations
 
@@ -37,10 +58,15 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOAD = {"name": "rips_torus", "points": 400, "target_m": 5_000_000, "seed": 2,
             "torus": {"R": 2.0, "r": 1.0, "sigma": 0.05}}
-CPU_SAMPLE_SECONDS = 15.0
-REF_STEP_SECONDS = 3.0
+BATCH = {"count": 4096, "seed": 4, "lo": 20, "hi": 120}
+SERVE = {"requests": 160, "m_lo": 1_000, "m_hi": 2_000_000, "seed": 5, "budget_bytes": 150 * (1 << 30),
+         "rates_x_plain": [0.5, 1, 2, 4, 8, 16, 32]}
 L2_FLUSH_BYTES = 512 << 20
 COL_WIDTH = 80  # slot width factor for the fixed-slot CPU port (p = 240 >= widest column)
+
+
+def log(*a):
+    print("[bench]", *a, file=sys.stderr, flush=True)
 
 
 def dist_env():
@@ -77,6 +103,30 @@ def barrier(dist, device=None):
             dist.barrier()
 
 
+def host_cpu() -> str:
+    """The host CPU model and its core count, as lscpu reports them."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return f"{model or 'unknown CPU'} x {os.cpu_count()} cores"
+
+
+def mem_available_bytes() -> int:
+    try:
+        for line in Path("/proc/meminfo").read_text().splitlines():
+            if line.startswith("MemAvailable:"):
+                return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 16 << 30
+
+
 def make_workload():
     from openph_gb300 import complexes as cx
     w = WORKLOAD
@@ -88,36 +138,113 @@ def make_workload():
     return bm
 
 
-def device_generation(bm, ctx, device, reps=3) -> dict:
-    """The same complex built on the GPU from the points (best of a few
-    runs, wall time of the call, which returns with the matrix in HBM),
-    beside the host generator's time, and whether the two are identical."""
-    import torch
+# ------------------------------------------------------------ pool jobs
+# Functions run in the spawned worker processes (they import what they use).
 
-    from openph_gb300 import complexes as cx
-    pts = torch.from_numpy(bm.meta["points"]).to(device)
-    torch.cuda.synchronize()
-    best, dm = None, None
-    for _ in range(reps):
+def _bm(colptr, rows):
+    from openph_gb300.complexes import BoundaryMatrix
+    return BoundaryMatrix(colptr, rows)
+
+
+def _job_twist_full(job):
+    """The oracle's twist on one matrix: lows, ess and its statistics."""
+    import oracle
+    colptr, rows = job
+    t0 = time.perf_counter()
+    low, ess, st = oracle.twist(_bm(colptr, rows))
+    st["wall"] = time.perf_counter() - t0
+    return low, ess, st
+
+
+def _job_fixed_full(job):
+    """One whole reduction by the fixed-slot port of the reference's twist
+    (slot width raised until the reduction fits, as the reference's users
+    do); the low array's checksum is returned for a parity check."""
+    import oracle
+    colptr, rows, width = job
+    bm = _bm(colptr, rows)
+    while True:
         t0 = time.perf_counter()
-        dm = cx.rips_device(pts, bm.meta["threshold"], ctx=ctx, device=device)
-        dt = time.perf_counter() - t0
-        best = dt if best is None else min(best, dt)
-    h = dm.to_host()
-    same = bool(np.array_equal(h.colptr, bm.colptr) and np.array_equal(h.rows, bm.rows))
-    return {"host_rips_s": bm.meta["host_rips_s"], "device_rips_ms": 1e3 * best, "device_equals_host": same,
-            "api": "oph_rips_device (points in HBM -> sorted CSC in HBM)"}
+        rc, low, _, st = oracle.twist_fixed_p(bm, width)
+        wall = time.perf_counter() - t0
+        if rc == 0:
+            return {"seconds": st["seconds"], "wall": wall, "col_width": width, "columns": st["columns_done"],
+                    "additions": st["additions"], "low_checksum": low_checksum(low)}
+        width *= 2
 
 
-def algorithmic_bytes(bm, st) -> dict:
-    """Bytes per reduction by the reference's layout: the CSC read once, low
-    written, and for every twist addition |P| + |T| read and |T xor P| written
-    (int32 slots)."""
-    base = 4 * (bm.nnz + bm.m + 1) + 4 * bm.m
-    adds = 4 * (st["slots_read"] + st["slots_written"])
-    return {"total": base + adds, "additions": adds, "twist_additions": st["additions"]}
+def low_checksum(low) -> int:
+    """A position-weighted checksum of a low array (parity of runs that do
+    not hand their whole output back)."""
+    w = np.arange(1, len(low) + 1, dtype=np.int64) % 1000003
+    return int(np.sum((low.astype(np.int64) + 2) * w) % (1 << 61))
 
 
+def _job_fixed_prefix(job):
+    """A bounded prefix of the fixed-slot port (warm-up of the reference arm)."""
+    import oracle
+    colptr, rows, width, seconds = job
+    oracle.twist_fixed_p(_bm(colptr, rows), width, max_columns=0, max_seconds=seconds)
+    return os.getpid()
+
+
+def _job_batch_oracle(items):
+    """Batch instances regenerated from their (points, seed) and reduced by
+    the oracle's twist: [(b, low, ess, seconds of the twist)]."""
+    import oracle
+    from openph_gb300 import complexes as cx
+    out = []
+    for b, n, seed in items:
+        _, colptr, rows = cx.rips_mixed_instances([n], [seed], threads=1)
+        t0 = time.perf_counter()
+        low, ess, _ = oracle.twist(_bm(colptr, rows))
+        out.append((b, low, ess, time.perf_counter() - t0))
+    return out
+
+
+def _serve_matrix(kind, m, seed):
+    from openph_gb300 import complexes as cx
+    if kind == "rips_cube":
+        n = max(4, int(round((6 * m) ** (1 / 3))))
+        return cx.rips_cube(n, seed=seed)
+    if kind == "rips_torus":
+        return cx.rips_torus(400, m, seed=seed)
+    side = max(4, int(round((m / 6) ** 0.5)))
+    return cx.lower_star_image(side, side, seed=seed)
+
+
+def _job_serve_request(job):
+    """One request of the serving stream: (kind, target m, seed) -> CSC."""
+    kind, m, seed = job
+    bm = _serve_matrix(kind, m, seed)
+    return kind, bm.colptr, bm.rows
+
+
+def _job_serve_oracle(job):
+    """One request regenerated and reduced by the oracle's twist."""
+    import oracle
+    k, kind, m, seed = job
+    bm = _serve_matrix(kind, m, seed)
+    t0 = time.perf_counter()
+    low, ess, _ = oracle.twist(bm)
+    return k, low, ess, time.perf_counter() - t0
+
+
+def _job_warm(_):
+    import oracle  # noqa: F401  (the port's library loaded once per worker)
+    from openph_gb300 import complexes  # noqa: F401
+    return os.getpid()
+
+
+def start_pool(processes=None):
+    import multiprocessing as mp
+    n = processes or os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(n)
+    pool.map(_job_warm, range(2 * n))
+    return pool, n
+
+
+# ------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons, sampled while running."""
 
@@ -128,7 +255,7 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"oph_clocks_{os.getpid()}.csv"
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"oph_clocks_{os.getpid()}_{id(self)}.csv"
 
     def __enter__(self):
         try:
@@ -174,53 +301,57 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_port_sample(bm, seconds: float):
-    """The fixed-slot twist port on a bounded prefix of the reduction order."""
-    import oracle
-    rc, _, _, st = oracle.twist_fixed_p(bm, COL_WIDTH, max_columns=0, max_seconds=seconds)
-    if rc != 0:
-        raise RuntimeError(f"CPU port failed with status {rc}")
-    return st["columns_done"] / st["seconds"], st
-
-
+# ------------------------------------------------------- reference arm
 def run_reference(args, ws, rank):
+    """The fixed-slot port of the reference's CPU twist on the host cores:
+    each step is one whole reduction of the torus, the steps side by side,
+    one process per core (as many as the host's memory holds)."""
     if rank != 0:
         return 0
     import oracle
     oracle.build()
     bm = make_workload()
-    for _ in range(args.warmup):
-        cpu_port_sample(bm, 0.5)
-    rates, cols, secs = [], 0, 0.0
-    for _ in range(args.steps):
-        r, st = cpu_port_sample(bm, REF_STEP_SECONDS)
-        rates.append(r)
-        cols += st["columns_done"]
-        secs += st["seconds"]
-    value = cols / secs
+    m, nnz = bm.m, bm.nnz
+    width = COL_WIDTH
+    per_proc = 2 * 4 * m * width * int(np.diff(bm.colptr).max()) + (1 << 30)
+    procs = max(1, min(args.steps, os.cpu_count() or 1, int(0.75 * mem_available_bytes()) // per_proc))
+    pool, _ = start_pool(procs)
+    job = (bm.colptr, bm.rows)
+    pool.map(_job_fixed_prefix, [job + (width, 1.0)] * max(args.warmup, procs))
+    log(f"reference arm: {args.steps} whole reductions on {procs} processes")
+    t0 = time.perf_counter()
+    res = pool.map(_job_fixed_full, [job + (width,)] * args.steps, chunksize=1)
+    wall = time.perf_counter() - t0
+    pool.close()
+    pool.join()
+    value = args.steps * m / wall
+    per_proc_rate = m / float(np.mean([r["seconds"] for r in res]))
     line = {
         "metric": "cols/s", "value": value, "unit": "cols/s", "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generator)",
         "impl": "reference",
-        "config": {"workload": f"rips_torus_{WORKLOAD['points']}pts_{bm.m}cols", "m": bm.m, "nnz": bm.nnz,
-                   "algorithm": "twist (reference CPU reduction, fixed-slot layout)", "col_width": COL_WIDTH,
-                   "seed": WORKLOAD["seed"]},
-        "cpu_baseline": {"value": value, "unit": "cols/s", "cores": 1, "kind": "port",
-                         "sample": f"first columns of the twist order of the same matrix, {REF_STEP_SECONDS:.0f} s "
-                                   f"per step ({cols} columns over {args.steps} steps); the reference's twist is "
-                                   "single-threaded"},
+        "config": {"workload": f"rips_torus_{WORKLOAD['points']}pts_{m}cols", "m": m, "nnz": nnz,
+                   "algorithm": "twist (reference CPU reduction, fixed-slot layout)",
+                   "col_width": res[0]["col_width"], "seed": WORKLOAD["seed"]},
+        "cpu_baseline": {"value": value, "unit": "cols/s", "cores": procs, "kind": "port",
+                         "sample": f"{args.steps} whole reductions of the same matrix ({m} columns each), "
+                                   f"{procs} at a time, one per process, on {host_cpu()}; one reduction takes "
+                                   f"{np.mean([r['seconds'] for r in res]):.1f} s of twist "
+                                   f"({per_proc_rate:.0f} cols/s per core); the reference's twist is "
+                                   "single-threaded",
+                         "per_core_value": per_proc_rate},
         "e2e": {"value": value, "unit": "cols/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
+# --------------------------------------------------------------- torus
 # What bounds each Phase II kernel, from its ncu captures (profiles/).
 ROOFLINE_NOTES = {
-    "tier3": "latency-bound: chains of dependent additions on a few long columns of the anti-transpose "
-             "(ncu: 0.4% SM throughput, DRAM idle, the bitmaps in L2); the merge-equivalent bytes are "
-             "what a merge would move, ~58x the kernel's DRAM traffic",
+    "tier3": "latency-bound: chains of dependent additions on a few long columns of the anti-transpose; "
+             "the merge-equivalent bytes are what a merge would move, far above the kernel's DRAM traffic",
     "narrow": "instruction-issue-bound (ncu: 60-89% issue active, DRAM 1-2%); T stays on chip per chain",
 }
 
@@ -235,34 +366,46 @@ def load_traffic():
     return None
 
 
-def run_ours(args, ws, rank, local):
+def algorithmic_bytes(bm, st) -> dict:
+    """Bytes per reduction by the reference's layout: the CSC read once, low
+    written, and for every twist addition |P| + |T| read and |T xor P| written
+    (int32 slots)."""
+    base = 4 * (bm.nnz + bm.m + 1) + 4 * bm.m
+    adds = 4 * (st["slots_read"] + st["slots_written"])
+    return {"total": base + adds, "additions": adds, "twist_additions": st["additions"]}
+
+
+def device_generation(bm, ctx, device, reps=3) -> dict:
+    """The same complex built on the GPU from the points (best of a few
+    runs, wall time of the call, which returns with the matrix in HBM),
+    beside the host generator's time, and whether the two are identical."""
+    import torch
+
+    from openph_gb300 import complexes as cx
+    pts = torch.from_numpy(bm.meta["points"]).to(device)
+    torch.cuda.synchronize()
+    best, dm = None, None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        dm = cx.rips_device(pts, bm.meta["threshold"], ctx=ctx, device=device)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    h = dm.to_host()
+    same = bool(np.array_equal(h.colptr, bm.colptr) and np.array_equal(h.rows, bm.rows))
+    return {"host_rips_s": bm.meta["host_rips_s"], "device_rips_ms": 1e3 * best, "device_equals_host": same,
+            "api": "oph_rips_device (points in HBM -> sorted CSC in HBM)"}
+
+
+def run_torus(args, ws, rank, local, bm, dist):
+    """The headline: GPU timing of the torus (device-resident and end to
+    end).  Returns the line without its oracle-dependent fields, and the
+    device outputs to check."""
     import torch
 
     from openph_gb300 import api
 
     device = torch.device("cuda", local)
-    torch.cuda.set_device(device)
-    dist = init_dist(ws, "nccl")
-    api.lib()
-    bm = make_workload()
     m, nnz = bm.m, bm.nnz
-
-    # the oracle: full CPU twist in the background (algorithmic bytes and a
-    # bit-exact check of the GPU result at full size); rank 0 only
-    oracle_out = {}
-
-    def oracle_job():
-        import oracle
-        low, ess, st = oracle.twist(bm)
-        oracle_out.update(low=low, ess=ess, st=st)
-
-    th = None
-    if rank == 0:
-        import oracle
-        oracle.build()
-        th = threading.Thread(target=oracle_job, daemon=True)
-        th.start()
-
     ctx = api.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=device)
     d_colptr = torch.from_numpy(bm.colptr).to(device)
@@ -284,8 +427,7 @@ def run_ours(args, ws, rank, local):
     infos = []
     barrier(dist, device)
     torch.cuda.synchronize()
-    # the headline: the library's own schedule (sweeps replayed from its
-    # captured CUDA graph), no per-phase events
+    # the headline: the library's own schedule, no per-phase events
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
             flush.fill_(k)  # evict L2 between steps (512 MB write)
@@ -334,13 +476,13 @@ def run_ours(args, ws, rank, local):
     h_ess = torch.empty(m, dtype=torch.int32).pin_memory()
     it = np.zeros(1, np.int32)
     L = api.lib()
-    L.oph_openph.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int,
-                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                             C.c_void_p, C.c_int]
+    fn = L.oph_openph
+    fn.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
 
     def e2e_step():
-        rc = L.oph_openph(b"pms", h_r.data_ptr(), h_c.data_ptr(), m, 0, None, nnz, h_low.data_ptr(),
-                          h_ess.data_ptr(), None, None, None, None, None, it.ctypes.data, local)
+        rc = fn(b"pms", h_r.data_ptr(), h_c.data_ptr(), m, 0, None, nnz, h_low.data_ptr(), h_ess.data_ptr(), None,
+                None, None, None, None, it.ctypes.data, local)
         if rc != 0:
             raise api.OphError(rc, "openph")
 
@@ -355,25 +497,17 @@ def run_ours(args, ws, rank, local):
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(sum(e2e_times), dist, device)
 
-    if rank != 0:
-        barrier(dist, device)
-        return 0
-
-    generation = device_generation(bm, ctx, device)
-    th.join()
-    st = oracle_out["st"]
+    generation = device_generation(bm, ctx, device) if rank == 0 else None
     low_gpu = d_low.cpu().numpy()
-    parity = bool(np.array_equal(low_gpu, oracle_out["low"]) and np.array_equal(d_ess.cpu().numpy(),
-                                                                               oracle_out["ess"]))
-    parity_e2e = bool(np.array_equal(h_low.numpy(), oracle_out["low"] + 1))
-    cpu_rate, cpu_st = cpu_port_sample(bm, CPU_SAMPLE_SECONDS)
+    ess_gpu = d_ess.cpu().numpy()
+    low_e2e = h_low.numpy().copy()
+    ess_e2e = h_ess.numpy().copy()
 
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
         peaks = json.loads(pk.read_text())
     peak = peaks.get("hbm_gbs", 6800.0)
-    ab = algorithmic_bytes(bm, st)
     # the dominant Phase II kernel (one launch per sweep, CUDA events around
     # each tier on the library's stream): its algorithmic bytes are the
     # per-addition figure 4 (|P| + |T| + |T xor P|) summed over the additions
@@ -411,18 +545,9 @@ def run_ours(args, ws, rank, local):
                      "algorithmic_bytes_per_launch": dom_bytes / launches_per_red if launches_per_red else None,
                      "mean_launch_ms": dom_ms / max(1, p2_launches),
                      "launches_per_reduction": launches_per_red,
-                     "twist_on_d_algorithmic_bytes_per_reduction": ab["additions"],
                      "traffic": (traffic or {}).get("bytes_per_launch"),
                      "traffic_source": (traffic or {}).get("source"),
                      "note": ROOFLINE_NOTES.get(dom)},
-        # the reduction-level figure of the algorithmic byte count: D's twist
-        # work (the reference's) over the time this library takes for the
-        # whole reduction; above 1 on the anti-transpose, which skips that work
-        "reduction_bytes": {"bytes_per_reduction": ab["total"],
-                            "per_s_gbs": ab["total"] / (total_s / args.steps) / 1e9,
-                            "frac_of_peak": ab["total"] / (total_s / args.steps) / 1e9 / peak,
-                            "definition": "4 (nnz + m + 1) + 4 m + 4 (|P| + |T| + |T xor P|) over the CPU "
-                                          "twist's additions on D, per reduction"},
         "phases_ms_per_step": {"setup_and_transpose": setup_ms / args.steps, "phase1": p1_ms / args.steps,
                                "phase2_narrow": narrow_ms / args.steps, "tier1": tier_ms[0] / args.steps,
                                "tier2": tier_ms[1] / args.steps, "tier3": tier_ms[2] / args.steps,
@@ -432,116 +557,51 @@ def run_ours(args, ws, rank, local):
         "matrix_reduced": "anti-transpose D' (OPH_DUAL_AUTO)" if infos[-1]["dual"] else "D",
         "sweeps": infos[-1]["sweeps"], "device_additions": infos[-1]["additions"],
         "device_slots_per_tier": slot_prof["tier_slots"],
-        "twist_additions_on_d": st["additions"],
-        "cpu_baseline": {"value": cpu_rate, "unit": "cols/s", "cores": 1, "kind": "port",
-                         "sample": f"fixed-slot twist port, first {cpu_st['columns_done']} columns of the twist "
-                                   f"order of the same matrix ({cpu_st['seconds']:.1f} s)"},
-        "parity": {"low_ess_equal_oracle": parity, "e2e_low_equal_oracle": parity_e2e},
         "generation": generation,
         "clocks": clocks.summary(),
         "gpu_launches": launches,
         "gpu_launches_source": "kernel launches counted by the library over the profiled pass of the same steps",
     }
-    print(json.dumps(line), flush=True)
     ctx.close()
-    if dist is not None:
-        barrier(dist, device)
-    return 0 if (parity and parity_e2e) else 3
+    del d_colptr, d_rows, d_low, d_ess, flush
+    torch.cuda.empty_cache()
+    return line, (low_gpu, ess_gpu, low_e2e, ess_e2e)
 
 
-BATCH = {"count": 4096, "seed": 4, "lo": 20, "hi": 120}
-
-
-def _batch_cpu_instance(job):
-    """One batch instance through the reference-layout twist port (runs in a
-    spawned worker; raises col_width until the instance fits, as the
-    reference's users do)."""
-    colptr, rows = job
-    import oracle
-    from openph_gb300.complexes import BoundaryMatrix
-    bm = BoundaryMatrix(colptr, rows)
-    width = COL_WIDTH
-    while True:
-        rc, _, _, st = oracle.twist_fixed_p(bm, width)
-        if rc == 0:
-            return st["seconds"]
-        width *= 2
-
-
-def cpu_batch_sample(col_off, colptr, rows, seconds: float) -> dict:
-    """Complexes/s of the CPU twist port with one instance per process on
-    every host core (spawned workers, the instances in order), over about
-    `seconds` of wall time."""
-    def jobs():
-        for b in range(len(col_off) - 1):
-            c0, c1 = int(col_off[b]), int(col_off[b + 1])
-            yield colptr[c0:c1 + 1] - colptr[c0], rows[int(colptr[c0]):int(colptr[c1])]
-
-    return cpu_pool_sample(jobs(), seconds, "instances of the batch")
-
-
-def _pool_warm(_):
-    import oracle  # noqa: F401  (loads the port's library once per worker)
-    from openph_gb300 import complexes  # noqa: F401
-    return os.getpid()
-
-
-def cpu_pool_sample(jobs, seconds: float, what: str) -> dict:
-    import multiprocessing as mp
-    cores = os.cpu_count() or 1
-    done = 0
-    with mp.get_context("spawn").Pool(cores) as pool:
-        pool.map(_pool_warm, range(4 * cores))  # workers started and imported before the clock
-        it = pool.imap(_batch_cpu_instance, jobs, chunksize=1)
-        t0 = time.perf_counter()
-        for _ in it:
-            done += 1
-            if time.perf_counter() - t0 >= seconds:
-                break
-        wall = time.perf_counter() - t0
-        pool.terminate()
-    return {"value": done / wall, "unit": "complexes/s", "cores": cores, "kind": "port",
-            "sample": f"the first {done} {what}, one per process on {cores} host cores, "
-                      f"reference-layout twist port ({wall:.1f} s wall)"}
-
-
-def run_batch(args, ws, rank, local):
-    """The batched workload: 4096 Rips complexes (n ~ U[20,120], half cube,
-    half noisy circle) reduced in one segmented pass, against plain pms one
-    complex at a time on the same GPU.  Bit-exactness: every instance of the
-    batched result equals the one-at-a-time result, and a seeded sample of
-    instances equals the oracle."""
+# --------------------------------------------------------------- batch
+def run_batch(args, local, pool, cores, count, before_timing=None):
+    """The batched workload: `count` Rips complexes in one segmented pass,
+    against plain pms one complex at a time on the same GPU, every instance
+    checked against its one-at-a-time result and the oracle's twist."""
     import torch
 
-    import oracle
     from openph_gb300 import api
     from openph_gb300 import complexes as cx
 
     device = torch.device("cuda", local)
-    torch.cuda.set_device(device)
-    dist = init_dist(ws, "nccl")
     t0 = time.perf_counter()
-    col_off, colptr, rows, npts, seeds = cx.rips_mixed_batch(args.count or BATCH["count"], BATCH["seed"],
-                                                             lo=BATCH["lo"], hi=BATCH["hi"])
+    col_off, colptr, rows, npts, seeds = cx.rips_mixed_batch(count, BATCH["seed"], lo=BATCH["lo"], hi=BATCH["hi"])
     gen_s = time.perf_counter() - t0
-    count = len(col_off) - 1
     total_m, total_nnz = int(col_off[-1]), int(colptr[-1])
+    log(f"batch: {count} complexes, {total_m} columns, generated in {gen_s:.1f} s")
+    if before_timing is not None:
+        before_timing()  # no pool work beside the timed region
     ctx = api.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=device)
     d_off = torch.from_numpy(col_off).to(device)
     d_colptr = torch.from_numpy(colptr).to(device)
     d_rows = torch.from_numpy(rows).to(device)
     d_low = torch.empty(total_m, dtype=torch.int32, device=device)
+    d_ess = torch.empty(total_m, dtype=torch.int32, device=device)
     torch.cuda.synchronize()
 
     def batched():
         return ctx.reduce_batch_device(count, d_off.data_ptr(), d_colptr.data_ptr(), d_rows.data_ptr(), total_m,
-                                       total_nnz, d_low.data_ptr(), None, "pms")
+                                       total_nnz, d_low.data_ptr(), d_ess.data_ptr(), "pms")
 
     for _ in range(args.warmup):
         batched()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    barrier(dist, device)
     with ClockSampler(local) as clocks:
         for k in range(args.steps):
             torch.cuda.synchronize()
@@ -549,21 +609,20 @@ def run_batch(args, ws, rank, local):
             info = batched()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
+    batch_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3
     # the kernel launches of one step, counted by the library in a profiled
     # (untimed) repeat of the same step
     ctx.set_profile(True)
     batched()
     launches = ctx.last_profile()["kernel_launches"] * args.steps
     ctx.set_profile(False)
-    batch_s = max_over_ranks(sum(a.elapsed_time(b) for a, b in ev) / 1e3, dist, device)
     low_batch = d_low.cpu().numpy()
+    ess_batch = d_ess.cpu().numpy()
 
     # plain pms, one complex at a time, device-resident inputs
     d_low1 = torch.empty(int(np.diff(col_off).max()), dtype=torch.int32, device=device)
-    colptr_d = [None] * count
-    for b in range(count):
-        c0, c1 = int(col_off[b]), int(col_off[b + 1])
-        colptr_d[b] = torch.from_numpy(colptr[c0:c1 + 1] - colptr[c0]).to(device)
+    colptr_d = [torch.from_numpy(colptr[col_off[b]:col_off[b + 1] + 1] - colptr[col_off[b]]).to(device)
+                for b in range(count)]
     rows_d = [d_rows[int(colptr[col_off[b]]):int(colptr[col_off[b + 1]])] for b in range(count)]
     for b in range(min(count, 8)):
         ctx.reduce_device(int(col_off[b + 1] - col_off[b]), colptr_d[b].data_ptr(), rows_d[b].data_ptr(),
@@ -581,7 +640,8 @@ def run_batch(args, ws, rank, local):
         seq_ms += e0.elapsed_time(e1)
         if not np.array_equal(d_low1[:mb].cpu().numpy(), low_batch[col_off[b]:col_off[b + 1]]):
             mismatches += 1
-    seq_s = max_over_ranks(seq_ms / 1e3, dist, device)
+    seq_s = seq_ms / 1e3
+    del colptr_d, rows_d, d_low1
 
     # end to end through the C ABI: pinned host CSC in, host lows out
     h_off = torch.from_numpy(col_off).pin_memory()
@@ -603,104 +663,91 @@ def run_batch(args, ws, rank, local):
         t0 = time.perf_counter()
         e2e_step()
         e2e_s += time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, dist, device)
     e2e_equal = bool(np.array_equal(h_low.numpy(), low_batch))
-
-    # oracle on a seeded sample of instances
-    rng = np.random.default_rng(7)
-    sample = sorted(rng.choice(count, size=min(count, 24), replace=False).tolist())
-    oracle_ok = True
-    for b in sample:
-        bm = cx.batch_instance(col_off, colptr, rows, b)
-        want, _, _ = oracle.twist(bm)
-        oracle_ok &= bool(np.array_equal(want, low_batch[col_off[b]:col_off[b + 1]]))
-    if rank == 0:
-        line = {
-            "metric": "complexes/s", "value": ws * count * args.steps / batch_s, "unit": "complexes/s",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * batch_s / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded generator)",
-            "config": {"workload": f"rips_mixed_batch_{count}", "total_m": total_m, "total_nnz": total_nnz,
-                       "points": [BATCH["lo"], BATCH["hi"]], "seed": BATCH["seed"], "algorithm": "pms",
-                       "l2": "inputs (%.1f GB) larger than L2" % ((total_nnz * 4 + total_m * 8) / 1e9)},
-            "plain_sequential": {"complexes_per_s": count / seq_s, "s_total": seq_s},
-            "batched_over_plain": (count * args.steps / batch_s) / (count / seq_s),
-            "e2e": {"value": ws * count * args.steps / e2e_s, "unit": "complexes/s",
-                    "h2d_bytes_per_step": 8 * (count + 1) + 8 * (total_m + 1) + 4 * total_nnz,
-                    "d2h_bytes_per_step": 4 * total_m, "ms_per_step": 1e3 * e2e_s / args.steps,
-                    "api": "oph_reduce_batch C ABI", "equal_to_device_run": e2e_equal},
-            "cpu_baseline": cpu_batch_sample(col_off, colptr, rows, CPU_SAMPLE_SECONDS),
-            "cols_per_s": ws * total_m * args.steps / batch_s,
-            "matrix_reduced": "anti-transpose D' (OPH_DUAL_AUTO)" if info["dual"] else "D",
-            "sweeps": info["sweeps"], "device_additions": info["additions"], "regrows": info["regrows"],
-            "pool_bytes": info["pool_bytes"],
-            "parity": {"batched_equals_one_at_a_time": mismatches == 0, "mismatched_instances": mismatches,
-                       "oracle_sample": len(sample), "oracle_sample_equal": oracle_ok},
-            "generation_s": gen_s, "clocks": clocks.summary(), "gpu_launches": launches,
-        }
-        print(json.dumps(line), flush=True)
     ctx.close()
-    return 0 if (mismatches == 0 and oracle_ok) else 3
+    del d_off, d_colptr, d_rows, d_low, d_ess, h_off, h_colptr, h_rows, h_low
+    torch.cuda.empty_cache()
+
+    # every instance against the oracle's twist, regenerated in the workers
+    # (all host cores; nothing on the GPU meanwhile)
+    log("batch: oracle over every instance")
+    order = np.argsort(-np.diff(col_off))  # largest first, for an even finish
+    chunks = [[(int(b), int(npts[b]), int(seeds[b])) for b in order[i:i + 4]] for i in range(0, count, 4)]
+    t0 = time.perf_counter()
+    oracle_bad, twist_s = [], 0.0
+    for res in pool.imap_unordered(_job_batch_oracle, chunks):
+        for b, low, ess, secs in res:
+            twist_s += secs
+            c0, c1 = int(col_off[b]), int(col_off[b + 1])
+            if not (np.array_equal(low, low_batch[c0:c1]) and np.array_equal(ess, ess_batch[c0:c1])):
+                oracle_bad.append(b)
+    oracle_wall = time.perf_counter() - t0
+    return {
+        "metric": "complexes/s", "value": count * args.steps / batch_s, "unit": "complexes/s",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * batch_s / args.steps,
+        "config": {"workload": f"rips_mixed_batch_{count}", "total_m": total_m, "total_nnz": total_nnz,
+                   "points": [BATCH["lo"], BATCH["hi"]], "seed": BATCH["seed"], "algorithm": "pms",
+                   "l2": "inputs (%.1f GB) larger than L2" % ((total_nnz * 4 + total_m * 8) / 1e9)},
+        "plain_sequential": {"complexes_per_s": count / seq_s, "s_total": seq_s,
+                             "api": "oph_reduce_device, one complex at a time, device-resident inputs"},
+        "batched_over_plain": (count * args.steps / batch_s) / (count / seq_s),
+        "e2e": {"value": count * args.steps / e2e_s, "unit": "complexes/s",
+                "h2d_bytes_per_step": 8 * (count + 1) + 8 * (total_m + 1) + 4 * total_nnz,
+                "d2h_bytes_per_step": 4 * total_m, "ms_per_step": 1e3 * e2e_s / args.steps,
+                "api": "oph_reduce_batch C ABI", "equal_to_device_run": e2e_equal},
+        "cpu_baseline": {"value": count / (twist_s / cores), "unit": "complexes/s", "cores": cores, "kind": "port",
+                         "sample": f"all {count} instances through the oracle's twist (the reference's twist "
+                                   f"restated on adaptive columns), one instance per process on {host_cpu()}: "
+                                   f"{twist_s:.1f} core-seconds of twist, {oracle_wall:.1f} s wall"},
+        "cols_per_s": total_m * args.steps / batch_s,
+        "matrix_reduced": "anti-transpose D' (OPH_DUAL_AUTO)" if info["dual"] else "D",
+        "sweeps": info["sweeps"], "device_additions": info["additions"], "regrows": info["regrows"],
+        "pool_bytes": info["pool_bytes"],
+        "parity": {"batched_equals_one_at_a_time": mismatches == 0, "mismatched_instances": mismatches,
+                   "oracle_checked": count, "oracle_equal": not oracle_bad, "oracle_mismatches": oracle_bad[:20]},
+        "generation_s": gen_s, "clocks": clocks.summary(), "gpu_launches": launches,
+    }
 
 
-SERVE = {"requests": 160, "m_lo": 1_000, "m_hi": 2_000_000, "seed": 5, "budget_bytes": 150 * (1 << 30),
-         "rates_x_plain": [0.5, 1, 2, 4, 8, 16, 32]}
-
-
-def _serve_request(args):
-    """One request of the serving stream: (kind, target m, seed) -> CSC."""
-    kind, m, seed = args
-    from openph_gb300 import complexes as cx
-    if kind == "rips_cube":
-        n = max(4, int(round((6 * m) ** (1 / 3))))
-        bm = cx.rips_cube(n, seed=seed)
-    elif kind == "rips_torus":
-        bm = cx.rips_torus(400, m, seed=seed)
-    else:
-        side = max(4, int(round((m / 6) ** 0.5)))
-        bm = cx.lower_star_image(side, side, seed=seed)
-    return kind, bm.colptr, bm.rows
-
-
-def serve_stream(count, seed):
+# --------------------------------------------------------------- serve
+def serve_jobs(count, seed):
     """Request mix: sizes log-uniform in [m_lo, m_hi], kind uniform over the
-    three generator families, fresh seeds; generated on all host cores."""
-    import concurrent.futures as cf
-    import multiprocessing as mp
+    three generator families, fresh seeds."""
     rng = np.random.default_rng(seed)
     ms = np.exp(rng.uniform(np.log(SERVE["m_lo"]), np.log(SERVE["m_hi"]), size=count)).astype(np.int64)
     kinds = rng.choice(["rips_cube", "rips_torus", "lower_star"], size=count)
     seeds = rng.integers(1 << 30, size=count)
-    jobs = [(str(k), int(m), int(sd)) for k, m, sd in zip(kinds, ms, seeds)]
-    with cf.ProcessPoolExecutor(max_workers=os.cpu_count(), mp_context=mp.get_context("spawn")) as ex:
-        out = list(ex.map(_serve_request, jobs, chunksize=1))
-    from openph_gb300.complexes import BoundaryMatrix
-    return [(k, BoundaryMatrix(cp, rw)) for k, cp, rw in out]
+    return [(str(k), int(m), int(sd)) for k, m, sd in zip(kinds, ms, seeds)]
 
 
-def run_serve(args, ws, rank, local):
+def run_serve(args, local, pool, cores, count, reqs_async):
     """Serving: a Poisson stream of reduction requests through the
     continuous-batching server (HBM budget 150 GB), rates swept to
     saturation; against plain pms one request at a time on the same GPU
-    (host CSC in, host lows out, like the server)."""
-    reqs = serve_stream(args.count or SERVE["requests"], SERVE["seed"])  # before any CUDA use
+    (host CSC in, host lows out, like the server); every request checked
+    against plain pms and the oracle's twist."""
     import torch
 
-    import oracle
     from openph_gb300 import api
-    torch.cuda.set_device(local)
+    from openph_gb300.complexes import BoundaryMatrix
+    jobs = serve_jobs(count, SERVE["seed"])
+    reqs = [(k, BoundaryMatrix(cp, rw)) for k, cp, rw in reqs_async.get()]
     n = len(reqs)
     total_m = sum(bm.m for _, bm in reqs)
+    log(f"serve: {n} requests, {total_m} columns")
+    torch.cuda.set_device(local)
     # plain: one at a time, service time of each
     ctx = api.Context(local)
     for _, bm in reqs[:3]:
         ctx.reduce(bm, "pms")
-    service, plain_low = [], []
-    for _, bm in reqs:
-        t0 = time.perf_counter()
-        low, _, _ = ctx.reduce(bm, "pms")
-        service.append(time.perf_counter() - t0)
-        plain_low.append(low)
+    service, plain_low, plain_ess = [], [], []
+    with ClockSampler(local) as clocks_plain:
+        for _, bm in reqs:
+            t0 = time.perf_counter()
+            low, ess, _ = ctx.reduce(bm, "pms")
+            service.append(time.perf_counter() - t0)
+            plain_low.append(low)
+            plain_ess.append(ess)
     ctx.close()
     service = np.array(service)
     plain_rate = n / service.sum()
@@ -710,72 +757,172 @@ def run_serve(args, ws, rank, local):
         srv.wait(srv.submit(bm))
     rng = np.random.default_rng(SERVE["seed"] + 1)
     results, mism = [], 0
-    for x in SERVE["rates_x_plain"]:
-        rate = x * plain_rate
-        gaps = rng.exponential(1.0 / rate, size=n)
-        arrivals = np.cumsum(gaps)
-        tickets = [None] * n
-        t_start = time.perf_counter()
+    with ClockSampler(local) as clocks:
+        for x in SERVE["rates_x_plain"]:
+            rate = x * plain_rate
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+            tickets = [None] * n
+            t_start = time.perf_counter()
 
-        def producer():
-            for k, (_, bm) in enumerate(reqs):
-                delay = arrivals[k] - (time.perf_counter() - t_start)
-                if delay > 0:
-                    time.sleep(delay)
-                tickets[k] = srv.submit(bm)
+            def producer():
+                for k, (_, bm) in enumerate(reqs):
+                    delay = arrivals[k] - (time.perf_counter() - t_start)
+                    if delay > 0:
+                        time.sleep(delay)
+                    tickets[k] = srv.submit(bm)
 
-        th = threading.Thread(target=producer)
-        th.start()
-        lat, done_ms, sub_ms = [], [], []
-        for k in range(n):
-            while tickets[k] is None:
-                time.sleep(0.0002)
-            low, _, info = srv.wait(tickets[k])
-            lat.append(info["latency_ms"])
-            done_ms.append(info["done_ms"])
-            sub_ms.append(info["submit_ms"])
-            if not np.array_equal(low, plain_low[k]):
-                mism += 1
-        th.join()
-        span_s = (max(done_ms) - min(sub_ms)) / 1e3
-        # plain pms at the same arrivals: a FIFO single server with the
-        # measured service times
-        fin, plat = 0.0, []
-        for k in range(n):
-            fin = max(fin, arrivals[k]) + service[k]
-            plat.append(1e3 * (fin - arrivals[k]))
-        results.append({"offered_per_s": rate, "served_per_s": n / span_s,
-                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                        "plain_p50_ms": float(np.percentile(plat, 50)), "plain_p99_ms": float(np.percentile(plat, 99)),
-                        "plain_served_per_s": n / max(fin, arrivals[-1])})
+            th = threading.Thread(target=producer)
+            th.start()
+            lat, done_ms, sub_ms = [], [], []
+            for k in range(n):
+                while tickets[k] is None:
+                    time.sleep(0.0002)
+                low, ess, info = srv.wait(tickets[k])
+                lat.append(info["latency_ms"])
+                done_ms.append(info["done_ms"])
+                sub_ms.append(info["submit_ms"])
+                if not (np.array_equal(low, plain_low[k]) and np.array_equal(ess, plain_ess[k])):
+                    mism += 1
+            th.join()
+            span_s = (max(done_ms) - min(sub_ms)) / 1e3
+            # plain pms at the same arrivals: a FIFO single server with the
+            # measured service times
+            fin, plat = 0.0, []
+            for k in range(n):
+                fin = max(fin, arrivals[k]) + service[k]
+                plat.append(1e3 * (fin - arrivals[k]))
+            results.append({"offered_per_s": rate, "served_per_s": n / span_s,
+                            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                            "plain_p50_ms": float(np.percentile(plat, 50)),
+                            "plain_p99_ms": float(np.percentile(plat, 99)),
+                            "plain_served_per_s": n / max(fin, arrivals[-1])})
     counters = srv.stats()
     srv.close()
-    # oracle on the smallest requests (the rest are checked against plain pms)
-    order = np.argsort([bm.m for _, bm in reqs])[:16]
-    oracle_ok = all(np.array_equal(oracle.twist(reqs[i][1])[0], plain_low[i]) for i in order)
+    torch.cuda.empty_cache()
+
+    # every request against the oracle's twist (regenerated in the workers)
+    log("serve: oracle over every request")
+    t0 = time.perf_counter()
+    oracle_bad, twist_s = [], 0.0
+    order = np.argsort([-bm.m for _, bm in reqs])
+    for k, low, ess, secs in pool.imap_unordered(_job_serve_oracle, [(int(k),) + jobs[k] for k in order]):
+        twist_s += secs
+        if not (np.array_equal(low, plain_low[k]) and np.array_equal(ess, plain_ess[k])):
+            oracle_bad.append(k)
+    oracle_wall = time.perf_counter() - t0
     best = max(results, key=lambda r: r["served_per_s"])
-    line = {
-        "metric": "complexes/s", "value": best["served_per_s"], "unit": "complexes/s", "n_gpus": ws,
-        "steps": len(results), "warmup": 3, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators, fresh seeds per request)",
+    return {
+        "metric": "complexes/s", "value": best["served_per_s"], "unit": "complexes/s",
+        "rates": len(results),
         "config": {"workload": "serving_poisson_stream", "requests": n, "total_m": total_m,
                    "m_range": [SERVE["m_lo"], SERVE["m_hi"]], "budget_gb": SERVE["budget_bytes"] / (1 << 30),
-                   "kinds": sorted({k for k, _ in reqs})},
-        "plain_sequential": {"complexes_per_s": plain_rate, "mean_service_ms": 1e3 * service.mean()},
+                   "kinds": sorted({k for k, _ in reqs}), "seed": SERVE["seed"]},
+        "plain_sequential": {"complexes_per_s": plain_rate, "mean_service_ms": 1e3 * service.mean(),
+                             "api": "oph_reduce (host CSC in, host low/ess out), one request at a time",
+                             "clocks": clocks_plain.summary()},
         "served_over_plain_at_saturation": best["served_per_s"] / plain_rate,
         "p50_ms_at_saturation": best["p50_ms"], "p99_ms_at_saturation": best["p99_ms"],
         "rate_sweep": results, "server": counters,
         "e2e": {"value": best["served_per_s"], "unit": "complexes/s",
                 "h2d_bytes_per_step": int(np.mean([8 * (bm.m + 1) + 4 * bm.nnz for _, bm in reqs])),
                 "d2h_bytes_per_step": int(np.mean([8 * bm.m for _, bm in reqs])),
-                "api": "oph_server_submit / oph_server_wait (host CSC in, host lows and ess out; a step = one request)"},
-        "cpu_baseline": cpu_pool_sample(((bm.colptr, bm.rows) for _, bm in reqs), CPU_SAMPLE_SECONDS,
-                                        "requests of the stream"),
-        "parity": {"served_equals_plain": mism == 0, "mismatches": mism, "oracle_checked_smallest": len(order),
-                   "oracle_equal": bool(oracle_ok)},
+                "api": "oph_server_submit / oph_server_wait (host CSC in, host lows and ess out; a step = one "
+                       "request)"},
+        "cpu_baseline": {"value": n / (twist_s / cores), "unit": "complexes/s", "cores": cores, "kind": "port",
+                         "sample": f"all {n} requests through the oracle's twist, one request per process on "
+                                   f"{host_cpu()}: {twist_s:.1f} core-seconds of twist, {oracle_wall:.1f} s wall"},
+        "parity": {"served_equals_plain": mism == 0, "mismatches": mism, "oracle_checked": n,
+                   "oracle_equal": not oracle_bad, "oracle_mismatches": oracle_bad[:20]},
+        "clocks": clocks.summary(),
     }
+
+
+# ---------------------------------------------------------------- main
+def run_ours(args, ws, rank, local):
+    # the worker pool first: spawned before this process touches CUDA
+    pool, cores = (start_pool() if rank == 0 else (None, 0))
+    bm = make_workload()
+    m = bm.m
+    torus_jobs = None
+    if rank == 0 and args.workload in ("all", "torus"):
+        # the oracle's twist (parity, algorithmic bytes) and one whole
+        # reduction by the fixed-slot port (the CPU baseline), each on one
+        # core, beside the torus timing
+        torus_jobs = (pool.apply_async(_job_twist_full, ((bm.colptr, bm.rows),)),
+                      pool.apply_async(_job_fixed_full, ((bm.colptr, bm.rows, COL_WIDTH),)))
+    import torch
+
+    from openph_gb300 import api
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    dist = init_dist(ws, "nccl")
+    api.lib()
+
+    line, outs = None, None
+    if args.workload in ("all", "torus"):
+        log("torus: GPU timing")
+        line, outs = run_torus(args, ws, rank, local, bm, dist)
+    if rank != 0:
+        barrier(dist, device)
+        return 0
+    ok = True
+    if line is None:
+        # a batch-only or serve-only run: that object becomes the line
+        line = {"n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded generators)"}
+    serve_async = None
+    if args.workload in ("all", "serve"):
+        # request generation on the pool (CPU only), while the batch runs
+        serve_async = pool.map_async(_job_serve_request, serve_jobs(args.count or SERVE["requests"], SERVE["seed"]),
+                                     chunksize=1)
+    if args.workload in ("all", "batch"):
+        batch = run_batch(args, local, pool, cores, args.count or BATCH["count"],
+                          serve_async.wait if serve_async is not None else None)
+        ok &= batch["parity"]["batched_equals_one_at_a_time"] and batch["parity"]["oracle_equal"]
+        if args.workload == "batch":
+            line.update(batch)
+        else:
+            line["batch"] = batch
+    if torus_jobs is not None:
+        low_o, ess_o, st = torus_jobs[0].get()
+        fixed = torus_jobs[1].get()
+        low_gpu, ess_gpu, low_e2e, ess_e2e = outs
+        parity = bool(np.array_equal(low_gpu, low_o) and np.array_equal(ess_gpu, ess_o))
+        parity_e2e = bool(np.array_equal(low_e2e, low_o + 1) and np.array_equal(ess_e2e, ess_o))
+        ok &= parity and parity_e2e
+        ab = algorithmic_bytes(bm, st)
+        step_s = line["ms_per_step"] / 1e3
+        line["cpu_baseline"] = {
+            "value": m / fixed["seconds"], "unit": "cols/s", "cores": 1, "kind": "port",
+            "sample": f"one whole reduction of the same matrix ({fixed['columns']} columns reduced, "
+                      f"{fixed['additions']} additions) by the fixed-slot port of the reference's twist "
+                      f"(col_width {fixed['col_width']}), {fixed['seconds']:.1f} s on one core of {host_cpu()}",
+            "adaptive_restatement_s": st["seconds"]}
+        line["parity"] = {"low_ess_equal_oracle": parity, "e2e_low_ess_equal_oracle": parity_e2e,
+                          "cpu_baseline_low_equal_oracle": fixed["low_checksum"] == low_checksum(low_o)}
+        line["twist_additions_on_d"] = st["additions"]
+        line["roofline"]["twist_on_d_algorithmic_bytes_per_reduction"] = ab["additions"]
+        # the reduction-level figure of the algorithmic byte count: D's twist
+        # work (the reference's) over the time this library takes for the
+        # whole reduction; above 1 on the anti-transpose, which skips that work
+        line["reduction_bytes"] = {
+            "bytes_per_reduction": ab["total"], "per_s_gbs": ab["total"] / step_s / 1e9,
+            "frac_of_peak": ab["total"] / step_s / 1e9 / line["roofline"]["peak"],
+            "definition": "4 (nnz + m + 1) + 4 m + 4 (|P| + |T| + |T xor P|) over the CPU twist's additions on "
+                          "D, per reduction; not a bandwidth achieved (the anti-transpose avoids that work)"}
+    if serve_async is not None:
+        serve = run_serve(args, local, pool, cores, args.count or SERVE["requests"], serve_async)
+        ok &= serve["parity"]["served_equals_plain"] and serve["parity"]["oracle_equal"]
+        if args.workload == "serve":
+            line.update(serve)
+        else:
+            line["serve"] = serve
+    pool.close()
+    pool.join()
     print(json.dumps(line), flush=True)
-    return 0 if (mism == 0 and oracle_ok) else 3
+    if dist is not None:
+        barrier(dist, device)
+    return 0 if ok else 3
 
 
 def main():
@@ -784,18 +931,17 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["torus", "batch", "serve"], default="torus",
-                    help="torus: the ~5M-column complex (the headline); batch: 4096 complexes in one pass; "
-                         "serve: a Poisson request stream through the continuous-batching server")
+    ap.add_argument("--workload", choices=["all", "torus", "batch", "serve"], default="all",
+                    help="all: the torus headline with the batch and serve objects; torus: the ~5M-column "
+                         "complex alone; batch: 4096 complexes in one pass; serve: a Poisson request stream "
+                         "through the continuous-batching server")
     ap.add_argument("--count", type=int, default=0, help="batch/serve: number of complexes / requests")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
-    if args.workload == "batch":
-        return run_batch(args, ws, rank, local)
-    if args.workload == "serve":
-        return run_serve(args, ws, rank, local)
+    if ws > 1 and args.workload == "all":
+        args.workload = "torus"  # replicas of the headline; the batch and serve objects are 1-GPU runs
     return run_ours(args, ws, rank, local)
 
 

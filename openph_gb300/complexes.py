@@ -312,8 +312,19 @@ def rips_mixed_batch(count: int = 4096, seed: int = 4, threads: int | None = Non
     counts uniform in [lo, hi], half uniform in the cube and half on a noisy
     circle (by instance seed parity).  Returns (col_off, colptr, rows_local,
     n_points, seeds) ready for Context.reduce_batch_packed."""
-    import os
     n, seeds = mixed_batch_sizes(count, seed, lo, hi)
+    col_off, colptr, rows = rips_mixed_instances(n, seeds, threads)
+    return col_off, colptr, rows, n, seeds
+
+
+def rips_mixed_instances(n_points, seeds, threads: int | None = None):
+    """Instances of the batched mix for explicit point counts and instance
+    seeds (instance b of rips_mixed_batch is rips_mixed_instances([n[b]],
+    [seeds[b]])).  Returns (col_off, colptr, rows_local)."""
+    import os
+    n = np.ascontiguousarray(n_points, dtype=np.int32)
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    count = int(n.shape[0])
     col_off = np.zeros(count + 1, np.int64)
     cx = _Complex()
     nt = threads or os.cpu_count() or 1
@@ -323,7 +334,7 @@ def rips_mixed_batch(count: int = 4096, seed: int = 4, threads: int | None = Non
     colptr = np.ctypeslib.as_array(cx.colptr, shape=(m + 1,)).copy()
     rows = np.ctypeslib.as_array(cx.rows, shape=(max(nnz, 1),))[:nnz].copy()
     _lib().oph_complex_free(C.byref(cx))
-    return col_off, colptr, rows, n, seeds
+    return col_off, colptr, rows
 
 
 def batch_instance(col_off, colptr, rows, b: int) -> BoundaryMatrix:
