@@ -342,6 +342,7 @@ __attribute__((visibility("default"))) int oph_context_destroy(oph_context *ctx)
     for (int i = 0; i < ctx->pev_n; i++) cudaEventDestroy(ctx->pev[i]);
     free(ctx->pev);
     if (ctx->sweep_graph) cudaGraphExecDestroy(ctx->sweep_graph);
+    if (ctx->loop_graph) cudaGraphExecDestroy(ctx->loop_graph);
     if (ctx->h_status) cudaFreeHost(ctx->h_status);
     cudaStreamDestroy(ctx->stream);
     delete ctx;

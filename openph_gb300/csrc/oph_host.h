@@ -131,6 +131,12 @@ struct Context {
     // launch arguments it was captured with
     cudaGraphExec_t sweep_graph = nullptr;
     std::vector<unsigned char> sweep_key;
+    // the whole sweep loop as one graph: a conditional WHILE node whose body
+    // runs two sweeps and sets the loop condition from the device status
+    // (converged, overflow, error, sweep cap), so the host waits once per
+    // reduction instead of once per batch of sweeps; loop_key as sweep_key
+    cudaGraphExec_t loop_graph = nullptr;
+    std::vector<unsigned char> loop_key;
 };
 
 // buffer slots of Context::bufs

@@ -1648,6 +1648,70 @@ static bool sweep_pair_graph(Context *ctx, const PmsArgs &a, const SweepGrids &g
     return true;
 }
 
+// The loop condition of the sweep-loop graph: another pair of sweeps while
+// the reduction has not converged, no column store allocation failed, no
+// error was raised and the sweep cap is not reached.
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, const DevStatus *st, int cap) {
+    const bool more = !st->converged && !st->overflow && !st->error && st->sweeps < cap;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// The whole sweep loop as one graph (a conditional WHILE node around two
+// sweeps and k_loop_cond), built on first use and again whenever an argument
+// changes.  Returns false, with nothing left built, when the driver refuses
+// any step; the caller then runs the host loop.
+static bool sweep_loop_graph(Context *ctx, const PmsArgs &a, const SweepGrids &g, int cap) {
+    std::vector<unsigned char> key(sizeof(PmsArgs) + sizeof(SweepGrids) + sizeof(int));
+    memcpy(key.data(), &a, sizeof(PmsArgs));
+    memcpy(key.data() + sizeof(PmsArgs), &g, sizeof(SweepGrids));
+    memcpy(key.data() + sizeof(PmsArgs) + sizeof(SweepGrids), &cap, sizeof(int));
+    if (ctx->loop_graph && key == ctx->loop_key) return true;
+    if (ctx->loop_graph) {
+        cudaGraphExecDestroy(ctx->loop_graph);
+        ctx->loop_graph = nullptr;
+    }
+    cudaStream_t s = ctx->stream;
+    cudaGraph_t graph = nullptr;
+    if (cudaGraphCreate(&graph, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    bool ok = false;
+    do {
+        cudaGraphConditionalHandle h;
+        // the body runs at least once per launch (the handle starts at 1)
+        if (cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) break;
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &p) != cudaSuccess) break;
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        if (cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+            cudaSuccess)
+            break;
+        launch_sweep_ev(a, g, s, nullptr, 0);
+        launch_sweep_ev(a, g, s, nullptr, 1);
+        k_loop_cond<<<1, 1, 0, s>>>(h, a.st, cap);
+        cudaGraph_t captured = nullptr;
+        if (cudaStreamEndCapture(s, &captured) != cudaSuccess) break;
+        if (cudaGraphInstantiate(&ctx->loop_graph, graph, 0) != cudaSuccess) {
+            ctx->loop_graph = nullptr;
+            break;
+        }
+        ok = true;
+    } while (0);
+    cudaGraphDestroy(graph);
+    if (!ok) {
+        cudaGetLastError();
+        return false;
+    }
+    ctx->loop_key = std::move(key);
+    return true;
+}
+
 int run_pms(Context *ctx, Work &w, oph_info *info) {
     const int64_t m = w.m;
     PmsArgs a{};
@@ -1726,7 +1790,34 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     DevStatus hs{};
     float p2_ms = 0, p2w_ms = 0, p1_ms = 0, wt_ms[3] = {0, 0, 0};
     int p2_launches = 0, regrows = 0;
-    for (;;) {
+    // the device-resident loop: one graph launch runs sweeps until the
+    // reduction converges (or a column store allocation fails, or the cap),
+    // one status read per launch
+    static const bool loop_on = !getenv("OPH_HOST_LOOP");
+    while (OPH_GRAPHS && loop_on && !timed && sweep_loop_graph(ctx, a, g, max_sweeps)) {
+        OPH_CUDA_TRY(cudaGraphLaunch(ctx->loop_graph, s));
+        OPH_CUDA_TRY(cudaMemcpyAsync(ctx->h_status, w.st, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+        OPH_CUDA_TRY(cudaStreamSynchronize(s));
+        const int before = sweeps_launched;
+        hs = *ctx->h_status;
+        // every pair the body ran: the sweeps counted plus the one that
+        // found convergence, rounded up to pairs
+        const int pairs = std::max(1, (hs.sweeps - before + 2) / 2);
+        sweeps_launched = std::max(hs.sweeps, before + 2 * pairs);
+        ctx->launches += pairs * (2 * kernels_per_sweep(a) + 1);
+        if (hs.error) { rc = OPH_ERR_BAD_INPUT; break; }
+        if (hs.overflow) {
+            int gr = grow_pool(ctx, w);
+            if (gr != OPH_OK) { rc = gr; break; }
+            a.pool = w.pool;
+            regrows++;
+            if (hs.converged) break;
+            continue;
+        }
+        if (hs.converged) break;
+        if (hs.sweeps >= max_sweeps) { rc = OPH_ERR_TIMEOUT; break; }
+    }
+    for (; !hs.converged && rc == OPH_OK;) {
         const int nb = std::min(batch, max_sweeps - sweeps_launched);
         DevStatus before = hs;
         int b = 0;
