@@ -230,12 +230,15 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
         if (bad) return OPH_ERR_BAD_INPUT;
     }
     Work wd;
-    if (dual && (rc = dual_build(ctx, w, wd))) return rc;
+    if (dual) {
+        // D' built straight into its column store, with its buckets, left[]
+        // and beta
+        if ((rc = dual_setup(ctx, w, wd))) return rc;
+    } else {
+        if ((rc = setup_store(ctx, w, pms))) return rc;
+        ctx->launches += pms ? 3 : 1;
+    }
     Work &wr = dual ? wd : w;
-    rc = setup_store(ctx, wr, pms);
-    if (rc) return rc;
-    ctx->launches += pms ? 3 : 1;
-    if (dual) dual_dims(ctx, w, wd);
     if (ctx->profile) {
         cudaEventRecord(ctx->ev[3], s);
         cudaEventSynchronize(ctx->ev[3]);

@@ -26,7 +26,26 @@
 // buckets take them from distinct buckets; k_dual_grade checks that on the
 // device, together with the structural checks of the set-up, and a matrix
 // that fails stays on D.
-#include <cub/device/device_radix_sort.cuh>
+//
+// The transpose is built straight into the column store of D', without a
+// general sort (the reference's analogue is the slot-store build create_rows_mp,
+// src/cuda/kernels.cu:25-38):
+//   count    cnt[c] = entries of D' column c (the entries of D in row m-1-c)
+//   scan     the column offsets of D', an exclusive prefix sum of cnt (tile
+//            sums, their scan, then the tiles)
+//   scatter  every entry (r, j) of D writes row m-1-j of D' column m-1-r
+//            into a slot taken from a per-column cursor counting down from
+//            cnt[c]; D's columns are visited in roughly ascending j, so the
+//            slots fill from the top down and the rows land nearly ascending
+//   finish   a warp per column of D': its rows sorted ascending (a bitonic
+//            network across the lanes for <= 32 rows, in shared memory for
+//            <= 1024; longer columns are queued), the segment header, low,
+//            and the bucket of D's column in the reversed position
+//   long     a CTA per queued column: LSD radix sort, 8-bit digits, through
+//            a scratch range at the column's own offsets
+//   records  per row of D': its pivot record reset with left[] (row m-1-j of
+//            D' first appears in column m-1-low_D(j)) and beta by atomicMax
+#include <climits>
 
 #include "oph_host.h"
 
@@ -103,48 +122,318 @@ __global__ void k_dual_buckets(const int64_t *__restrict__ colptr, int64_t m, in
         bucket[j] = (int8_t)bucket_of(colptr[j + 1] - colptr[j]);
 }
 
-// left of D' without atomics: row m-1-j of D' first appears in column
-// m-1-low_D(j) (the largest row of D's column j), for every nonempty j.
-__global__ void k_dual_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                            PivRec *__restrict__ rec) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t b = colptr[j + 1];
-        if (b > colptr[j]) rec[m - 1 - j].left = (int)(m - 1 - rows[b - 1]);
+// ------------------------------------------------------------- transpose
+constexpr int SCAN_THREADS = 1024, SCAN_ITEMS = 4, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Sum of v over the block (every thread gets it); red holds 33 partials.
+__device__ __forceinline__ long long block_sum(long long v, long long *red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        long long t = lane < nw ? red[lane] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) red[32] = t;
     }
+    __syncthreads();
+    const long long total = red[32];
+    __syncthreads();
+    return total;
 }
 
-
-// Sort keys of D': entry k of D (row r, column j) becomes key m-1-r (its
-// column in D'), value m-1-j (its row), written at nnz-1-k so that a stable
-// sort by key leaves the rows of each column of D' ascending.
-__global__ void k_dual_keys(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                            int64_t nnz, uint32_t *__restrict__ key, int32_t *__restrict__ val) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
-        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) {
-            key[nnz - 1 - k] = (uint32_t)(m - 1 - rows[k]);
-            val[nnz - 1 - k] = (int32_t)(m - 1 - j);
+// Exclusive prefix of v over the block; red holds 33 partials.
+__device__ __forceinline__ long long block_exclusive(long long v, long long *red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    long long incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
+    }
+    if (lane == 31) red[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const long long t = lane < nw ? red[lane] : 0;
+        long long ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += u;
         }
+        if (lane < nw) red[lane] = ti - t;  // exclusive prefix of the warp totals
+    }
+    __syncthreads();
+    const long long out = red[wid] + incl - v;
+    __syncthreads();
+    return out;
 }
 
-// colptr of D' from the sorted keys (each column's first entry writes the
-// pointers of the empty columns before it).
-__global__ void k_dual_colptr(const uint32_t *__restrict__ key, int64_t nnz, int64_t m, int64_t *__restrict__ colptr) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = key[k];
-        const int64_t pc = k > 0 ? (int64_t)key[k - 1] : -1;
-        if (pc != c)
-            for (int64_t q = pc + 1; q <= c; q++) colptr[q] = k;
-        if (k == nnz - 1)
-            for (int64_t q = c + 1; q <= m; q++) colptr[q] = nnz;
+__device__ __forceinline__ void load_items(const int *__restrict__ cnt, int64_t n, int64_t base, int *v) {
+    if (base + SCAN_ITEMS <= n) {
+        const int4 q = *reinterpret_cast<const int4 *>(cnt + base);
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+        v[3] = q.w;
+    } else {
+#pragma unroll
+        for (int t = 0; t < SCAN_ITEMS; t++) v[t] = base + t < n ? cnt[base + t] : 0;
     }
 }
 
-// The buckets of D' (those of D, reversed), over the ones the set-up derived
-// from D' itself.
-__global__ void k_dual_dims(const int64_t *__restrict__ colptr, int64_t m, int8_t *__restrict__ dim) {
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < m; c += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = m - 1 - c;
-        dim[c] = (int8_t)bucket_of(colptr[i + 1] - colptr[i]);
+// (scan 1) the sum of every tile of SCAN_TILE counts
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_sums(const int *__restrict__ cnt, int64_t n,
+                                                            long long *__restrict__ tsum) {
+    __shared__ long long red[33];
+    for (int64_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) {
+        int v[SCAN_ITEMS];
+        load_items(cnt, n, t * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS, v);
+        const long long total = block_sum((long long)v[0] + v[1] + v[2] + v[3], red);
+        if (threadIdx.x == 0) tsum[t] = total;
+    }
+}
+
+// (scan 2) exclusive prefix of the tile sums in place (one block); the grand
+// total into *total
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tsums(long long *__restrict__ tsum, int64_t ntiles,
+                                                             int64_t *__restrict__ total) {
+    __shared__ long long red[33];
+    long long carry = 0;
+    for (int64_t b0 = 0; b0 < ntiles; b0 += SCAN_THREADS) {
+        const int64_t t = b0 + threadIdx.x;
+        const long long v = t < ntiles ? tsum[t] : 0;
+        const long long ex = block_exclusive(v, red);
+        if (t < ntiles) tsum[t] = carry + ex;
+        carry += block_sum(v, red);
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// (scan 3) the offsets: out[i] = sum of cnt[0 .. i)
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int *__restrict__ cnt, int64_t n,
+                                                             const long long *__restrict__ tsum,
+                                                             int64_t *__restrict__ out) {
+    __shared__ long long red[33];
+    for (int64_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) {
+        const int64_t base = t * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        load_items(cnt, n, base, v);
+        long long run = tsum[t] + block_exclusive((long long)v[0] + v[1] + v[2] + v[3], red);
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS; q++) {
+            if (base + q < n) out[base + q] = run;
+            run += v[q];
+        }
+    }
+}
+
+// entries of every column of D' (= entries of D in each row)
+__global__ void k_dual_count(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                             int *__restrict__ cnt) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
+        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) atomicAdd(&cnt[m - 1 - rows[k]], 1);
+}
+
+// Segment of column c of a store whose column offsets are `off` (the layout
+// of k_setup_columns: room for the header, capacities in 16-byte units).
+__device__ __forceinline__ int64_t seg_start(int64_t c, int64_t off) { return 8 * c + 4 * ((off + 3) >> 2); }
+
+// every entry of D into its column of D' (row m-1-j), slots from the top
+__global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                               const int64_t *__restrict__ dcolptr, int *__restrict__ cursor,
+                               int *__restrict__ pool) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        const int val = (int)(m - 1 - j);
+        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) {
+            const int64_t c = m - 1 - rows[k];
+            const int pos = atomicSub(&cursor[c], 1) - 1;
+            pool[seg_start(c, dcolptr[c]) + SEG_HDR + pos] = val;
+        }
+    }
+}
+
+// Ascending order of one value per lane (a bitonic network across the warp).
+__device__ __forceinline__ int warp_sort32(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1)
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const int o = __shfl_xor_sync(0xffffffffu, v, stride);
+            const bool up = (lane & size) == 0, lower = (lane & stride) == 0;
+            v = (lower == up) ? min(v, o) : max(v, o);
+        }
+    return v;
+}
+
+constexpr int FIN_WARPS = 8, LONG_COL = 1024;
+
+// a warp per column of D': rows sorted, header, low, bucket
+__global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish(const int64_t *__restrict__ dcolptr,
+                                                                const int64_t *__restrict__ colptr, int64_t m,
+                                                                int *__restrict__ pool, int64_t *__restrict__ seg,
+                                                                int32_t *__restrict__ low, int8_t *__restrict__ dim,
+                                                                int *__restrict__ long_list, int *long_count) {
+    __shared__ int sbuf[FIN_WARPS][LONG_COL];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * FIN_WARPS;
+    int *B = sbuf[wid];
+    for (int64_t c = blockIdx.x * (int64_t)FIN_WARPS + wid; c < m; c += nwarps) {
+        const int64_t a = dcolptr[c], b = dcolptr[c + 1];
+        const int n = (int)(b - a);
+        const int64_t s = seg_start(c, a), e = seg_start(c + 1, b);
+        int *R = pool + s + SEG_HDR;
+        int lowv = -1;
+        if (n <= 32) {
+            int v = lane < n ? R[lane] : INT_MAX;
+            v = warp_sort32(v);
+            if (lane < n) R[lane] = v;
+            if (n > 0) lowv = __shfl_sync(0xffffffffu, v, n - 1);
+        } else if (n <= LONG_COL) {
+            bool sorted = true;
+            for (int k = lane; k + 1 < n; k += 32) sorted &= R[k] < R[k + 1];
+            if (__all_sync(0xffffffffu, sorted)) {
+                lowv = R[n - 1];
+            } else {
+                int N = 64;
+                while (N < n) N <<= 1;
+                for (int k = lane; k < N; k += 32) B[k] = k < n ? R[k] : INT_MAX;
+                __syncwarp();
+                for (int size = 2; size <= N; size <<= 1)
+                    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                        for (int i = lane; i < N; i += 32) {
+                            const int l = i ^ stride;
+                            if (l > i) {
+                                const bool up = (i & size) == 0;
+                                const int x = B[i], y = B[l];
+                                if ((x > y) == up) {
+                                    B[i] = y;
+                                    B[l] = x;
+                                }
+                            }
+                        }
+                        __syncwarp();
+                    }
+                for (int k = lane; k < n; k += 32) R[k] = B[k];
+                lowv = B[n - 1];
+                __syncwarp();  // B is reused by the warp's next column
+            }
+        } else if (lane == 0) {
+            long_list[atomicAdd(long_count, 1)] = (int)c;
+        }
+        if (lane == 0) {
+            seg[c] = s;
+            pool[s] = n;
+            pool[s + 1] = (int)(e - s - SEG_HDR);
+            pool[s + 2] = 0;
+            pool[s + 3] = 0;
+            if (n <= LONG_COL) low[c] = lowv;
+            const int64_t i = m - 1 - c;
+            const int64_t nd = colptr[i + 1] - colptr[i];
+            dim[c] = (int8_t)(nd - 1 > 126 ? 126 : nd - 1);
+        }
+    }
+}
+
+// a CTA per column of more than LONG_COL rows: LSD radix sort, 8-bit digits,
+// between the column's rows and scratch[dcolptr[c] ..] (four passes, so the
+// result ends where it began); then its low
+constexpr int LS_THREADS = 1024;
+__global__ void __launch_bounds__(LS_THREADS) k_dual_sort_long(const int64_t *__restrict__ dcolptr,
+                                                               int *__restrict__ pool, int32_t *__restrict__ low,
+                                                               const int *__restrict__ long_list,
+                                                               const int *long_count, int *long_cursor,
+                                                               int *__restrict__ scratch) {
+    __shared__ int base[256], tot[256];
+    __shared__ int wcnt[LS_THREADS / 32][256];
+    __shared__ int s_idx;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (;;) {
+        if (tid == 0) s_idx = atomicAdd(long_cursor, 1);
+        __syncthreads();
+        const int idx = s_idx;
+        __syncthreads();
+        if (idx >= *long_count) break;
+        const int64_t c = long_list[idx];
+        const int64_t a = dcolptr[c];
+        const int n = (int)(dcolptr[c + 1] - a);
+        int *R = pool + seg_start(c, a) + SEG_HDR;
+        int *src = R, *dst = scratch + a;
+        for (int shift = 0; shift < 32; shift += 8) {
+            if (tid < 256) base[tid] = 0;
+            __syncthreads();
+            for (int k = tid; k < n; k += LS_THREADS) atomicAdd(&base[(src[k] >> shift) & 255], 1);
+            __syncthreads();
+            if (tid < 32) {  // exclusive prefix of the 256 digit counts, 8 per lane
+                int v[8], sum = 0;
+                for (int q = 0; q < 8; q++) {
+                    v[q] = base[8 * tid + q];
+                    sum += v[q];
+                }
+                int incl = sum;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += u;
+                }
+                int run = incl - sum;
+                for (int q = 0; q < 8; q++) {
+                    base[8 * tid + q] = run;
+                    run += v[q];
+                }
+            }
+            __syncthreads();
+            // stable scatter, LS_THREADS elements at a time: the rank among
+            // the warp's equal digits, then among earlier warps' (counts)
+            for (int t0 = 0; t0 < n; t0 += LS_THREADS) {
+                const int k = t0 + tid;
+                const bool act = k < n;
+                const int v = act ? src[k] : 0;
+                const int d = act ? (v >> shift) & 255 : 256;
+                for (int q = tid; q < (LS_THREADS / 32) * 256; q += LS_THREADS) (&wcnt[0][0])[q] = 0;
+                __syncthreads();
+                const unsigned peers = __match_any_sync(0xffffffffu, d);
+                const int rank = __popc(peers & ((1u << lane) - 1u));
+                if (act && rank == 0) wcnt[wid][d] = __popc(peers);
+                __syncthreads();
+                if (tid < 256) {
+                    int run = 0;
+                    for (int w = 0; w < LS_THREADS / 32; w++) {
+                        const int x = wcnt[w][tid];
+                        wcnt[w][tid] = run;
+                        run += x;
+                    }
+                    tot[tid] = run;
+                }
+                __syncthreads();
+                if (act) dst[base[d] + wcnt[wid][d] + rank] = v;
+                __syncthreads();
+                if (tid < 256) base[tid] += tot[tid];
+                __syncthreads();
+            }
+            int *t = src;
+            src = dst;
+            dst = t;
+        }
+        if (tid == 0) low[c] = R[n - 1];
+        __syncthreads();
+    }
+}
+
+// per row i of D' (column j = m-1-i of D): the pivot record reset, left[i] =
+// m-1-low_D(j) (or -1 for an empty column), beta[left] = the largest row
+__global__ void k_dual_rec(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                           PivRec *__restrict__ rec, int32_t *__restrict__ beta) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = m - 1 - i;
+        const int64_t lo = colptr[j], hi = colptr[j + 1];
+        const int l = hi > lo ? (int)(m - 1 - rows[hi - 1]) : -1;
+        int4 *r = reinterpret_cast<int4 *>(rec + i);
+        r[0] = make_int4(-1, 0, l, (int)SEG4_NONE);
+        r[1] = make_int4(-1, -1, -1, -1);
+        if (l >= 0) atomicMax(&beta[l], (int)i);
     }
 }
 
@@ -164,11 +453,6 @@ __global__ void k_dual_low(const int32_t *__restrict__ low_d, int64_t m, int32_t
 static int grid_of(Context *ctx, int64_t n) {
     int64_t g = (n + 255) / 256, cap = (int64_t)ctx->sm_count * 16;
     return (int)std::max<int64_t>(1, std::min(g, cap));
-}
-
-void dual_left(Context *ctx, const Work &wd) {
-    k_dual_left<<<grid_of(ctx, wd.m), 256, 0, ctx->stream>>>(wd.src_colptr, wd.src_rows, wd.m, wd.rec);
-    ctx->launches++;
 }
 
 int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input) {
@@ -215,46 +499,50 @@ int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_inpu
     return OPH_OK;
 }
 
-int dual_build(Context *ctx, const Work &w, Work &wd) {
+int dual_setup(Context *ctx, const Work &w, Work &wd) {
     cudaStream_t s = ctx->stream;
     const int64_t m = w.m, nnz = w.nnz;
-    int64_t *colptr = (int64_t *)ctx_alloc(ctx, S_DCOLPTR, sizeof(int64_t) * (m + 1));
-    const size_t n1 = (size_t)(nnz > 0 ? nnz : 1);
-    char *kv = (char *)ctx_alloc(ctx, S_DSORT, n1 * 4 * sizeof(int32_t));
-    if (!colptr || !kv) return OPH_ERR_OOM;
-    uint32_t *k0 = (uint32_t *)kv, *k1 = k0 + n1;
-    int32_t *v0 = (int32_t *)(k1 + n1), *v1 = v0 + n1;
     wd = w;
-    wd.colptr = colptr;
     wd.ascending = true;
-    wd.src_colptr = w.colptr;
-    wd.src_rows = w.rows;
-    if (nnz == 0) {
-        OPH_CUDA_TRY(cudaMemsetAsync(colptr, 0, sizeof(int64_t) * (m + 1), s));
-        wd.rows = v0;
-        return OPH_OK;
-    }
-    k_dual_keys<<<grid_of(ctx, m), 256, 0, s>>>(w.colptr, w.rows, m, nnz, k0, v0);
-    int bits = 1;
-    while (bits < 32 && (1ll << bits) < m) bits++;
-    cub::DoubleBuffer<uint32_t> dk(k0, k1);
-    cub::DoubleBuffer<int32_t> dv(v0, v1);
-    size_t tb = 0;
-    OPH_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, dk, dv, nnz, 0, bits, s));
-    void *tmp = ctx_alloc(ctx, S_DTEMP, tb > 0 ? tb : 1);
-    if (!tmp) return OPH_ERR_OOM;
-    OPH_CUDA_TRY(cub::DeviceRadixSort::SortPairs(tmp, tb, dk, dv, nnz, 0, bits, s));
-    k_dual_colptr<<<grid_of(ctx, nnz), 256, 0, s>>>(dk.Current(), nnz, m, colptr);
-    ctx->launches += 3 + (bits + 7) / 8;
+    wd.checked = true;
+    wd.rows = nullptr;
+    int rc = init_store(ctx, wd);
+    if (rc) return rc;
+    if (m == 0) return OPH_OK;
+    int64_t *dcolptr = (int64_t *)ctx_alloc(ctx, S_DCOLPTR, sizeof(int64_t) * (m + 1));
+    // cnt (then the cursors), the long-column list, the radix sort's
+    // scratch, two counters and the scan's tile sums, in one buffer
+    const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
+    auto r256 = [](int64_t b) { return (b + 255) & ~255ll; };
+    const int64_t o_long = r256(4 * m), o_scr = o_long + r256(4 * m);
+    const int64_t o_ctr = o_scr + r256(4 * (nnz > 0 ? nnz : 1)), o_tsum = o_ctr + 256;
+    const int64_t bytes = o_tsum + 8 * (ntiles + 1);
+    char *buf = (char *)ctx_alloc(ctx, S_DSORT, (size_t)bytes);
+    if (!dcolptr || !buf) return OPH_ERR_OOM;
+    int *cnt = (int *)buf, *long_list = (int *)(buf + o_long), *scratch = (int *)(buf + o_scr);
+    int *ctr = (int *)(buf + o_ctr);
+    long long *tsum = (long long *)(buf + o_tsum);
+    wd.colptr = dcolptr;
+    OPH_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * m, s));
+    OPH_CUDA_TRY(cudaMemsetAsync(ctr, 0, 256, s));
+    OPH_CUDA_TRY(cudaMemsetAsync(wd.beta, 0xff, sizeof(int32_t) * m, s));
+    const int gm = grid_of(ctx, m);
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 2));
+    k_dual_count<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, cnt);
+    k_scan_sums<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum);
+    k_scan_tsums<<<1, SCAN_THREADS, 0, s>>>(tsum, ntiles, dcolptr + m);
+    k_scan_apply<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum, dcolptr);
+    k_dual_scatter<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, dcolptr, cnt, wd.pool);
+    const int gf =
+        (int)std::max<int64_t>(1, std::min<int64_t>((m + FIN_WARPS - 1) / FIN_WARPS, (int64_t)ctx->sm_count * 8));
+    k_dual_finish<<<gf, FIN_WARPS * 32, 0, s>>>(dcolptr, w.colptr, m, wd.pool, wd.seg, wd.low, wd.dim, long_list,
+                                                &ctr[0]);
+    k_dual_sort_long<<<ctx->sm_count, LS_THREADS, 0, s>>>(dcolptr, wd.pool, wd.low, long_list, &ctr[0], &ctr[1],
+                                                          scratch);
+    k_dual_rec<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, wd.rec, wd.beta);
+    ctx->launches += 8;
     OPH_CUDA_TRY(cudaGetLastError());
-    wd.rows = dv.Current();
-    wd.entry_col = dk.Current();
     return OPH_OK;
-}
-
-void dual_dims(Context *ctx, const Work &w, Work &wd) {
-    k_dual_dims<<<grid_of(ctx, w.m), 256, 0, ctx->stream>>>(w.colptr, w.m, wd.dim);
-    ctx->launches++;
 }
 
 int dual_lows(Context *ctx, const Work &wd, int32_t **low) {

@@ -49,15 +49,16 @@ struct Work {
     int *pool = nullptr;              // column store
     DevStatus *st = nullptr;
     bool ascending = false;           // pms: buckets in ascending order (the anti-transpose)
-    const uint32_t *entry_col = nullptr;  // nnz: column of each entry, when known (the anti-transpose)
-    const int64_t *src_colptr = nullptr;  // the anti-transpose: D's CSC, from which left[] follows
-    const int32_t *src_rows = nullptr;
     bool checked = false;             // colptr/rows already passed the structural check
 };
 
 struct Context;
 
 // setup.cu
+// init_store: the column store (pool) and a fresh status block for w;
+// setup_store: init_store, then the columns of w's CSC into the store, low,
+// dim, and with need_beta the pivot records, left[] and beta.
+int init_store(Context *ctx, Work &w);
 int setup_store(Context *ctx, Work &w, bool need_beta);
 int coo1_to_csc(Context *ctx, const int *d_rows1, const int *d_cols1, int64_t nnz, int64_t m, int64_t *d_colptr,
                 int32_t *d_rows0);
@@ -74,18 +75,17 @@ int run_pms(Context *ctx, Work &w, oph_info *info);
 int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *info);
 
 // dual.cu: pms on the anti-transpose.  dual_choose grades w's buckets and
-// decides (*bad_input: malformed CSC); dual_build writes the anti-transpose
-// into wd (wd shares w's per-column arrays); dual_dims gives wd D's buckets
-// after the set-up; dual_lows maps wd's lows back to D's.
+// decides (*bad_input: malformed CSC); dual_setup builds the anti-transpose
+// of w straight into wd's column store (wd shares w's per-column arrays),
+// with D's buckets reversed, left[], beta and the pivot records; dual_lows
+// maps wd's lows back to D's.
 // The automatic choice: D' for matrices of at least DUAL_MIN_M columns whose
 // top bucket holds DUAL_RATIO times the bottom one's columns (below that
 // size the few more sweeps and the transpose cost more than D's additions).
 constexpr unsigned long long DUAL_RATIO = 8;
 constexpr int64_t DUAL_MIN_M = 1 << 17;
 int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input);
-int dual_build(Context *ctx, const Work &w, Work &wd);
-void dual_dims(Context *ctx, const Work &w, Work &wd);
-void dual_left(Context *ctx, const Work &wd);
+int dual_setup(Context *ctx, const Work &w, Work &wd);
 int dual_lows(Context *ctx, const Work &wd, int32_t **low);
 
 // capi.cu

@@ -128,10 +128,7 @@ __device__ __forceinline__ int warp_max(int v) {
 
 // (b) per-tile maxima of repeated lows, per dimension bucket; counts repeats
 //     (per instance too, when the columns belong to several).
-__global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
-    if (a.st->converged) return;
-    const int64_t n = p1_count(a);
-    if ((int64_t)blockIdx.x * P1_TILE >= n) return;
+__device__ __forceinline__ void k_p1_tiles_tile(PmsArgs a, const int64_t n, const int64_t tile) {
     __shared__ int sm[P1_THREADS / 32][MAXC];
     __shared__ int sreps;
     if (threadIdx.x == 0) sreps = 0;
@@ -140,7 +137,7 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
     for (int d = 0; d < MAXC; d++) mx[d] = -1;
     int reps = 0;
     int cur_inst = -1, cur_reps = 0;  // per-instance counts, flushed on change
-    const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
+    const int64_t base = (int64_t)tile * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
         const int64_t idx = base + t;
@@ -177,9 +174,20 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
     if (threadIdx.x < MAXC) {
         int v = -1;
         for (int w = 0; w < P1_THREADS / 32; w++) v = max(v, sm[w][threadIdx.x]);
-        a.agg[blockIdx.x * MAXC + threadIdx.x] = v;
+        a.agg[tile * MAXC + threadIdx.x] = v;
     }
     if (threadIdx.x == 0 && sreps) atomicAdd(&a.st->reps, sreps);
+}
+// One pass over the list's tiles, a grid-stride loop: the grid is sized
+// for the machine, not for the matrix (a grid of one block per tile of
+// the full matrix costs ~0.3 ms of empty blocks per sweep at 3.5e8 columns).
+__global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
+    if (a.st->converged) return;
+    const int64_t n = p1_count(a);
+    for (int64_t tile = blockIdx.x; tile * P1_TILE < n; tile += gridDim.x) {
+        k_p1_tiles_tile(a, n, tile);
+        __syncthreads();  // the next tile reuses the shared arrays
+    }
 }
 
 // (c) exclusive prefix max of the tile maxima, one warp per bucket; decides
@@ -216,17 +224,14 @@ __global__ void k_p1_scan(PmsArgs a) {
 // (d) mark pivots: first for its low, unclassified, low above the running
 //     ceiling of repeated lows in its bucket.  With a compacted list, also
 //     count per tile the columns that stay unresolved.
-__global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
-    if (a.st->converged) return;
-    const int64_t n = p1_count(a);
-    if ((int64_t)blockIdx.x * P1_TILE >= n) return;
+__device__ __forceinline__ void k_p1_mark_tile(PmsArgs a, const int64_t n, const int64_t tile) {
     __shared__ int sm[P1_THREADS / 32][MAXC];
     __shared__ int skeep;
     __shared__ int sunres[MAXC];
     if (threadIdx.x == 0) skeep = 0;
     if (threadIdx.x < MAXC) sunres[threadIdx.x] = 0;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
+    const int64_t base = (int64_t)tile * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
     int lows[P1_ITEMS], bkt[P1_ITEMS];
     bool rep[P1_ITEMS];
     int mx[MAXC];
@@ -266,7 +271,7 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
     __syncthreads();
 #pragma unroll
     for (int d = 0; d < MAXC; d++) {
-        int c = a.agg[blockIdx.x * MAXC + d];
+        int c = a.agg[tile * MAXC + d];
         for (int w = 0; w < wid; w++) c = max(c, sm[w][d]);
         pre[d] = max(pre[d], c);
     }
@@ -303,9 +308,20 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
     if (a.ulist) {
         if (keep) atomicAdd(&skeep, keep);
         __syncthreads();
-        if (threadIdx.x == 0) a.kagg[blockIdx.x] = skeep;
+        if (threadIdx.x == 0) a.kagg[tile] = skeep;
         if (a.ascending && threadIdx.x < MAXC && sunres[threadIdx.x])
             atomicAdd(&a.st->bucket_unres[threadIdx.x], sunres[threadIdx.x]);
+    }
+}
+// One pass over the list's tiles, a grid-stride loop: the grid is sized
+// for the machine, not for the matrix (a grid of one block per tile of
+// the full matrix costs ~0.3 ms of empty blocks per sweep at 3.5e8 columns).
+__global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
+    if (a.st->converged) return;
+    const int64_t n = p1_count(a);
+    for (int64_t tile = blockIdx.x; tile * P1_TILE < n; tile += gridDim.x) {
+        k_p1_mark_tile(a, n, tile);
+        __syncthreads();  // the next tile reuses the shared arrays
     }
 }
 
@@ -375,13 +391,10 @@ __device__ __forceinline__ bool p2_ready(const PmsArgs &a, int j) {
     return a.classes[p] == 0 && a.low[p] > lj;
 }
 
-__global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
-    if (a.st->converged) return;
-    const int64_t n = p1_count(a);
-    if ((int64_t)blockIdx.x * P1_TILE >= n) return;
+__device__ __forceinline__ void k_p1_scatter_tile(PmsArgs a, const int64_t n, const int64_t tile) {
     __shared__ int wsum[P1_THREADS / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int64_t base = (int64_t)blockIdx.x * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
+    const int64_t base = (int64_t)tile * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
     int cols[P1_ITEMS];
     unsigned keepmask = 0;
     int cnt = 0;
@@ -408,7 +421,7 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
     }
     if (lane == 31) wsum[wid] = incl;
     __syncthreads();
-    int off = a.kagg[blockIdx.x] + incl - cnt;
+    int off = a.kagg[tile] + incl - cnt;
     for (int w = 0; w < wid; w++) off += wsum[w];
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++)
@@ -424,6 +437,17 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
         const bool want = ((keepmask >> t) & 1u) && a.dim[cols[t]] + 1 <= open &&
                           (!OPH_P2_FILTER || p2_ready(a, cols[t]));
         warp_append(want, cols[t], a.worklist, &a.st->t_count[0]);
+    }
+}
+// One pass over the list's tiles, a grid-stride loop: the grid is sized
+// for the machine, not for the matrix (a grid of one block per tile of
+// the full matrix costs ~0.3 ms of empty blocks per sweep at 3.5e8 columns).
+__global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
+    if (a.st->converged) return;
+    const int64_t n = p1_count(a);
+    for (int64_t tile = blockIdx.x; tile * P1_TILE < n; tile += gridDim.x) {
+        k_p1_scatter_tile(a, n, tile);
+        __syncthreads();  // the next tile reuses the shared arrays
     }
 }
 
@@ -1481,7 +1505,7 @@ int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
     g->g3 = ctx->sm_count;  // tier 3: one 1024-thread CTA per SM
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
-    g->t = (int)std::max<int64_t>(1, ntiles);
+    g->t = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 8));
     if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0 || g->gs < 0) {
         fprintf(stderr, "openph_gb300: Phase II kernel set-up failed: %s\n", cudaGetErrorString(cudaGetLastError()));
         return OPH_ERR_CUDA;

@@ -420,7 +420,7 @@ struct Server {
             sa.ntiles = (hi + 2047) / 2048;
             SweepGrids gg = g;
             gg.m = grid(hi);
-            gg.t = (int)std::max<int64_t>(1, sa.ntiles);
+            gg.t = (int)std::max<int64_t>(1, std::min<int64_t>(sa.ntiles, (int64_t)ctx->sm_count * 8));
             cudaMemsetAsync(a.ireps, 0, sizeof(int) * max_slots, s);
             k_srv_sweep_reset<<<1, 1, 0, s>>>(a.st);
             launch_sweep(sa, gg, s);

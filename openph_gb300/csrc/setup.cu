@@ -111,39 +111,6 @@ __global__ void k_setup_columns(const int64_t *__restrict__ colptr, const int32_
     }
 }
 
-// The same set-up with one thread per entry, for a matrix whose column of
-// every entry is known (entry_col, ascending): the anti-transpose, whose
-// long columns would leave a thread per column copying hundreds of rows
-// while its warp idles.  Built from a checked matrix, so nothing is checked.
-__global__ void k_setup_headers(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                                int *__restrict__ pool, int64_t *__restrict__ seg, int32_t *__restrict__ low,
-                                int8_t *__restrict__ dim) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t a = colptr[j], b = colptr[j + 1];
-        const int64_t s = 8 * j + 4 * ((a + 3) >> 2);
-        const int64_t e = 8 * (j + 1) + 4 * ((b + 3) >> 2);
-        const int n = (int)(b - a);
-        seg[j] = s;
-        pool[s] = n;
-        pool[s + 1] = (int)(e - s - SEG_HDR);
-        pool[s + 2] = 0;
-        pool[s + 3] = 0;
-        low[j] = n > 0 ? rows[b - 1] : -1;
-        dim[j] = (int8_t)(n - 1 > 126 ? 126 : n - 1);
-    }
-}
-__global__ void k_setup_entries(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows,
-                                const uint32_t *__restrict__ entry_col, int64_t nnz, int *__restrict__ pool,
-                                PivRec *__restrict__ rec) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = entry_col[k];
-        const int64_t a = colptr[j];
-        const int r = rows[k];
-        pool[8 * j + 4 * ((a + 3) >> 2) + SEG_HDR + (k - a)] = r;
-        if (rec) atomicMin(&rec[r].left, (int)j);
-    }
-}
-
 // left[i] = first column holding row i (atomicMin over the entries, into
 // the pivot records, which start as the 0x7f byte pattern).
 __global__ void k_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
@@ -210,7 +177,7 @@ static int64_t initial_pool_ints(Context *ctx, int64_t m, int64_t nnz) {
     return packed * 4 + (16 << 20);
 }
 
-int setup_store(Context *ctx, Work &w, bool need_beta) {
+int init_store(Context *ctx, Work &w) {
     const int64_t m = w.m;
     int64_t pool_ints = initial_pool_ints(ctx, m, w.nnz);
     // tail padding: narrow-tier kernels read up to a group's width past a
@@ -224,23 +191,21 @@ int setup_store(Context *ctx, Work &w, bool need_beta) {
     init.pool_size = (unsigned long long)pool_ints;
     init.max_dim = -1;
     OPH_CUDA_TRY(cudaMemcpyAsync(w.st, &init, sizeof(init), cudaMemcpyHostToDevice, ctx->stream));
+    return OPH_OK;
+}
+
+int setup_store(Context *ctx, Work &w, bool need_beta) {
+    const int64_t m = w.m;
+    int rc = init_store(ctx, w);
+    if (rc) return rc;
     if (m == 0) return OPH_OK;
     if (need_beta) {
         OPH_CUDA_TRY(cudaMemsetAsync(w.rec, 0x7f, sizeof(PivRec) * m, ctx->stream));
         OPH_CUDA_TRY(cudaMemsetAsync(w.beta, 0xff, sizeof(int32_t) * m, ctx->stream));
     }
-    if (w.entry_col) {
-        k_setup_headers<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.pool, w.seg, w.low,
-                                                                        w.dim);
-        if (w.nnz > 0)
-            k_setup_entries<<<grid_for(ctx, w.nnz, 256), 256, 0, ctx->stream>>>(
-                w.colptr, w.rows, w.entry_col, w.nnz, w.pool, need_beta && !w.src_colptr ? w.rec : nullptr);
-        if (need_beta && w.src_colptr) dual_left(ctx, w);
-    } else {
-        k_setup_columns<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.pool, w.seg, w.low,
-                                                                        w.dim, w.st);
-        if (need_beta) k_left<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.rec);
-    }
+    k_setup_columns<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.pool, w.seg, w.low,
+                                                                    w.dim, w.st);
+    if (need_beta) k_left<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.colptr, w.rows, m, w.rec);
     OPH_CUDA_TRY(cudaGetLastError());
     if (need_beta) {
         k_beta<<<grid_for(ctx, m, 256), 256, 0, ctx->stream>>>(w.rec, m, w.beta);

@@ -142,3 +142,37 @@ def test_rips_torus_1m_device_input(dctx):
     assert info["dual"] == 1
     np.testing.assert_array_equal(low.cpu().numpy(), want)
     np.testing.assert_array_equal(ess.cpu().numpy(), want_ess)
+
+
+def fan(n_rim, seed):
+    """A fan: vertex 0 joined to n_rim rim vertices, the rim a path, the
+    triangles {0, k, k+1}; edges and triangles in a seeded filtration order
+    (every face before its cofaces).  Vertex 0's column of the anti-transpose
+    holds n_rim rows."""
+    from openph_gb300.complexes import BoundaryMatrix
+    rng = np.random.default_rng(seed)
+    nv = n_rim + 1
+    edges = [(0, k) for k in range(1, nv)] + [(k, k + 1) for k in range(1, nv - 1)]
+    order = rng.permutation(len(edges))
+    edges = [edges[i] for i in order]
+    epos = {e: nv + i for i, e in enumerate(edges)}
+    tris = [(0, k, k + 1) for k in range(1, nv - 1)]
+    tris.sort(key=lambda t: max(epos[(0, t[1])], epos[(0, t[2])], epos[(t[1], t[2])]))
+    cols = [[] for _ in range(nv)] + [[a, b] for a, b in edges]
+    cols += [[epos[(0, k)], epos[(0, l)], epos[(k, l)]] for _, k, l in tris]
+    return BoundaryMatrix.from_columns(cols)
+
+
+@pytest.mark.parametrize("n_rim", [40, 700, 3000, 20000])
+def test_transpose_long_columns(dctx, n_rim):
+    """Columns of the anti-transpose of every length class: <= 32 rows (a
+    warp's registers), <= 1024 (a warp in shared memory) and beyond (a CTA's
+    radix sort, several tiles of it at 20,000 rows)."""
+    bm = fan(n_rim, seed=n_rim)
+    dctx.set_dual("always")
+    low, ess, info = dctx.reduce(bm, "pms")
+    dctx.set_dual("auto")
+    assert info["dual"] == 1
+    want, want_ess, _ = oracle.twist(bm)
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
