@@ -37,10 +37,11 @@
 //            into a slot taken from a per-column cursor counting down from
 //            cnt[c]; D's columns are visited in roughly ascending j, so the
 //            slots fill from the top down and the rows land nearly ascending
-//   finish   a warp per column of D': its rows sorted ascending (a bitonic
-//            network across the lanes for <= 32 rows, in shared memory for
-//            <= 1024; longer columns are queued), the segment header, low,
-//            and the bucket of D's column in the reversed position
+//   finish   a thread per column of D': the segment header, the bucket of
+//            D's column in the reversed position, and for a column of at
+//            most 8 rows its rows sorted in registers and its low; then a
+//            warp per longer column (a bitonic network across the lanes for
+//            <= 32 rows, in shared memory for <= 1024; longer ones queued)
 //   long     a CTA per queued column: LSD radix sort, 8-bit digits, through
 //            a scratch range at the column's own offsets
 //   records  per row of D': its pivot record reset with left[] (row m-1-j of
@@ -269,34 +270,85 @@ __device__ __forceinline__ int warp_sort32(int v) {
     return v;
 }
 
-constexpr int FIN_WARPS = 8, LONG_COL = 1024;
+constexpr int FIN_WARPS = 8, SHORT_COL = 8, LONG_COL = 1024;
 
-// a warp per column of D': rows sorted, header, low, bucket
-__global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish(const int64_t *__restrict__ dcolptr,
-                                                                const int64_t *__restrict__ colptr, int64_t m,
-                                                                int *__restrict__ pool, int64_t *__restrict__ seg,
-                                                                int32_t *__restrict__ low, int8_t *__restrict__ dim,
-                                                                int *__restrict__ long_list, int *long_count) {
+// a thread per column of D': the segment header, the bucket of D's column in
+// the reversed position, and for a column of at most SHORT_COL rows its rows
+// sorted (in registers) and its low; longer columns are queued for warps
+__global__ void k_dual_finish(const int64_t *__restrict__ dcolptr, const int64_t *__restrict__ colptr, int64_t m,
+                              int *__restrict__ pool, int64_t *__restrict__ seg, int32_t *__restrict__ low,
+                              int8_t *__restrict__ dim, int *__restrict__ mid_list, int *mid_count) {
+    for (int64_t c0 = blockIdx.x * (int64_t)blockDim.x; c0 < m; c0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = c0 + threadIdx.x;
+        bool queue = false;
+        if (c < m) {
+            const int64_t a = dcolptr[c], b = dcolptr[c + 1];
+            const int n = (int)(b - a);
+            const int64_t s = seg_start(c, a), e = seg_start(c + 1, b);
+            int *R = pool + s + SEG_HDR;
+            *reinterpret_cast<int4 *>(pool + s) = make_int4(n, (int)(e - s - SEG_HDR), 0, 0);
+            seg[c] = s;
+            const int64_t i = m - 1 - c;
+            const int64_t nd = colptr[i + 1] - colptr[i];
+            dim[c] = (int8_t)(nd - 1 > 126 ? 126 : nd - 1);
+            if (n <= SHORT_COL) {
+                int v[SHORT_COL];
+#pragma unroll
+                for (int k = 0; k < SHORT_COL; k++) v[k] = k < n ? R[k] : INT_MAX;
+                // insertion sort (the rows arrive nearly ascending)
+#pragma unroll
+                for (int k = 1; k < SHORT_COL; k++)
+#pragma unroll
+                    for (int q = k; q > 0; q--) {
+                        const int lo = min(v[q - 1], v[q]), hi = max(v[q - 1], v[q]);
+                        v[q - 1] = lo;
+                        v[q] = hi;
+                    }
+                int top = -1;
+#pragma unroll
+                for (int k = 0; k < SHORT_COL; k++)
+                    if (k < n) {
+                        R[k] = v[k];
+                        top = v[k];
+                    }
+                low[c] = top;
+            } else {
+                queue = true;
+            }
+        }
+        warp_append(queue, (int)c, mid_list, mid_count);
+    }
+}
+
+// a warp per queued column (more than SHORT_COL rows): its rows sorted (a
+// bitonic network across the lanes for <= 32 rows, in shared memory for
+// <= LONG_COL) and its low; longer columns are queued for a CTA
+__global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_warp(const int64_t *__restrict__ dcolptr,
+                                                                     int *__restrict__ pool,
+                                                                     int32_t *__restrict__ low,
+                                                                     const int *__restrict__ mid_list,
+                                                                     const int *mid_count,
+                                                                     int *__restrict__ long_list, int *long_count) {
     __shared__ int sbuf[FIN_WARPS][LONG_COL];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * FIN_WARPS;
+    const int count = *mid_count;
     int *B = sbuf[wid];
-    for (int64_t c = blockIdx.x * (int64_t)FIN_WARPS + wid; c < m; c += nwarps) {
-        const int64_t a = dcolptr[c], b = dcolptr[c + 1];
-        const int n = (int)(b - a);
-        const int64_t s = seg_start(c, a), e = seg_start(c + 1, b);
-        int *R = pool + s + SEG_HDR;
-        int lowv = -1;
+    for (int64_t idx = blockIdx.x * (int64_t)FIN_WARPS + wid; idx < count; idx += nwarps) {
+        const int64_t c = mid_list[idx];
+        const int64_t a = dcolptr[c];
+        const int n = (int)(dcolptr[c + 1] - a);
+        int *R = pool + seg_start(c, a) + SEG_HDR;
         if (n <= 32) {
             int v = lane < n ? R[lane] : INT_MAX;
             v = warp_sort32(v);
             if (lane < n) R[lane] = v;
-            if (n > 0) lowv = __shfl_sync(0xffffffffu, v, n - 1);
+            if (lane == n - 1) low[c] = v;
         } else if (n <= LONG_COL) {
             bool sorted = true;
             for (int k = lane; k + 1 < n; k += 32) sorted &= R[k] < R[k + 1];
             if (__all_sync(0xffffffffu, sorted)) {
-                lowv = R[n - 1];
+                if (lane == 0) low[c] = R[n - 1];
             } else {
                 int N = 64;
                 while (N < n) N <<= 1;
@@ -318,22 +370,11 @@ __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish(const int64_t *_
                         __syncwarp();
                     }
                 for (int k = lane; k < n; k += 32) R[k] = B[k];
-                lowv = B[n - 1];
+                if (lane == 0) low[c] = B[n - 1];
                 __syncwarp();  // B is reused by the warp's next column
             }
         } else if (lane == 0) {
             long_list[atomicAdd(long_count, 1)] = (int)c;
-        }
-        if (lane == 0) {
-            seg[c] = s;
-            pool[s] = n;
-            pool[s + 1] = (int)(e - s - SEG_HDR);
-            pool[s + 2] = 0;
-            pool[s + 3] = 0;
-            if (n <= LONG_COL) low[c] = lowv;
-            const int64_t i = m - 1 - c;
-            const int64_t nd = colptr[i + 1] - colptr[i];
-            dim[c] = (int8_t)(nd - 1 > 126 ? 126 : nd - 1);
         }
     }
 }
@@ -514,12 +555,13 @@ int dual_setup(Context *ctx, const Work &w, Work &wd) {
     // scratch, two counters and the scan's tile sums, in one buffer
     const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
     auto r256 = [](int64_t b) { return (b + 255) & ~255ll; };
-    const int64_t o_long = r256(4 * m), o_scr = o_long + r256(4 * m);
+    const int64_t o_long = r256(4 * m), o_mid = o_long + r256(4 * m), o_scr = o_mid + r256(4 * m);
     const int64_t o_ctr = o_scr + r256(4 * (nnz > 0 ? nnz : 1)), o_tsum = o_ctr + 256;
     const int64_t bytes = o_tsum + 8 * (ntiles + 1);
     char *buf = (char *)ctx_alloc(ctx, S_DSORT, (size_t)bytes);
     if (!dcolptr || !buf) return OPH_ERR_OOM;
-    int *cnt = (int *)buf, *long_list = (int *)(buf + o_long), *scratch = (int *)(buf + o_scr);
+    int *cnt = (int *)buf, *long_list = (int *)(buf + o_long), *mid_list = (int *)(buf + o_mid);
+    int *scratch = (int *)(buf + o_scr);
     int *ctr = (int *)(buf + o_ctr);
     long long *tsum = (long long *)(buf + o_tsum);
     wd.colptr = dcolptr;
@@ -533,14 +575,13 @@ int dual_setup(Context *ctx, const Work &w, Work &wd) {
     k_scan_tsums<<<1, SCAN_THREADS, 0, s>>>(tsum, ntiles, dcolptr + m);
     k_scan_apply<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum, dcolptr);
     k_dual_scatter<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, dcolptr, cnt, wd.pool);
-    const int gf =
-        (int)std::max<int64_t>(1, std::min<int64_t>((m + FIN_WARPS - 1) / FIN_WARPS, (int64_t)ctx->sm_count * 8));
-    k_dual_finish<<<gf, FIN_WARPS * 32, 0, s>>>(dcolptr, w.colptr, m, wd.pool, wd.seg, wd.low, wd.dim, long_list,
-                                                &ctr[0]);
+    k_dual_finish<<<gm, 256, 0, s>>>(dcolptr, w.colptr, m, wd.pool, wd.seg, wd.low, wd.dim, mid_list, &ctr[2]);
+    k_dual_finish_warp<<<ctx->sm_count * 8, FIN_WARPS * 32, 0, s>>>(dcolptr, wd.pool, wd.low, mid_list, &ctr[2],
+                                                                  long_list, &ctr[0]);
     k_dual_sort_long<<<ctx->sm_count, LS_THREADS, 0, s>>>(dcolptr, wd.pool, wd.low, long_list, &ctr[0], &ctr[1],
                                                           scratch);
     k_dual_rec<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, wd.rec, wd.beta);
-    ctx->launches += 8;
+    ctx->launches += 9;
     OPH_CUDA_TRY(cudaGetLastError());
     return OPH_OK;
 }
