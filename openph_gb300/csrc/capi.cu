@@ -47,20 +47,6 @@ void *ctx_alloc(Context *ctx, int slot, size_t bytes) {
 }
 
 // --------------------------------------------------------------- kernels
-// Batch input: shift each instance's local rows into its column range.
-__global__ void k_shift_rows(const int64_t *__restrict__ colptr, const int64_t *__restrict__ inst_off, int count,
-                             int64_t m, const int32_t *__restrict__ rows_local, int32_t *__restrict__ rows_global) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
-        int lo = 0, hi = count;  // last b with inst_off[b] <= j
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (inst_off[mid] <= j) lo = mid; else hi = mid;
-        }
-        const int64_t base = inst_off[lo];
-        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) rows_global[k] = rows_local[k] + (int32_t)base;
-    }
-}
-
 enum EssMode { ESS_PAIRS = 0, ESS_ROW_PARALLEL = 1, ESS_RUNNING = 2 };
 
 // Output pass 1: low (0- or 1-based, optionally local to its batch instance),
@@ -449,16 +435,13 @@ static int batch_core(oph_context *ctx, int algo, int32_t count, const int64_t *
                       oph_info *info) {
     cudaStream_t s = ctx->stream;
     ctx->launches = 0;
-    // instance offsets, colptr and local rows checked before the shift reads
-    // through them
-    int rc = check_csc(ctx, d_colptr, d_rows_local, total_m, total_nnz, d_col_off, count);
-    if (rc) return rc;
+    // instance offsets, colptr and local rows checked, and the rows shifted
+    // into their instances' column ranges, in one pass (a checked entry is
+    // the only one written)
     int32_t *d_rows_g = (int32_t *)ctx_alloc(ctx, S_COO_R, sizeof(int32_t) * (total_nnz > 0 ? total_nnz : 1));
     if (!d_rows_g) return OPH_ERR_OOM;
-    if (total_m > 0)
-        k_shift_rows<<<grid_for(ctx, total_m), 256, 0, s>>>(d_colptr, d_col_off, count, total_m, d_rows_local,
-                                                            d_rows_g);
-    OPH_CUDA_TRY(cudaGetLastError());
+    int rc = check_csc(ctx, d_colptr, d_rows_local, total_m, total_nnz, d_col_off, count, d_rows_g);
+    if (rc) return rc;
     Work w;
     rc = alloc_work(ctx, w, total_m);
     if (rc) return rc;

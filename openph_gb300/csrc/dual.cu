@@ -40,8 +40,9 @@
 //   finish   a thread per column of D': the segment header, the bucket of
 //            D's column in the reversed position, and for a column of at
 //            most 8 rows its rows sorted in registers and its low; then a
-//            warp per longer column (a bitonic network across the lanes for
-//            <= 32 rows, in shared memory for <= 1024; longer ones queued)
+//            warp per longer column of at most 1024 rows (a bitonic network
+//            over the warp's registers, up to 32 values a lane; longer ones
+//            are queued)
 //   long     a CTA per queued column: LSD radix sort, 8-bit digits, through
 //            a scratch range at the column's own offsets
 //   records  per row of D': its pivot record reset with left[] (row m-1-j of
@@ -72,35 +73,62 @@ __global__ void k_dual_grade(const int64_t *__restrict__ colptr, const int32_t *
     }
     if (threadIdx.x < 2) s_flags[threadIdx.x] = 0;
     __syncthreads();
+    // per-thread tallies, merged once per block (no shared atomic per
+    // column): bucket counts, and the row bucket seen for each column bucket
+    // (TAB_NONE or a bucket; a second, different one marks the input mixed)
+    unsigned long long cnt[MAXC];
+    int tabv[MAXC];
+#pragma unroll
+    for (int b = 0; b < MAXC; b++) {
+        cnt[b] = 0;
+        tabv[b] = TAB_NONE;
+    }
+    bool mixed_t = false, bad_t = false;
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
         const int64_t lo = colptr[j], hi = colptr[j + 1];
         if (lo < 0 || hi < lo || hi > nnz) {  // bounds first: nothing is read past rows[nnz)
-            s_flags[1] = 1;
+            bad_t = true;
             continue;
         }
         const int b = bucket_of(hi - lo);
         if (b + 1 >= MAXC) {  // a bucket the Phase I scan does not keep
-            s_flags[0] = 1;
+            mixed_t = true;
             continue;
         }
-        atomicAdd(&s_count[b + 1], 1ull);
         int rb = TAB_NONE, prev = -1;
         for (int64_t k = lo; k < hi; k++) {
             const int r = rows[k];
             if (r <= prev || r >= m) {
-                s_flags[1] = 1;
+                bad_t = true;
                 break;
             }
             prev = r;
             const int br = bucket[r];
             if (k == lo) rb = br;
-            else if (br != rb) s_flags[0] = 1;
+            else if (br != rb) mixed_t = true;
         }
-        if (rb != TAB_NONE) {
-            const int old = atomicCAS(&s_tab[b + 1], TAB_NONE, rb);
-            if (old != TAB_NONE && old != rb) s_flags[0] = 1;
+#pragma unroll
+        for (int d = 0; d < MAXC; d++)
+            if (d == b + 1) {
+                cnt[d]++;
+                if (rb != TAB_NONE) {
+                    if (tabv[d] == TAB_NONE) tabv[d] = rb;
+                    else if (tabv[d] != rb) mixed_t = true;
+                }
+            }
+    }
+#pragma unroll
+    for (int d = 0; d < MAXC; d++) {
+        unsigned long long c = cnt[d];
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_count[d], c);
+        if (tabv[d] != TAB_NONE) {
+            const int old = atomicCAS(&s_tab[d], TAB_NONE, tabv[d]);
+            if (old != TAB_NONE && old != tabv[d]) mixed_t = true;
         }
     }
+    if (mixed_t) s_flags[0] = 1;
+    if (bad_t) s_flags[1] = 1;
     __syncthreads();
     if (threadIdx.x < MAXC) {
         if (s_count[threadIdx.x]) atomicAdd(&count[threadIdx.x], s_count[threadIdx.x]);
@@ -231,43 +259,58 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int *__restri
     }
 }
 
+// In the count and the scatter the warp's threads walk their columns of D
+// entry by entry in step, so equal targets in D' meet in one instruction and
+// share one atomic (__match_any_sync): consecutive Rips triangles mostly
+// share their longest edge, hence their last row.
+
 // entries of every column of D' (= entries of D in each row)
 __global__ void k_dual_count(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                              int *__restrict__ cnt) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
-        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) atomicAdd(&cnt[m - 1 - rows[k]], 1);
+    const int lane = threadIdx.x & 31;
+    for (int64_t j0 = blockIdx.x * (int64_t)blockDim.x; j0 < m; j0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = j0 + threadIdx.x;
+        const int64_t lo = j < m ? colptr[j] : 0, hi = j < m ? colptr[j + 1] : 0;
+        const int n = (int)(hi - lo);
+        const int nmax = __reduce_max_sync(0xffffffffu, n);
+        for (int t = 0; t < nmax; t++) {
+            const int64_t c = t < n ? m - 1 - rows[lo + t] : -1;
+            const unsigned peers = __match_any_sync(0xffffffffu, c);
+            if (c >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[c], __popc(peers));
+        }
+    }
 }
 
 // Segment of column c of a store whose column offsets are `off` (the layout
 // of k_setup_columns: room for the header, capacities in 16-byte units).
 __device__ __forceinline__ int64_t seg_start(int64_t c, int64_t off) { return 8 * c + 4 * ((off + 3) >> 2); }
 
-// every entry of D into its column of D' (row m-1-j), slots from the top
+// every entry of D into its column of D' (row m-1-j), slots from the top;
+// equal targets within the warp take their slots with one atomic
 __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                                const int64_t *__restrict__ dcolptr, int *__restrict__ cursor,
                                int *__restrict__ pool) {
-    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t j0 = blockIdx.x * (int64_t)blockDim.x; j0 < m; j0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = j0 + threadIdx.x;
+        const int64_t lo = j < m ? colptr[j] : 0, hi = j < m ? colptr[j + 1] : 0;
+        const int n = (int)(hi - lo);
         const int val = (int)(m - 1 - j);
-        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) {
-            const int64_t c = m - 1 - rows[k];
-            const int pos = atomicSub(&cursor[c], 1) - 1;
-            pool[seg_start(c, dcolptr[c]) + SEG_HDR + pos] = val;
+        const int nmax = __reduce_max_sync(0xffffffffu, n);
+        for (int t = 0; t < nmax; t++) {
+            const int64_t c = t < n ? m - 1 - rows[lo + t] : -1;
+            const unsigned peers = __match_any_sync(0xffffffffu, c);
+            const int leader = __ffs(peers) - 1;
+            int top = 0;
+            if (c >= 0 && lane == leader) top = atomicSub(&cursor[c], __popc(peers));
+            top = __shfl_sync(0xffffffffu, top, leader);
+            if (c >= 0) {
+                // the lower lane (the smaller column of D) takes the higher slot
+                const int pos = top - 1 - __popc(peers & ((1u << lane) - 1u));
+                pool[seg_start(c, dcolptr[c]) + SEG_HDR + pos] = val;
+            }
         }
     }
-}
-
-// Ascending order of one value per lane (a bitonic network across the warp).
-__device__ __forceinline__ int warp_sort32(int v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int size = 2; size <= 32; size <<= 1)
-#pragma unroll
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            const int o = __shfl_xor_sync(0xffffffffu, v, stride);
-            const bool up = (lane & size) == 0, lower = (lane & stride) == 0;
-            v = (lower == up) ? min(v, o) : max(v, o);
-        }
-    return v;
 }
 
 constexpr int FIN_WARPS = 8, SHORT_COL = 8, LONG_COL = 1024;
@@ -320,62 +363,95 @@ __global__ void k_dual_finish(const int64_t *__restrict__ dcolptr, const int64_t
     }
 }
 
-// a warp per queued column (more than SHORT_COL rows): its rows sorted (a
-// bitonic network across the lanes for <= 32 rows, in shared memory for
-// <= LONG_COL) and its low; longer columns are queued for a CTA
+// Ascending order of the warp's 32 K values, lane l holding elements
+// l K .. l K + K - 1: a bitonic network, in registers within a lane and by
+// shuffles across lanes (K a power of two).
+template <int K>
+__device__ __forceinline__ void warp_sort_reg(int (&v)[K]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int size = 2; size <= 32 * K; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (stride < K) {
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const int q = k ^ stride;
+                    if (q > k) {
+                        const bool up = ((lane * K + k) & size) == 0;
+                        const int x = v[k], y = v[q];
+                        v[k] = up ? min(x, y) : max(x, y);
+                        v[q] = up ? max(x, y) : min(x, y);
+                    }
+                }
+            } else {
+                const int ls = stride / K;
+                const bool lower = (lane & ls) == 0;
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const bool up = ((lane * K + k) & size) == 0;
+                    const int o = __shfl_xor_sync(0xffffffffu, v[k], ls);
+                    v[k] = (lower == up) ? min(v[k], o) : max(v[k], o);
+                }
+            }
+        }
+    }
+}
+
+// A column of n <= 32 K rows at R sorted by the warp; returns the low.
+template <int K>
+__device__ __forceinline__ int warp_sort_column(int *R, int n) {
+    const int lane = threadIdx.x & 31;
+    int v[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int e = lane * K + k;
+        v[k] = e < n ? R[e] : INT_MAX;
+    }
+    warp_sort_reg<K>(v);
+    int top = INT_MIN;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int e = lane * K + k;
+        if (e < n) {
+            R[e] = v[k];
+            top = v[k];
+        }
+    }
+    return __reduce_max_sync(0xffffffffu, top);
+}
+
+// a warp per queued column (more than SHORT_COL rows): its rows sorted in
+// registers and its low; columns of more than LONG_COL rows are queued for
+// a CTA
 __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_warp(const int64_t *__restrict__ dcolptr,
                                                                      int *__restrict__ pool,
                                                                      int32_t *__restrict__ low,
                                                                      const int *__restrict__ mid_list,
                                                                      const int *mid_count,
                                                                      int *__restrict__ long_list, int *long_count) {
-    __shared__ int sbuf[FIN_WARPS][LONG_COL];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * FIN_WARPS;
     const int count = *mid_count;
-    int *B = sbuf[wid];
     for (int64_t idx = blockIdx.x * (int64_t)FIN_WARPS + wid; idx < count; idx += nwarps) {
         const int64_t c = mid_list[idx];
         const int64_t a = dcolptr[c];
         const int n = (int)(dcolptr[c + 1] - a);
         int *R = pool + seg_start(c, a) + SEG_HDR;
-        if (n <= 32) {
-            int v = lane < n ? R[lane] : INT_MAX;
-            v = warp_sort32(v);
-            if (lane < n) R[lane] = v;
-            if (lane == n - 1) low[c] = v;
-        } else if (n <= LONG_COL) {
-            bool sorted = true;
-            for (int k = lane; k + 1 < n; k += 32) sorted &= R[k] < R[k + 1];
-            if (__all_sync(0xffffffffu, sorted)) {
-                if (lane == 0) low[c] = R[n - 1];
-            } else {
-                int N = 64;
-                while (N < n) N <<= 1;
-                for (int k = lane; k < N; k += 32) B[k] = k < n ? R[k] : INT_MAX;
-                __syncwarp();
-                for (int size = 2; size <= N; size <<= 1)
-                    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                        for (int i = lane; i < N; i += 32) {
-                            const int l = i ^ stride;
-                            if (l > i) {
-                                const bool up = (i & size) == 0;
-                                const int x = B[i], y = B[l];
-                                if ((x > y) == up) {
-                                    B[i] = y;
-                                    B[l] = x;
-                                }
-                            }
-                        }
-                        __syncwarp();
-                    }
-                for (int k = lane; k < n; k += 32) R[k] = B[k];
-                if (lane == 0) low[c] = B[n - 1];
-                __syncwarp();  // B is reused by the warp's next column
-            }
-        } else if (lane == 0) {
-            long_list[atomicAdd(long_count, 1)] = (int)c;
+        bool sorted = true;
+        for (int k = lane; k + 1 < n; k += 32) sorted &= R[k] < R[k + 1];
+        int top;
+        if (__all_sync(0xffffffffu, sorted)) top = R[n - 1];
+        else if (n <= 32) top = warp_sort_column<1>(R, n);
+        else if (n <= 128) top = warp_sort_column<4>(R, n);
+        else if (n <= 256) top = warp_sort_column<8>(R, n);
+        else if (n <= 512) top = warp_sort_column<16>(R, n);
+        else if (n <= LONG_COL) top = warp_sort_column<32>(R, n);
+        else {
+            if (lane == 0) long_list[atomicAdd(long_count, 1)] = (int)c;
+            continue;
         }
+        if (lane == 0) low[c] = top;
     }
 }
 

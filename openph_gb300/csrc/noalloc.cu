@@ -35,7 +35,8 @@ __global__ void k_setup_columns(const int64_t *__restrict__ colptr, const int32_
                                 int *__restrict__ pool, int64_t *__restrict__ seg, int32_t *__restrict__ low,
                                 int8_t *__restrict__ dim, DevStatus *st);
 __global__ void k_check_csc(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                            int64_t nnz, const int64_t *__restrict__ inst_off, int count, int *bad);
+                            int64_t nnz, const int64_t *__restrict__ inst_off, int count, int *bad,
+                            int32_t *__restrict__ rows_out);
 __global__ void k_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                        PivRec *__restrict__ rec);
 __global__ void k_beta(PivRec *__restrict__ rec, int64_t m, int32_t *__restrict__ beta);
@@ -160,7 +161,7 @@ extern "C" __attribute__((visibility("default"))) int oph_reduce_pms_noalloc(int
     // the caller's CSC is checked (read only) before any kernel writes
     // through its offsets or rows
     DevStatus hs;
-    k_check_csc<<<grid, 256, 0, s>>>(d_colptr, d_rows, m, nnz, nullptr, 0, &st->error);
+    k_check_csc<<<grid, 256, 0, s>>>(d_colptr, d_rows, m, nnz, nullptr, 0, &st->error, nullptr);
     OPH_CUDA_TRY(cudaGetLastError());
     OPH_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
     OPH_CUDA_TRY(cudaStreamSynchronize(s));

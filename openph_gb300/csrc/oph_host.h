@@ -63,9 +63,10 @@ int setup_store(Context *ctx, Work &w, bool need_beta);
 int coo1_to_csc(Context *ctx, const int *d_rows1, const int *d_cols1, int64_t nnz, int64_t m, int64_t *d_colptr,
                 int32_t *d_rows0);
 // Structural check of a device CSC (k_check_csc), synchronous: OPH_OK or
-// OPH_ERR_BAD_INPUT.  With d_inst_off, rows are local to their instance.
+// OPH_ERR_BAD_INPUT.  With d_inst_off, rows are local to their instance, and
+// d_rows_out (if set) receives them shifted into the instance's columns.
 int check_csc(Context *ctx, const int64_t *d_colptr, const int32_t *d_rows, int64_t m, int64_t nnz,
-              const int64_t *d_inst_off, int count);
+              const int64_t *d_inst_off = nullptr, int count = 0, int32_t *d_rows_out = nullptr);
 int grow_pool(Context *ctx, Work &w);
 
 // pms.cu

@@ -41,9 +41,12 @@ __global__ void k_coo1_to_csc(const int *__restrict__ r1, const int *__restrict_
 // m, or, for a batch (inst_off != nullptr), the size of the column's
 // instance, whose offsets must run from 0 to m without decreasing.  Only
 // reads; any violation sets *bad.  Bounds come first: no row is read
-// outside [0, nnz) and no offset outside [0, count].
+// outside [0, nnz) and no offset outside [0, count].  With rows_out (a
+// batch), every checked entry is also written there shifted into its
+// instance's column range (the rows of a batch as one block-diagonal matrix).
 __global__ void k_check_csc(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                            int64_t nnz, const int64_t *__restrict__ inst_off, int count, int *bad) {
+                            int64_t nnz, const int64_t *__restrict__ inst_off, int count, int *bad,
+                            int32_t *__restrict__ rows_out) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
     if (tid == 0 && (colptr[0] != 0 || colptr[m] != nnz)) atomicExch(bad, 1);
     if (inst_off) {
@@ -58,14 +61,15 @@ __global__ void k_check_csc(const int64_t *__restrict__ colptr, const int32_t *_
             atomicExch(bad, 1);
             continue;
         }
-        int64_t lim = m;
+        int64_t lim = m, base = 0;
         if (inst_off) {
             int a = 0, z = count;  // last b with inst_off[b] <= j (bounded steps whatever the offsets)
             while (z - a > 1) {
                 const int mid = (a + z) >> 1;
                 if (inst_off[mid] <= j) a = mid; else z = mid;
             }
-            lim = inst_off[a + 1] - inst_off[a];
+            base = inst_off[a];
+            lim = inst_off[a + 1] - base;
         }
         int prev = -1;
         for (int64_t k = lo; k < hi; k++) {
@@ -75,6 +79,7 @@ __global__ void k_check_csc(const int64_t *__restrict__ colptr, const int32_t *_
                 break;
             }
             prev = r;
+            if (rows_out) rows_out[k] = r + (int32_t)base;
         }
     }
 }
@@ -140,13 +145,13 @@ static int grid_for(Context *ctx, int64_t n, int block) {
 }
 
 int check_csc(Context *ctx, const int64_t *d_colptr, const int32_t *d_rows, int64_t m, int64_t nnz,
-              const int64_t *d_inst_off, int count) {
+              const int64_t *d_inst_off, int count, int32_t *d_rows_out) {
     int *d_bad = (int *)ctx_alloc(ctx, S_CHECK, sizeof(int));
     if (!d_bad) return OPH_ERR_OOM;
     cudaStream_t s = ctx->stream;
     OPH_CUDA_TRY(cudaMemsetAsync(d_bad, 0, sizeof(int), s));
     k_check_csc<<<grid_for(ctx, std::max<int64_t>(m, count), 256), 256, 0, s>>>(d_colptr, d_rows, m, nnz,
-                                                                                d_inst_off, count, d_bad);
+                                                                                d_inst_off, count, d_bad, d_rows_out);
     ctx->launches++;
     OPH_CUDA_TRY(cudaGetLastError());
     int bad = 0;
