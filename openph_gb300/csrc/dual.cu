@@ -40,8 +40,8 @@
 //   finish   a thread per column of D': the segment header, the bucket of
 //            D's column in the reversed position, and for a column of at
 //            most 8 rows its rows sorted in registers and its low; then a
-//            warp per longer column of at most 1024 rows (a bitonic network
-//            over the warp's registers, up to 32 values a lane; longer ones
+//            warp per longer column of at most 256 rows (a bitonic network
+//            over the warp's registers, up to 8 values a lane; longer ones
 //            are queued)
 //   long     a CTA per queued column: LSD radix sort, 8-bit digits, through
 //            a scratch range at the column's own offsets
@@ -274,7 +274,7 @@ __global__ void k_dual_count(const int64_t *__restrict__ colptr, const int32_t *
         const int n = (int)(hi - lo);
         const int nmax = __reduce_max_sync(0xffffffffu, n);
         for (int t = 0; t < nmax; t++) {
-            const int64_t c = t < n ? m - 1 - rows[lo + t] : -1;
+            const int c = t < n ? (int)(m - 1 - rows[lo + t]) : -1;
             const unsigned peers = __match_any_sync(0xffffffffu, c);
             if (c >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[c], __popc(peers));
         }
@@ -298,7 +298,7 @@ __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t
         const int val = (int)(m - 1 - j);
         const int nmax = __reduce_max_sync(0xffffffffu, n);
         for (int t = 0; t < nmax; t++) {
-            const int64_t c = t < n ? m - 1 - rows[lo + t] : -1;
+            const int c = t < n ? (int)(m - 1 - rows[lo + t]) : -1;
             const unsigned peers = __match_any_sync(0xffffffffu, c);
             const int leader = __ffs(peers) - 1;
             int top = 0;
@@ -313,7 +313,7 @@ __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t
     }
 }
 
-constexpr int FIN_WARPS = 8, SHORT_COL = 8, LONG_COL = 1024;
+constexpr int FIN_WARPS = 8, SHORT_COL = 8, LONG_COL = 256;
 
 // a thread per column of D': the segment header, the bucket of D's column in
 // the reversed position, and for a column of at most SHORT_COL rows its rows
@@ -408,6 +408,13 @@ __device__ __forceinline__ int warp_sort_column(int *R, int n) {
         const int e = lane * K + k;
         v[k] = e < n ? R[e] : INT_MAX;
     }
+    // already ascending (each lane's run and its boundary with the next)?
+    bool asc = true;
+#pragma unroll
+    for (int k = 0; k + 1 < K; k++) asc &= v[k] <= v[k + 1];
+    const int next_first = __shfl_down_sync(0xffffffffu, v[0], 1);
+    if (lane < 31) asc &= v[K - 1] <= next_first;
+    if (__all_sync(0xffffffffu, asc)) return __shfl_sync(0xffffffffu, v[(n - 1) % K], (n - 1) / K);
     warp_sort_reg<K>(v);
     int top = INT_MIN;
 #pragma unroll
@@ -422,13 +429,16 @@ __device__ __forceinline__ int warp_sort_column(int *R, int n) {
 }
 
 // a warp per queued column (more than SHORT_COL rows): its rows sorted in
-// registers and its low; columns of more than LONG_COL rows are queued for
-// a CTA
+// registers and its low, for columns of at most MID_COL rows (a few values a
+// lane keeps the kernel's registers, hence its occupancy, low); longer
+// columns are queued for k_dual_finish_wide (<= LONG_COL) or a CTA
+constexpr int MID_COL = 128;
 __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_warp(const int64_t *__restrict__ dcolptr,
                                                                      int *__restrict__ pool,
                                                                      int32_t *__restrict__ low,
                                                                      const int *__restrict__ mid_list,
                                                                      const int *mid_count,
+                                                                     int *__restrict__ wide_list, int *wide_count,
                                                                      int *__restrict__ long_list, int *long_count) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * FIN_WARPS;
@@ -437,20 +447,35 @@ __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_warp(const int64
         const int64_t c = mid_list[idx];
         const int64_t a = dcolptr[c];
         const int n = (int)(dcolptr[c + 1] - a);
-        int *R = pool + seg_start(c, a) + SEG_HDR;
-        bool sorted = true;
-        for (int k = lane; k + 1 < n; k += 32) sorted &= R[k] < R[k + 1];
-        int top;
-        if (__all_sync(0xffffffffu, sorted)) top = R[n - 1];
-        else if (n <= 32) top = warp_sort_column<1>(R, n);
-        else if (n <= 128) top = warp_sort_column<4>(R, n);
-        else if (n <= 256) top = warp_sort_column<8>(R, n);
-        else if (n <= 512) top = warp_sort_column<16>(R, n);
-        else if (n <= LONG_COL) top = warp_sort_column<32>(R, n);
-        else {
-            if (lane == 0) long_list[atomicAdd(long_count, 1)] = (int)c;
+        if (n > MID_COL) {
+            if (lane == 0) {
+                if (n <= LONG_COL) wide_list[atomicAdd(wide_count, 1)] = (int)c;
+                else long_list[atomicAdd(long_count, 1)] = (int)c;
+            }
             continue;
         }
+        int *R = pool + seg_start(c, a) + SEG_HDR;
+        const int top = n <= 32 ? warp_sort_column<1>(R, n) : warp_sort_column<4>(R, n);
+        if (lane == 0) low[c] = top;
+    }
+}
+
+// the same for the queued columns of MID_COL < n <= LONG_COL rows (eight
+// values a lane)
+__global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_wide(const int64_t *__restrict__ dcolptr,
+                                                                     int *__restrict__ pool,
+                                                                     int32_t *__restrict__ low,
+                                                                     const int *__restrict__ wide_list,
+                                                                     const int *wide_count) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int64_t nwarps = (int64_t)gridDim.x * FIN_WARPS;
+    const int count = *wide_count;
+    for (int64_t idx = blockIdx.x * (int64_t)FIN_WARPS + wid; idx < count; idx += nwarps) {
+        const int64_t c = wide_list[idx];
+        const int64_t a = dcolptr[c];
+        const int n = (int)(dcolptr[c + 1] - a);
+        int *R = pool + seg_start(c, a) + SEG_HDR;
+        const int top = warp_sort_column<8>(R, n);
         if (lane == 0) low[c] = top;
     }
 }
@@ -631,12 +656,14 @@ int dual_setup(Context *ctx, const Work &w, Work &wd) {
     // scratch, two counters and the scan's tile sums, in one buffer
     const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
     auto r256 = [](int64_t b) { return (b + 255) & ~255ll; };
-    const int64_t o_long = r256(4 * m), o_mid = o_long + r256(4 * m), o_scr = o_mid + r256(4 * m);
+    const int64_t o_long = r256(4 * m), o_mid = o_long + r256(4 * m), o_wide = o_mid + r256(4 * m);
+    const int64_t o_scr = o_wide + r256(4 * m);
     const int64_t o_ctr = o_scr + r256(4 * (nnz > 0 ? nnz : 1)), o_tsum = o_ctr + 256;
     const int64_t bytes = o_tsum + 8 * (ntiles + 1);
     char *buf = (char *)ctx_alloc(ctx, S_DSORT, (size_t)bytes);
     if (!dcolptr || !buf) return OPH_ERR_OOM;
     int *cnt = (int *)buf, *long_list = (int *)(buf + o_long), *mid_list = (int *)(buf + o_mid);
+    int *wide_list = (int *)(buf + o_wide);
     int *scratch = (int *)(buf + o_scr);
     int *ctr = (int *)(buf + o_ctr);
     long long *tsum = (long long *)(buf + o_tsum);
@@ -653,11 +680,12 @@ int dual_setup(Context *ctx, const Work &w, Work &wd) {
     k_dual_scatter<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, dcolptr, cnt, wd.pool);
     k_dual_finish<<<gm, 256, 0, s>>>(dcolptr, w.colptr, m, wd.pool, wd.seg, wd.low, wd.dim, mid_list, &ctr[2]);
     k_dual_finish_warp<<<ctx->sm_count * 8, FIN_WARPS * 32, 0, s>>>(dcolptr, wd.pool, wd.low, mid_list, &ctr[2],
-                                                                  long_list, &ctr[0]);
+                                                                  wide_list, &ctr[3], long_list, &ctr[0]);
+    k_dual_finish_wide<<<ctx->sm_count * 4, FIN_WARPS * 32, 0, s>>>(dcolptr, wd.pool, wd.low, wide_list, &ctr[3]);
     k_dual_sort_long<<<ctx->sm_count, LS_THREADS, 0, s>>>(dcolptr, wd.pool, wd.low, long_list, &ctr[0], &ctr[1],
                                                           scratch);
     k_dual_rec<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, wd.rec, wd.beta);
-    ctx->launches += 9;
+    ctx->launches += 10;
     OPH_CUDA_TRY(cudaGetLastError());
     return OPH_OK;
 }

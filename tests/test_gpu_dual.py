@@ -163,11 +163,12 @@ def fan(n_rim, seed):
     return BoundaryMatrix.from_columns(cols)
 
 
-@pytest.mark.parametrize("n_rim", [40, 700, 3000, 20000])
+@pytest.mark.parametrize("n_rim", [12, 40, 200, 700, 3000, 20000])
 def test_transpose_long_columns(dctx, n_rim):
-    """Columns of the anti-transpose of every length class: <= 32 rows (a
-    warp's registers), <= 1024 (a warp in shared memory) and beyond (a CTA's
-    radix sort, several tiles of it at 20,000 rows)."""
+    """Columns of the anti-transpose of every length class: <= 8 rows (a
+    thread), <= 32 and <= 128 (a warp's registers, 1 or 4 values a lane),
+    <= 256 (8 values a lane) and beyond (a CTA's radix sort, several tiles
+    of it at 20,000 rows)."""
     bm = fan(n_rim, seed=n_rim)
     dctx.set_dual("always")
     low, ess, info = dctx.reduce(bm, "pms")
