@@ -40,9 +40,9 @@
 //   finish   a thread per column of D': the segment header, the bucket of
 //            D's column in the reversed position, and for a column of at
 //            most 8 rows its rows sorted in registers and its low; then a
-//            warp per longer column of at most 256 rows (a bitonic network
-//            over the warp's registers, up to 8 values a lane; longer ones
-//            are queued)
+//            warp per longer column of at most 1024 rows (a bitonic network
+//            over the warp's registers, up to 8 values a lane, or over its
+//            slice of shared memory; longer ones are queued)
 //   long     a CTA per queued column: LSD radix sort, 8-bit digits, through
 //            a scratch range at the column's own offsets
 //   records  per row of D': its pivot record reset with left[] (row m-1-j of
@@ -313,7 +313,7 @@ __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t
     }
 }
 
-constexpr int FIN_WARPS = 8, SHORT_COL = 8, LONG_COL = 256;
+constexpr int FIN_WARPS = 8, SHORT_COL = 8, WIDE_COL = 256, LONG_COL = 1024;
 
 // a thread per column of D': the segment header, the bucket of D's column in
 // the reversed position, and for a column of at most SHORT_COL rows its rows
@@ -460,23 +460,57 @@ __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_warp(const int64
     }
 }
 
-// the same for the queued columns of MID_COL < n <= LONG_COL rows (eight
-// values a lane)
+// the same for the queued columns of MID_COL < n <= LONG_COL rows: eight
+// values a lane up to WIDE_COL rows, else a bitonic network over the warp's
+// slice of shared memory
 __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_wide(const int64_t *__restrict__ dcolptr,
                                                                      int *__restrict__ pool,
                                                                      int32_t *__restrict__ low,
                                                                      const int *__restrict__ wide_list,
                                                                      const int *wide_count) {
+    __shared__ int sbuf[FIN_WARPS][LONG_COL];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int64_t nwarps = (int64_t)gridDim.x * FIN_WARPS;
     const int count = *wide_count;
+    int *B = sbuf[wid];
     for (int64_t idx = blockIdx.x * (int64_t)FIN_WARPS + wid; idx < count; idx += nwarps) {
         const int64_t c = wide_list[idx];
         const int64_t a = dcolptr[c];
         const int n = (int)(dcolptr[c + 1] - a);
         int *R = pool + seg_start(c, a) + SEG_HDR;
-        const int top = warp_sort_column<8>(R, n);
-        if (lane == 0) low[c] = top;
+        if (n <= WIDE_COL) {
+            const int top = warp_sort_column<8>(R, n);
+            if (lane == 0) low[c] = top;
+            continue;
+        }
+        bool sorted = true;
+        for (int k = lane; k + 1 < n; k += 32) sorted &= R[k] < R[k + 1];
+        if (__all_sync(0xffffffffu, sorted)) {
+            if (lane == 0) low[c] = R[n - 1];
+            continue;
+        }
+        int N = 2 * WIDE_COL;
+        while (N < n) N <<= 1;
+        for (int k = lane; k < N; k += 32) B[k] = k < n ? R[k] : INT_MAX;
+        __syncwarp();
+        for (int size = 2; size <= N; size <<= 1)
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                for (int i = lane; i < N; i += 32) {
+                    const int l = i ^ stride;
+                    if (l > i) {
+                        const bool up = (i & size) == 0;
+                        const int x = B[i], y = B[l];
+                        if ((x > y) == up) {
+                            B[i] = y;
+                            B[l] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        for (int k = lane; k < n; k += 32) R[k] = B[k];
+        if (lane == 0) low[c] = B[n - 1];
+        __syncwarp();  // B is reused by the warp's next column
     }
 }
 
