@@ -149,8 +149,10 @@ int oph_reduce_batch_device(oph_context *ctx, int algo, int32_t count, const int
  * one block-diagonal column space, admits queued requests between sweeps
  * while they fit in the device arena (budget_bytes of HBM, allocated up
  * front), and releases each request as soon as it has converged.  At most
- * max_active requests are on the device at once.  Results are identical to
- * a single-matrix pms reduction of the same matrix.
+ * max_active requests are on the device at once.  Each request is reduced on
+ * the matrix a single-matrix pms reduction would choose for it (OPH_DUAL_AUTO
+ * below: a Rips-like request through its anti-transpose, built at
+ * admission), and the results are identical to that reduction's.
  */
 typedef struct oph_server oph_server;
 
@@ -167,6 +169,7 @@ typedef struct {
 typedef struct {
     int64_t completed, pending, active, sweeps, regrows;
     int64_t pool_bytes_in_use, columns_in_use, arena_bytes;
+    int64_t dual_admitted;  /* requests reduced through their anti-transpose */
 } oph_server_counters;
 
 int oph_server_create(int device, int64_t budget_bytes, int32_t max_active, oph_server **out);

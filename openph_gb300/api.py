@@ -51,7 +51,7 @@ class RequestInfo(C.Structure):
 
 class ServerCounters(C.Structure):
     _fields_ = [(k, C.c_int64) for k in ("completed", "pending", "active", "sweeps", "regrows", "pool_bytes_in_use",
-                                         "columns_in_use", "arena_bytes")]
+                                         "columns_in_use", "arena_bytes", "dual_admitted")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

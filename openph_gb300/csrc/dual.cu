@@ -289,13 +289,13 @@ __device__ __forceinline__ int64_t seg_start(int64_t c, int64_t off) { return 8 
 // equal targets within the warp take their slots with one atomic
 __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                                const int64_t *__restrict__ dcolptr, int *__restrict__ cursor,
-                               int *__restrict__ pool) {
+                               int *__restrict__ pool, int roff) {
     const int lane = threadIdx.x & 31;
     for (int64_t j0 = blockIdx.x * (int64_t)blockDim.x; j0 < m; j0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = j0 + threadIdx.x;
         const int64_t lo = j < m ? colptr[j] : 0, hi = j < m ? colptr[j + 1] : 0;
         const int n = (int)(hi - lo);
-        const int val = (int)(m - 1 - j);
+        const int val = roff + (int)(m - 1 - j);
         const int nmax = __reduce_max_sync(0xffffffffu, n);
         for (int t = 0; t < nmax; t++) {
             const int c = t < n ? (int)(m - 1 - rows[lo + t]) : -1;
@@ -320,7 +320,8 @@ constexpr int FIN_WARPS = 8, SHORT_COL = 8, WIDE_COL = 256, LONG_COL = 1024;
 // sorted (in registers) and its low; longer columns are queued for warps
 __global__ void k_dual_finish(const int64_t *__restrict__ dcolptr, const int64_t *__restrict__ colptr, int64_t m,
                               int *__restrict__ pool, int64_t *__restrict__ seg, int32_t *__restrict__ low,
-                              int8_t *__restrict__ dim, int *__restrict__ mid_list, int *mid_count) {
+                              int8_t *__restrict__ dim, int *__restrict__ mid_list, int *mid_count,
+                              int64_t seg_base) {
     for (int64_t c0 = blockIdx.x * (int64_t)blockDim.x; c0 < m; c0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = c0 + threadIdx.x;
         bool queue = false;
@@ -330,7 +331,7 @@ __global__ void k_dual_finish(const int64_t *__restrict__ dcolptr, const int64_t
             const int64_t s = seg_start(c, a), e = seg_start(c + 1, b);
             int *R = pool + s + SEG_HDR;
             *reinterpret_cast<int4 *>(pool + s) = make_int4(n, (int)(e - s - SEG_HDR), 0, 0);
-            seg[c] = s;
+            seg[c] = seg_base + s;
             const int64_t i = m - 1 - c;
             const int64_t nd = colptr[i + 1] - colptr[i];
             dim[c] = (int8_t)(nd - 1 > 126 ? 126 : nd - 1);
@@ -601,15 +602,15 @@ __global__ void __launch_bounds__(LS_THREADS) k_dual_sort_long(const int64_t *__
 // per row i of D' (column j = m-1-i of D): the pivot record reset, left[i] =
 // m-1-low_D(j) (or -1 for an empty column), beta[left] = the largest row
 __global__ void k_dual_rec(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                           PivRec *__restrict__ rec, int32_t *__restrict__ beta) {
+                           PivRec *__restrict__ rec, int32_t *__restrict__ beta, int roff) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = m - 1 - i;
         const int64_t lo = colptr[j], hi = colptr[j + 1];
         const int l = hi > lo ? (int)(m - 1 - rows[hi - 1]) : -1;
         int4 *r = reinterpret_cast<int4 *>(rec + i);
-        r[0] = make_int4(-1, 0, l, (int)SEG4_NONE);
+        r[0] = make_int4(-1, 0, l >= 0 ? roff + l : -1, (int)SEG4_NONE);
         r[1] = make_int4(-1, -1, -1, -1);
-        if (l >= 0) atomicMax(&beta[l], (int)i);
+        if (l >= 0) atomicMax(&beta[l], roff + (int)i);
     }
 }
 
@@ -626,31 +627,34 @@ __global__ void k_dual_low(const int32_t *__restrict__ low_d, int64_t m, int32_t
     }
 }
 
-static int grid_of(Context *ctx, int64_t n) {
-    int64_t g = (n + 255) / 256, cap = (int64_t)ctx->sm_count * 16;
+static int grid_of(int sm_count, int64_t n) {
+    int64_t g = (n + 255) / 256, cap = (int64_t)sm_count * 16;
     return (int)std::max<int64_t>(1, std::min(g, cap));
 }
+static int grid_of(Context *ctx, int64_t n) { return grid_of(ctx->sm_count, n); }
 
-int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input) {
+struct Grade {
+    unsigned long long count[MAXC];
+    int tab[MAXC];
+    int mixed, bad;
+};
+
+size_t dual_grade_tmp_bytes(int64_t m) { return sizeof(Grade) + 256 + (size_t)(m > 0 ? m : 1); }
+
+int dual_grade(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m, int64_t nnz,
+               int mode, void *tmp, bool *use, bool *bad_input, int *launches) {
     *use = false;
     *bad_input = false;
-    if (mode == OPH_DUAL_NEVER || w.m == 0) return OPH_OK;
-    cudaStream_t s = ctx->stream;
-    struct Grade {
-        unsigned long long count[MAXC];
-        int tab[MAXC];
-        int mixed, bad;
-    };
-    Grade *d = (Grade *)ctx_alloc(ctx, S_DGRADE, sizeof(Grade));
-    if (!d) return OPH_ERR_OOM;
+    if (mode == OPH_DUAL_NEVER || m == 0) return OPH_OK;
+    Grade *d = (Grade *)tmp;
+    int8_t *bucket = (int8_t *)tmp + ((sizeof(Grade) + 255) & ~(size_t)255);
     Grade init{};
     for (int b = 0; b < MAXC; b++) init.tab[b] = TAB_NONE;
     OPH_CUDA_TRY(cudaMemcpyAsync(d, &init, sizeof(Grade), cudaMemcpyHostToDevice, s));
-    // the buckets go through w.dim, which the set-up rewrites afterwards
-    k_dual_buckets<<<grid_of(ctx, w.m), 256, 0, s>>>(w.colptr, w.m, w.dim);
-    k_dual_grade<<<grid_of(ctx, w.m), 256, 0, s>>>(w.colptr, w.rows, w.m, w.nnz, w.dim, d->count, d->tab,
-                                                    &d->mixed, &d->bad);
-    ctx->launches += 2;
+    k_dual_buckets<<<grid_of(sm_count, m), 256, 0, s>>>(colptr, m, bucket);
+    k_dual_grade<<<grid_of(sm_count, m), 256, 0, s>>>(colptr, rows, m, nnz, bucket, d->count, d->tab, &d->mixed,
+                                                       &d->bad);
+    if (launches) *launches += 2;
     OPH_CUDA_TRY(cudaGetLastError());
     Grade g;
     OPH_CUDA_TRY(cudaMemcpyAsync(&g, d, sizeof(Grade), cudaMemcpyDeviceToHost, s));
@@ -671,57 +675,116 @@ int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_inpu
             hi = b;
         }
     if (mode == OPH_DUAL_ALWAYS) *use = true;
-    else *use = w.m >= DUAL_MIN_M && lo >= 0 && hi > lo && g.count[lo] * DUAL_RATIO <= g.count[hi];
+    else *use = m >= DUAL_MIN_M && lo >= 0 && hi > lo && g.count[lo] * DUAL_RATIO <= g.count[hi];
+    return OPH_OK;
+}
+
+int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input) {
+    *use = false;
+    *bad_input = false;
+    if (mode == OPH_DUAL_NEVER || w.m == 0) return OPH_OK;
+    void *tmp = ctx_alloc(ctx, S_DGRADE, dual_grade_tmp_bytes(w.m));
+    if (!tmp) return OPH_ERR_OOM;
+    return dual_grade(ctx->stream, ctx->sm_count, w.colptr, w.rows, w.m, w.nnz, mode, tmp, use, bad_input,
+                      &ctx->launches);
+}
+
+bool host_prefers_dual(int64_t m, const int64_t *colptr, const int32_t *rows) {
+    if (m < DUAL_MIN_M) return false;
+    unsigned long long count[MAXC] = {};
+    int tab[MAXC];
+    for (int b = 0; b < MAXC; b++) tab[b] = TAB_NONE;
+    auto bucket = [&](int64_t c) { return (int)std::min<int64_t>(colptr[c + 1] - colptr[c] - 1, 126); };
+    for (int64_t j = 0; j < m; j++) {
+        const int b = bucket(j);
+        if (b + 1 >= MAXC) return false;
+        count[b + 1]++;
+        if (colptr[j + 1] == colptr[j]) continue;
+        const int rb = bucket(rows[colptr[j]]);
+        for (int64_t k = colptr[j] + 1; k < colptr[j + 1]; k++)
+            if (bucket(rows[k]) != rb) return false;
+        if (tab[b + 1] == TAB_NONE) tab[b + 1] = rb;
+        else if (tab[b + 1] != rb) return false;
+    }
+    for (int a = 0; a < MAXC; a++)
+        for (int b = a + 1; b < MAXC; b++)
+            if (tab[a] != TAB_NONE && tab[a] == tab[b]) return false;
+    int lo = -1, hi = -1;
+    for (int b = 0; b < MAXC; b++)
+        if (count[b]) {
+            if (lo < 0) lo = b;
+            hi = b;
+        }
+    return lo >= 0 && hi > lo && count[lo] * DUAL_RATIO <= count[hi];
+}
+
+// Layout of the transpose's temporaries: the column offsets of D', the counts
+// (then the cursors), the three queues of longer columns, the radix sort's
+// scratch, four counters and the scan's tile sums.
+struct DualTmp {
+    int64_t o_dcolptr, o_cnt, o_long, o_mid, o_wide, o_scr, o_ctr, o_tsum, bytes;
+    DualTmp(int64_t m, int64_t nnz) {
+        auto r256 = [](int64_t b) { return (b + 255) & ~255ll; };
+        const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
+        o_dcolptr = 0;
+        o_cnt = r256(8 * (m + 1));
+        o_long = o_cnt + r256(4 * m);
+        o_mid = o_long + r256(4 * m);
+        o_wide = o_mid + r256(4 * m);
+        o_scr = o_wide + r256(4 * m);
+        o_ctr = o_scr + r256(4 * (nnz > 0 ? nnz : 1));
+        o_tsum = o_ctr + 256;
+        bytes = o_tsum + 8 * (ntiles + 1);
+    }
+};
+
+size_t dual_tmp_bytes(int64_t m, int64_t nnz) { return (size_t)DualTmp(m, nnz).bytes; }
+
+int dual_build_store(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m,
+                     int64_t nnz, int *pool, int64_t seg_base, int roff, int64_t *seg, int32_t *low, int8_t *dim,
+                     PivRec *rec, int32_t *beta, void *tmp, int *launches) {
+    if (m == 0) return OPH_OK;
+    const DualTmp L(m, nnz);
+    char *buf = (char *)tmp;
+    int64_t *dcolptr = (int64_t *)(buf + L.o_dcolptr);
+    int *cnt = (int *)(buf + L.o_cnt), *long_list = (int *)(buf + L.o_long), *mid_list = (int *)(buf + L.o_mid);
+    int *wide_list = (int *)(buf + L.o_wide), *scratch = (int *)(buf + L.o_scr), *ctr = (int *)(buf + L.o_ctr);
+    long long *tsum = (long long *)(buf + L.o_tsum);
+    const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
+    OPH_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * m, s));
+    OPH_CUDA_TRY(cudaMemsetAsync(ctr, 0, 256, s));
+    OPH_CUDA_TRY(cudaMemsetAsync(beta, 0xff, sizeof(int32_t) * m, s));
+    const int gm = grid_of(sm_count, m);
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)sm_count * 2));
+    k_dual_count<<<gm, 256, 0, s>>>(colptr, rows, m, cnt);
+    k_scan_sums<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum);
+    k_scan_tsums<<<1, SCAN_THREADS, 0, s>>>(tsum, ntiles, dcolptr + m);
+    k_scan_apply<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum, dcolptr);
+    k_dual_scatter<<<gm, 256, 0, s>>>(colptr, rows, m, dcolptr, cnt, pool, roff);
+    k_dual_finish<<<gm, 256, 0, s>>>(dcolptr, colptr, m, pool, seg, low, dim, mid_list, &ctr[2], seg_base);
+    k_dual_finish_warp<<<sm_count * 8, FIN_WARPS * 32, 0, s>>>(dcolptr, pool, low, mid_list, &ctr[2], wide_list,
+                                                             &ctr[3], long_list, &ctr[0]);
+    k_dual_finish_wide<<<sm_count * 4, FIN_WARPS * 32, 0, s>>>(dcolptr, pool, low, wide_list, &ctr[3]);
+    k_dual_sort_long<<<sm_count, LS_THREADS, 0, s>>>(dcolptr, pool, low, long_list, &ctr[0], &ctr[1], scratch);
+    k_dual_rec<<<gm, 256, 0, s>>>(colptr, rows, m, rec, beta, roff);
+    if (launches) *launches += 10;
+    OPH_CUDA_TRY(cudaGetLastError());
     return OPH_OK;
 }
 
 int dual_setup(Context *ctx, const Work &w, Work &wd) {
-    cudaStream_t s = ctx->stream;
-    const int64_t m = w.m, nnz = w.nnz;
     wd = w;
     wd.ascending = true;
     wd.checked = true;
     wd.rows = nullptr;
+    wd.colptr = nullptr;
     int rc = init_store(ctx, wd);
     if (rc) return rc;
-    if (m == 0) return OPH_OK;
-    int64_t *dcolptr = (int64_t *)ctx_alloc(ctx, S_DCOLPTR, sizeof(int64_t) * (m + 1));
-    // cnt (then the cursors), the long-column list, the radix sort's
-    // scratch, two counters and the scan's tile sums, in one buffer
-    const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
-    auto r256 = [](int64_t b) { return (b + 255) & ~255ll; };
-    const int64_t o_long = r256(4 * m), o_mid = o_long + r256(4 * m), o_wide = o_mid + r256(4 * m);
-    const int64_t o_scr = o_wide + r256(4 * m);
-    const int64_t o_ctr = o_scr + r256(4 * (nnz > 0 ? nnz : 1)), o_tsum = o_ctr + 256;
-    const int64_t bytes = o_tsum + 8 * (ntiles + 1);
-    char *buf = (char *)ctx_alloc(ctx, S_DSORT, (size_t)bytes);
-    if (!dcolptr || !buf) return OPH_ERR_OOM;
-    int *cnt = (int *)buf, *long_list = (int *)(buf + o_long), *mid_list = (int *)(buf + o_mid);
-    int *wide_list = (int *)(buf + o_wide);
-    int *scratch = (int *)(buf + o_scr);
-    int *ctr = (int *)(buf + o_ctr);
-    long long *tsum = (long long *)(buf + o_tsum);
-    wd.colptr = dcolptr;
-    OPH_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * m, s));
-    OPH_CUDA_TRY(cudaMemsetAsync(ctr, 0, 256, s));
-    OPH_CUDA_TRY(cudaMemsetAsync(wd.beta, 0xff, sizeof(int32_t) * m, s));
-    const int gm = grid_of(ctx, m);
-    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 2));
-    k_dual_count<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, cnt);
-    k_scan_sums<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum);
-    k_scan_tsums<<<1, SCAN_THREADS, 0, s>>>(tsum, ntiles, dcolptr + m);
-    k_scan_apply<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum, dcolptr);
-    k_dual_scatter<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, dcolptr, cnt, wd.pool);
-    k_dual_finish<<<gm, 256, 0, s>>>(dcolptr, w.colptr, m, wd.pool, wd.seg, wd.low, wd.dim, mid_list, &ctr[2]);
-    k_dual_finish_warp<<<ctx->sm_count * 8, FIN_WARPS * 32, 0, s>>>(dcolptr, wd.pool, wd.low, mid_list, &ctr[2],
-                                                                  wide_list, &ctr[3], long_list, &ctr[0]);
-    k_dual_finish_wide<<<ctx->sm_count * 4, FIN_WARPS * 32, 0, s>>>(dcolptr, wd.pool, wd.low, wide_list, &ctr[3]);
-    k_dual_sort_long<<<ctx->sm_count, LS_THREADS, 0, s>>>(dcolptr, wd.pool, wd.low, long_list, &ctr[0], &ctr[1],
-                                                          scratch);
-    k_dual_rec<<<gm, 256, 0, s>>>(w.colptr, w.rows, m, wd.rec, wd.beta);
-    ctx->launches += 10;
-    OPH_CUDA_TRY(cudaGetLastError());
-    return OPH_OK;
+    if (w.m == 0) return OPH_OK;
+    void *tmp = ctx_alloc(ctx, S_DSORT, dual_tmp_bytes(w.m, w.nnz));
+    if (!tmp) return OPH_ERR_OOM;
+    return dual_build_store(ctx->stream, ctx->sm_count, w.colptr, w.rows, w.m, w.nnz, wd.pool, 0, 0, wd.seg, wd.low,
+                            wd.dim, wd.rec, wd.beta, tmp, &ctx->launches);
 }
 
 int dual_lows(Context *ctx, const Work &wd, int32_t **low) {

@@ -87,6 +87,22 @@ constexpr unsigned long long DUAL_RATIO = 8;
 constexpr int64_t DUAL_MIN_M = 1 << 17;
 int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input);
 int dual_setup(Context *ctx, const Work &w, Work &wd);
+// The same pieces for callers with their own buffers (the request server):
+// dual_grade grades a device CSC (synchronous; tmp of dual_grade_tmp_bytes);
+// host_prefers_dual makes the automatic choice on a host CSC;
+// dual_build_store writes the anti-transpose of a device CSC of m columns
+// into the column store at pool (its segments recorded as seg_base + offset,
+// its rows shifted by roff), with low, seg, dim, the pivot records and beta
+// of its columns (each array given from the matrix's first column; tmp of
+// dual_tmp_bytes).
+size_t dual_grade_tmp_bytes(int64_t m);
+int dual_grade(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m, int64_t nnz,
+               int mode, void *tmp, bool *use, bool *bad_input, int *launches);
+bool host_prefers_dual(int64_t m, const int64_t *colptr, const int32_t *rows);
+size_t dual_tmp_bytes(int64_t m, int64_t nnz);
+int dual_build_store(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m,
+                     int64_t nnz, int *pool, int64_t seg_base, int roff, int64_t *seg, int32_t *low, int8_t *dim,
+                     PivRec *rec, int32_t *beta, void *tmp, int *launches);
 int dual_lows(Context *ctx, const Work &wd, int32_t **low);
 
 // capi.cu
@@ -144,7 +160,7 @@ struct Context {
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_IASC, S_IBUCKET, S_IOPEN, S_RANGES, S_NSLOTS
 };
 
 }  // namespace oph

@@ -276,6 +276,9 @@ __device__ __forceinline__ void k_p1_mark_tile(PmsArgs a, const int64_t n, const
         pre[d] = max(pre[d], c);
     }
     int keep = 0;
+    int icur = -1, icnt[MAXC];  // per-instance bucket counts (a.ibucket)
+#pragma unroll
+    for (int d = 0; d < MAXC; d++) icnt[d] = 0;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
         const int64_t idx = base + t;
@@ -304,6 +307,33 @@ __device__ __forceinline__ void k_p1_mark_tile(PmsArgs a, const int64_t n, const
         }
         keep += kept;
         if (kept && a.ascending) atomicAdd(&sunres[bkt[t]], 1);
+        if (kept && a.ibucket) {
+            const int ib = a.inst[j];
+            if (a.iasc[ib]) {
+                if (ib != icur) {  // flush the previous instance's counts
+                    if (icur >= 0)
+#pragma unroll
+                        for (int d = 0; d < MAXC; d++)
+                            if (icnt[d]) atomicAdd(&a.ibucket[icur * MAXC + d], icnt[d]);
+#pragma unroll
+                    for (int d = 0; d < MAXC; d++) icnt[d] = 0;
+                    icur = ib;
+                }
+#pragma unroll
+                for (int d = 0; d < MAXC; d++)
+                    if (d == bkt[t]) icnt[d]++;
+            }
+        }
+    }
+    if (a.ibucket) {
+        // the warp's threads on one instance add their counts once
+        const unsigned peers = __match_any_sync(0xffffffffu, icur);
+        const bool leader = lane == __ffs(peers) - 1;
+#pragma unroll
+        for (int d = 0; d < MAXC; d++) {
+            const int c = __reduce_add_sync(peers, icnt[d]);
+            if (leader && icur >= 0 && c) atomicAdd(&a.ibucket[icur * MAXC + d], c);
+        }
     }
     if (a.ulist) {
         if (keep) atomicAdd(&skeep, keep);
@@ -363,6 +393,18 @@ __global__ void k_p1_kscan(PmsArgs a) {
                 a.st->bucket_unres[d] = 0;
             }
             a.st->bucket_open = open;
+        }
+    }
+    if (a.iopen) {
+        // per instance: the lowest bucket with unresolved columns opens
+        // (counts of this sweep's k_p1_mark, cleared for the next one)
+        for (int b = threadIdx.x; b < a.nslots; b += blockDim.x) {
+            int open = MAXC;
+            for (int d = MAXC - 1; d >= 0; d--) {
+                if (a.ibucket[b * MAXC + d] > 0) open = d;
+                a.ibucket[b * MAXC + d] = 0;
+            }
+            a.iopen[b] = a.iasc[b] ? open : MAXC;
         }
     }
 }
@@ -434,7 +476,8 @@ __device__ __forceinline__ void k_p1_scatter_tile(PmsArgs a, const int64_t n, co
     const int open = a.ascending ? __ldcg(&a.st->bucket_open) : MAXC;
 #pragma unroll
     for (int t = 0; t < P1_ITEMS; t++) {
-        const bool want = ((keepmask >> t) & 1u) && a.dim[cols[t]] + 1 <= open &&
+        const bool kept = (keepmask >> t) & 1u;
+        const bool want = kept && a.dim[cols[t]] + 1 <= (a.iopen ? a.iopen[a.inst[cols[t]]] : open) &&
                           (!OPH_P2_FILTER || p2_ready(a, cols[t]));
         warp_append(want, cols[t], a.worklist, &a.st->t_count[0]);
     }

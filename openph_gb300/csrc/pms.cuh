@@ -50,6 +50,15 @@ struct PmsArgs {
     // tier 3 merges)
     uint32_t *bm;
     int64_t bm_words;
+    // per-instance bucket order (the server, whose instances are reduced on
+    // D or on their anti-transpose; nullptr: `ascending` above for all):
+    // iasc[b] = 1 for an instance in ascending order, ibucket[b * MAXC + d]
+    // its unresolved columns of bucket d seen by this sweep's Phase I, and
+    // iopen[b] the highest bucket its Phase II takes (MAXC: every bucket)
+    const int8_t *iasc;
+    int *ibucket;
+    int *iopen;
+    int nslots;
 };
 
 // Launch geometry of the Phase II tiers (occupancy-derived, per device).

@@ -16,7 +16,17 @@
 //   * regrows the pool region of any request whose column store overflowed
 //     (copy, then rebase its segments and its pivot records).
 // A request therefore joins the running batch at the next sweep boundary and
-// leaves it as soon as it converges.  The reduction of a request is the
+// leaves it as soon as it converges.
+//
+// Each request is reduced on the matrix plain pms would choose for it alone
+// (the automatic rule of dual.cu, decided at submission): a Rips-like
+// request goes through its anti-transpose, built at admission straight into
+// its own column range and pool region, with its dimension buckets in
+// ascending order (per instance: iasc / ibucket / iopen); the others on D.
+// Phase I visits only the unresolved columns: a list in column order,
+// compacted by every sweep, into which each admitted request's column range
+// is merged (k_srv_merge).  A retired request's columns leave the list in
+// the next sweep, and only then is its column range handed out again.  The reduction of a request is the
 // same whether it runs alone or in the mix: block-diagonal columns never add
 // into each other, and the lows of a reduced matrix are unique.
 #include <algorithm>
@@ -96,6 +106,7 @@ struct Request {
     double t_submit = 0, t_admit = 0, t_done = 0;
     int sweeps = 0, status = OPH_OK, slot = -1;
     bool done = false;
+    bool dual = false;  // reduced through its anti-transpose
     int64_t c0 = -1, reg = -1, reg_ints = 0;
 };
 
@@ -140,6 +151,53 @@ __global__ void k_srv_init(const int64_t *__restrict__ colptr, const int32_t *__
     }
 }
 
+// Admission of a request reduced through its anti-transpose: the per-column
+// state that dual_build_store does not write.
+__global__ void k_srv_init_cols(int64_t m, int64_t c0, int b, PmsArgs a) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = c0 + jj;
+        a.inst[j] = b;
+        a.classes[j] = 0;
+        a.clear[j] = 0;
+        a.first[j] = FIRST_NONE;
+    }
+}
+
+// The Phase I list with this round's admitted column ranges merged in: the
+// sorted list `in` (*in_count columns) and the ranges [r0[q], r0[q] + len of
+// q) (ascending, disjoint from every listed column; pre[q] = columns of the
+// ranges before q, pre[K] = all of them) into the sorted list `out`.
+__global__ void k_srv_merge(const int32_t *__restrict__ in, const int *in_count, const int64_t *__restrict__ r0,
+                            const int64_t *__restrict__ pre, int K, int32_t *__restrict__ out, int *out_count) {
+    const int64_t n_in = *in_count, total = pre[K], N = n_in + total;
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < N; x += (int64_t)gridDim.x * blockDim.x) {
+        if (x < n_in) {
+            const int v = in[x];
+            int lo = 0, hi = K;  // ranges starting below v
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (r0[mid] < v) lo = mid + 1; else hi = mid;
+            }
+            out[x + pre[lo]] = v;
+        } else {
+            const int64_t y = x - n_in;
+            int lo = 0, hi = K - 1;  // the range holding admitted column y
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (pre[mid] <= y) lo = mid; else hi = mid - 1;
+            }
+            const int64_t c = r0[lo] + (y - pre[lo]);
+            int64_t a = 0, z = n_in;  // listed columns below the range
+            while (a < z) {
+                const int64_t mid = (a + z) >> 1;
+                if (in[mid] < r0[lo]) a = mid + 1; else z = mid;
+            }
+            out[a + y] = (int32_t)c;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out_count = (int)N;
+}
+
 __global__ void k_srv_left(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
                            int64_t c0, PmsArgs a) {
     for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x)
@@ -167,6 +225,25 @@ __global__ void k_srv_out2(int64_t m, int64_t c0, PmsArgs a, int32_t *out) {
     for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
         const int l = a.low[c0 + jj];
         if (l >= 0) out[m + (l - c0)] = 0;
+    }
+}
+// The same for a request reduced through its anti-transpose: every pair
+// (column c, low r) of D' (local indices) is the pair (column m-1-r, low
+// m-1-c) of D; both ends of a pair are not essential.
+__global__ void k_srv_out_dual1(int64_t m, int32_t *out) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        out[jj] = -1;
+        out[m + jj] = 1;
+    }
+}
+__global__ void k_srv_out_dual2(int64_t m, int64_t c0, PmsArgs a, int32_t *out) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < m; c += (int64_t)gridDim.x * blockDim.x) {
+        const int l = a.low[c0 + c];
+        if (l < 0) continue;
+        const int64_t r = l - c0;
+        out[m - 1 - r] = (int32_t)(m - 1 - c);
+        out[m + (m - 1 - r)] = 0;
+        out[m + (m - 1 - c)] = 0;
     }
 }
 // ... then the columns become inert (no low, cleared, no instance).
@@ -216,6 +293,13 @@ struct Server {
     PmsArgs a{};
     SweepGrids g{};
     int *h_ireps = nullptr, *h_iover = nullptr;
+    // the Phase I list: lp = which of its two arrays is current; the ranges
+    // admitted this round (for k_srv_merge), their device copy; the column
+    // ranges of retired requests, free once a sweep has dropped them
+    int lp = 0;
+    std::vector<std::pair<int64_t, int64_t>> admitted_rng;
+    int64_t *d_rng = nullptr, *h_rng = nullptr;
+    std::vector<std::pair<int64_t, int64_t>> retired_cols;
     RangeAlloc cols, pool;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -226,7 +310,7 @@ struct Server {
     bool stop = false;
     int64_t next_ticket = 1;
     // statistics
-    int64_t completed = 0, sweeps = 0, admitted = 0, regrows = 0;
+    int64_t completed = 0, sweeps = 0, admitted = 0, regrows = 0, dual_admitted = 0;
     int error = OPH_OK;
 
     int64_t packed_ints(int64_t m, int64_t nnz) const { return 8 * (m + 1) + 4 * ((nnz + 3) / 4) + 64; }
@@ -245,13 +329,16 @@ struct Server {
         // a host submission is staged in the pool; a device one was copied
         // to its own buffer at submission
         const bool host = r->d_buf == nullptr;
-        const int64_t stage_ints = host ? 2 * (r->m + 1) + r->nnz + 4 : 0;
+        // staging: the host CSC, and the anti-transpose's temporaries
+        const int64_t tmp_ints = r->dual ? (int64_t)((dual_tmp_bytes(r->m, r->nnz) + 255) / 4) + 64 : 0;
+        const int64_t csc_ints = host ? 2 * (r->m + 1) + r->nnz + 4 : 0;
+        const int64_t stage_ints = csc_ints + tmp_ints;
         const int64_t reg_ints = region_ints(r->m, r->nnz);
         const int64_t c0 = cols.alloc(std::max<int64_t>(r->m, 1), 1);
         if (c0 < 0) return 1;
         const int64_t reg = pool.alloc(reg_ints, 64);
         if (reg < 0) { cols.release(c0, std::max<int64_t>(r->m, 1)); return 1; }
-        const int64_t stg = host ? pool.alloc(stage_ints, 64) : 0;
+        const int64_t stg = stage_ints ? pool.alloc(stage_ints, 64) : 0;
         if (stg < 0) {
             cols.release(c0, std::max<int64_t>(r->m, 1));
             pool.release(reg, reg_ints);
@@ -266,20 +353,33 @@ struct Server {
             cudaMemcpyAsync(d_colptr, r->colptr.data(), sizeof(int64_t) * (r->m + 1), cudaMemcpyHostToDevice, s);
             if (r->nnz) cudaMemcpyAsync(d_rows, r->rows.data(), sizeof(int32_t) * r->nnz, cudaMemcpyHostToDevice, s);
         }
-        if (r->m > 0) {
+        const int8_t asc = r->dual ? 1 : 0;
+        cudaMemcpyAsync(const_cast<int8_t *>(a.iasc) + b, &asc, 1, cudaMemcpyHostToDevice, s);
+        if (r->m > 0 && r->dual) {
+            // the anti-transpose, straight into the request's columns and
+            // region (rows shifted into its column range)
+            k_srv_init_cols<<<grid(r->m), 256, 0, s>>>(r->m, c0, b, a);
+            void *tmp = a.pool + stg + ((csc_ints + 63) & ~63ll);
+            dual_build_store(s, ctx->sm_count, d_colptr, d_rows, r->m, r->nnz, a.pool + reg, reg, (int)c0,
+                             a.seg + c0, a.low + c0, const_cast<int8_t *>(a.dim) + c0, a.rec + c0,
+                             const_cast<int32_t *>(a.beta) + c0, tmp, nullptr);
+        } else if (r->m > 0) {
             k_srv_init<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, b, reg, a);
             k_srv_left<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, a);
             k_srv_beta<<<grid(r->m), 256, 0, s>>>(r->m, c0, a);
         }
+        if (r->m > 0) admitted_rng.emplace_back(c0, r->m);
+        dual_admitted += r->dual ? 1 : 0;
         k_srv_set_region<<<1, 1, 0, s>>>(a.ipool, a.ireps, a.iover, b,
                                          (unsigned long long)(reg + packed_ints(r->m, r->nnz)),
                                          (unsigned long long)(reg + reg_ints));
         if (r->m > 0) launch_phase0(a, c0, c0 + r->m, grid(r->m), s);
-        if (host) {
-            // the staged input is read by the kernels above: its region is
-            // released after the sweep's synchronisation
+        if (stage_ints) {
+            // the staged input and temporaries are read by the kernels above:
+            // their region is released after the sweep's synchronisation
             staged.emplace_back(stg, stage_ints);
-        } else {
+        }
+        if (!host) {
             // the device copy is freed in stream order after those kernels
             cudaFreeAsync(r->d_buf, s);
             r->d_buf = nullptr;
@@ -307,8 +407,13 @@ struct Server {
             if (out >= 0) outs.emplace_back(out, 2 * m + 4);
             else out = r->reg;  // the request's own region is no longer read
             dptr[k] = a.pool + out;
-            k_srv_out1<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
-            k_srv_out2<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
+            if (r->dual) {
+                k_srv_out_dual1<<<grid(m), 256, 0, s>>>(m, dptr[k]);
+                k_srv_out_dual2<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
+            } else {
+                k_srv_out1<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
+                k_srv_out2<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
+            }
         }
         for (size_t k = 0; k < done.size(); k++) {
             Request *r = done[k];
@@ -323,7 +428,9 @@ struct Server {
         {
             std::lock_guard<std::mutex> lk(mu);
             for (Request *r : done) {
-                cols.release(r->c0, std::max<int64_t>(r->m, 1));
+                // its columns leave the Phase I list in the next sweep; the
+                // range is handed out again only after that
+                retired_cols.emplace_back(r->c0, std::max<int64_t>(r->m, 1));
                 pool.release(r->reg, r->reg_ints);
                 slots[r->slot] = nullptr;
                 r->t_done = t;
@@ -379,6 +486,14 @@ struct Server {
             // admission, first come first served
             int active = 0;
             for (auto *r : slots) active += r != nullptr;
+            if (active == 0) {
+                // nothing on the device: the list starts empty (retired
+                // columns left in it go too), and every range is free
+                cudaMemsetAsync(&a.st->ucount[lp], 0, sizeof(int), s);
+                std::lock_guard<std::mutex> lk(mu);
+                for (auto &rc : retired_cols) cols.release(rc.first, rc.second);
+                retired_cols.clear();
+            }
             for (;;) {
                 Request *r = nullptr;
                 {
@@ -411,6 +526,25 @@ struct Server {
                 }
                 continue;
             }
+            // the admitted ranges into the Phase I list (column order)
+            if (!admitted_rng.empty()) {
+                std::sort(admitted_rng.begin(), admitted_rng.end());
+                const int K = (int)admitted_rng.size();
+                int64_t acc = 0;
+                for (int q = 0; q < K; q++) {
+                    h_rng[q] = admitted_rng[q].first;
+                    h_rng[K + q] = acc;
+                    acc += admitted_rng[q].second;
+                }
+                h_rng[2 * K] = acc;
+                cudaMemcpyAsync(d_rng, h_rng, sizeof(int64_t) * (2 * K + 1), cudaMemcpyHostToDevice, s);
+                int32_t *L[2] = {a.ulist, a.ulist_next};
+                k_srv_merge<<<grid(acc + 4096), 256, 0, s>>>(L[lp], &a.st->ucount[lp], d_rng, d_rng + K, K,
+                                                             L[lp ^ 1], &a.st->ucount[lp ^ 1]);
+                lp ^= 1;
+                admitted_rng.clear();
+            }
+            const size_t retired_before = retired_cols.size();
             // one sweep over every active request
             int64_t hi = 0;
             for (auto *r : slots)
@@ -423,7 +557,8 @@ struct Server {
             gg.t = (int)std::max<int64_t>(1, std::min<int64_t>(sa.ntiles, (int64_t)ctx->sm_count * 8));
             cudaMemsetAsync(a.ireps, 0, sizeof(int) * max_slots, s);
             k_srv_sweep_reset<<<1, 1, 0, s>>>(a.st);
-            launch_sweep(sa, gg, s);
+            launch_sweep(sa, gg, s, lp);  // compacts list lp into the other one
+            lp ^= 1;
             cudaMemcpyAsync(h_ireps, a.ireps, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
             cudaMemcpyAsync(h_iover, a.iover, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
             if (cudaStreamSynchronize(s) != cudaSuccess) {
@@ -432,6 +567,12 @@ struct Server {
             }
             for (auto &st : staged) pool.release(st.first, st.second);
             staged.clear();
+            {
+                // columns retired before this sweep have left the list
+                std::lock_guard<std::mutex> lk(mu);
+                for (size_t q = 0; q < retired_before; q++) cols.release(retired_cols[q].first, retired_cols[q].second);
+                retired_cols.erase(retired_cols.begin(), retired_cols.begin() + retired_before);
+            }
             sweeps++;
             for (auto *r : slots)
                 if (r) r->sweeps++;
@@ -483,7 +624,7 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     // the arena: per-column arrays for mcap columns (a tenth of the budget)
     // and a segment pool for the rest (at most what 32-bit segment fields
     // address)
-    const int64_t per_col = 4 + 1 + 1 + 1 + 4 + 4 + 4 + 4 + 4 + 8 + (int64_t)sizeof(PivRec) + 4;
+    const int64_t per_col = 4 + 1 + 1 + 1 + 4 + 4 + 4 + 4 + 4 + 8 + (int64_t)sizeof(PivRec) + 4 + 8 + 1;
     sv->mcap = std::min<int64_t>(budget_bytes / 10 / per_col, (1ll << 29) - 1);
     int64_t pool_bytes = budget_bytes - sv->mcap * per_col - budget_bytes / 16;
     sv->pool_ints = std::min<int64_t>(pool_bytes / 4 - POOL_PAD, MAX_POOL_INTS - 1);
@@ -507,15 +648,31 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     a.iover = (int *)ctx_alloc(ctx, S_TMP, 4 * (size_t)max_active);
     a.st = (DevStatus *)ctx_alloc(ctx, S_STATUS, sizeof(DevStatus));
     a.pool = (int *)ctx_alloc(ctx, S_POOL, sizeof(int) * (sv->pool_ints + POOL_PAD));
-    bool ok = a.low && a.classes && a.clear && a.dim && a.first && a.beta && a.worklist && a.widelist &&
+    // the Phase I list (two arrays) and its per-tile counts
+    a.ulist = (int32_t *)ctx_alloc(ctx, S_ULIST, sizeof(int32_t) * 2 * mc);
+    a.ulist_next = a.ulist ? a.ulist + mc : nullptr;
+    a.kagg = (int32_t *)ctx_alloc(ctx, S_KAGG, sizeof(int32_t) * ((mc + 2047) / 2048 + 2));
+    // per-instance bucket order
+    a.iasc = (const int8_t *)ctx_alloc(ctx, S_IASC, (size_t)max_active);
+    a.ibucket = (int *)ctx_alloc(ctx, S_IBUCKET, sizeof(int) * MAXC * (size_t)max_active);
+    a.iopen = (int *)ctx_alloc(ctx, S_IOPEN, sizeof(int) * (size_t)max_active);
+    a.nslots = max_active;
+    sv->d_rng = (int64_t *)ctx_alloc(ctx, S_RANGES, sizeof(int64_t) * (2 * (size_t)max_active + 1));
+    // tier 3's bitmaps (one per CTA of its grid, a window of up to 2^23 rows)
+    a.bm_words = std::min<int64_t>(((mc + 32) / 32 + 3) & ~3ll, 1 << 18);
+    a.bm = (uint32_t *)ctx_alloc(ctx, S_BITMAP, sizeof(uint32_t) * (size_t)a.bm_words * ctx->sm_count);
+    bool ok = a.ulist && a.kagg && a.iasc && a.ibucket && a.iopen && sv->d_rng && a.bm && a.low && a.classes &&
+              a.clear && a.dim && a.first && a.beta && a.worklist && a.widelist &&
               a.slist && a.seg && a.rec && a.inst && a.agg && a.ipool && a.ireps && a.iover && a.st && a.pool;
     if (ok) ok = cudaMallocHost((void **)&sv->h_ireps, 4 * (size_t)max_active) == cudaSuccess &&
-                 cudaMallocHost((void **)&sv->h_iover, 4 * (size_t)max_active) == cudaSuccess;
+                 cudaMallocHost((void **)&sv->h_iover, 4 * (size_t)max_active) == cudaSuccess &&
+                 cudaMallocHost((void **)&sv->h_rng, sizeof(int64_t) * (2 * (size_t)max_active + 1)) == cudaSuccess;
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->sub_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
         if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
         if (sv->h_iover) cudaFreeHost(sv->h_iover);
+        if (sv->h_rng) cudaFreeHost(sv->h_rng);
         if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
         oph_context_destroy(raw);
         delete sv;
@@ -529,6 +686,9 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     cudaMemsetAsync(a.inst, 0xff, 4 * mc, s);
     cudaMemsetAsync(a.first, 0x7f, 4 * mc, s);
     cudaMemsetAsync(a.iover, 0, 4 * (size_t)max_active, s);
+    cudaMemsetAsync(a.ibucket, 0, sizeof(int) * MAXC * (size_t)max_active, s);
+    cudaMemsetAsync(const_cast<int8_t *>(a.iasc), 0, (size_t)max_active, s);
+    cudaMemsetAsync(a.bm, 0, sizeof(uint32_t) * (size_t)a.bm_words * ctx->sm_count, s);
     k_srv_inert<<<sv->grid(mc), 256, 0, s>>>(mc, 0, a);
     DevStatus init{};
     init.pool_used = 0;
@@ -566,6 +726,7 @@ __attribute__((visibility("default"))) int oph_server_submit(oph_server *sv, int
     Request *r = new Request();
     r->m = m;
     r->nnz = nnz;
+    r->dual = host_prefers_dual(m, colptr, rows);
     r->colptr.assign(colptr, colptr + m + 1);
     if (nnz) r->rows.assign(rows, rows + nnz);
     r->t_submit = now_ms();
@@ -620,10 +781,21 @@ __attribute__((visibility("default"))) int oph_server_submit_device(oph_server *
         cudaStreamSynchronize(s);
         return e != cudaSuccess ? OPH_ERR_CUDA : OPH_ERR_BAD_INPUT;
     }
+    // the matrix plain pms would reduce for this request, graded on the device
+    bool use = false, bad_g = false;
+    void *gtmp = nullptr;
+    if (m > 0 && cudaMallocAsync(&gtmp, dual_grade_tmp_bytes(m), s) == cudaSuccess) {
+        if (dual_grade(s, sv->ctx->sm_count, cp, rw, m, nnz, OPH_DUAL_AUTO, gtmp, &use, &bad_g, nullptr) != OPH_OK)
+            use = false;
+        cudaFreeAsync(gtmp, s);
+    } else {
+        cudaGetLastError();
+    }
     Request *r = new Request();
     r->m = m;
     r->nnz = nnz;
     r->d_buf = buf;
+    r->dual = use && !bad_g;
     r->t_submit = now_ms();
     {
         std::lock_guard<std::mutex> lk(sv->mu);
@@ -684,6 +856,7 @@ __attribute__((visibility("default"))) int oph_server_stats(oph_server *sv, oph_
     out->pool_bytes_in_use = sv->pool.used * 4;
     out->columns_in_use = sv->cols.used;
     out->arena_bytes = sv->budget;
+    out->dual_admitted = sv->dual_admitted;
     return OPH_OK;
 }
 
@@ -703,6 +876,7 @@ __attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
     if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
     if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
     if (sv->h_iover) cudaFreeHost(sv->h_iover);
+    if (sv->h_rng) cudaFreeHost(sv->h_rng);
     oph_context_destroy(reinterpret_cast<oph_context *>(sv->ctx));
     delete sv;
     return OPH_OK;

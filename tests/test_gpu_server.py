@@ -135,3 +135,70 @@ def test_device_submission_rejects_malformed(cuda_lib):
         good = DeviceMatrix(cp, torch.as_tensor(bm.rows, device="cuda"), None)
         low, _, _ = srv.wait(srv.submit_device(good))
     np.testing.assert_array_equal(low, oracle.twist(bm)[0])
+
+
+@pytest.fixture(scope="module")
+def dual_mix():
+    """Requests of at least 2^17 columns whose top dimension dwarfs the
+    bottom one (reduced through their anti-transpose, as a single-matrix
+    reduction would), a lower-star image of the same size (stays on D) and
+    small complexes, with the oracle's answers."""
+    reqs = [cx.rips_torus(400, 150_000, seed=41), cx.rips_cube(95, seed=42), cx.lower_star_image(160, 160, seed=43),
+            cx.rips_cube(20, seed=44), cx.rips_torus(60, 8000, seed=45), cx.rips_torus(400, 140_000, seed=46)]
+    return reqs, [oracle.twist(bm)[:2] for bm in reqs]
+
+
+def test_anti_transpose_requests_in_the_mix(cuda_lib, dual_mix):
+    reqs, want = dual_mix
+    with Context(0) as c:
+        alone = [c.reduce(bm, "pms") for bm in reqs]
+    with Server(0, budget_bytes=8 << 30, max_active=16) as srv:
+        tickets = [srv.submit(bm) for bm in reqs]
+        mixed = [srv.wait(t)[:2] for t in tickets]
+        st = srv.stats()
+    assert st["dual_admitted"] == sum(info["dual"] for _, _, info in alone) == 3
+    for (wl, we), (lm, em), (la, ea, _) in zip(want, mixed, alone):
+        np.testing.assert_array_equal(lm, wl)
+        np.testing.assert_array_equal(em, we)
+        np.testing.assert_array_equal(lm, la)
+
+
+def test_anti_transpose_requests_arriving_while_running(cuda_lib, dual_mix):
+    """The same requests, twice over, submitted from another thread while
+    earlier ones are on the device; small arenas of columns force retired
+    column ranges to be handed out again."""
+    reqs, want = dual_mix
+    order = [0, 3, 1, 4, 2, 5] * 2
+    out = {}
+    with Server(0, budget_bytes=4 << 30, max_active=4) as srv:
+        def producer():
+            for k, i in enumerate(order):
+                out[k] = srv.submit(reqs[i])
+                time.sleep(0.002)
+        th = threading.Thread(target=producer)
+        th.start()
+        th.join()
+        res = {k: srv.wait(t) for k, t in out.items()}
+        st = srv.stats()
+    assert st["dual_admitted"] == 6
+    for k, i in enumerate(order):
+        np.testing.assert_array_equal(res[k][0], want[i][0])
+        np.testing.assert_array_equal(res[k][1], want[i][1])
+
+
+def test_anti_transpose_device_submission(cuda_lib, dual_mix):
+    torch = pytest.importorskip("torch")
+    reqs, want = dual_mix
+
+    class Dev:
+        def __init__(self, bm):
+            self.colptr = torch.from_numpy(bm.colptr).cuda()
+            self.rows = torch.from_numpy(bm.rows).cuda()
+
+    with Server(0, budget_bytes=8 << 30, max_active=8) as srv:
+        tickets = [srv.submit_device(Dev(reqs[0])), srv.submit(reqs[2]), srv.submit_device(Dev(reqs[1]))]
+        res = [srv.wait(t) for t in tickets]
+        assert srv.stats()["dual_admitted"] == 2
+    for (low, ess, _), i in zip(res, (0, 2, 1)):
+        np.testing.assert_array_equal(low, want[i][0])
+        np.testing.assert_array_equal(ess, want[i][1])
