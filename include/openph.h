@@ -173,8 +173,11 @@ typedef struct {
 } oph_server_counters;
 
 int oph_server_create(int device, int64_t budget_bytes, int32_t max_active, oph_server **out);
-/* Queue a 0-based CSC matrix (copied); returns a ticket.  OPH_ERR_OOM if it
- * can never fit the arena, OPH_ERR_BAD_INPUT if malformed. */
+/* Queue a 0-based CSC matrix; returns a ticket.  The matrix is copied to
+ * the device (the caller may free its buffers on return) and checked and
+ * graded there, so the submitting thread does no per-entry work.
+ * OPH_ERR_OOM if it can never fit the arena, OPH_ERR_BAD_INPUT if
+ * malformed.  Queued copies live outside the arena until admission. */
 int oph_server_submit(oph_server *srv, int64_t m, const int64_t *colptr, const int32_t *rows, int64_t *ticket);
 /* The same for a 0-based CSC already in device memory on the server's device
  * (d_colptr[m + 1] with d_colptr[0] == 0, d_rows[nnz]): the server copies it

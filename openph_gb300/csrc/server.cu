@@ -97,10 +97,8 @@ struct RangeAlloc {
 
 struct Request {
     int64_t ticket = 0, m = 0, nnz = 0;
-    std::vector<int64_t> colptr;
-    std::vector<int32_t> rows;
-    // a request submitted from device memory: its own copy of the CSC
-    // (colptr then rows, server-owned), read in place at admission
+    // the server's own device copy of the CSC (colptr then rows), made at
+    // submission and read in place at admission
     void *d_buf = nullptr;
     std::vector<int32_t> low, ess;
     double t_submit = 0, t_admit = 0, t_done = 0;
@@ -326,13 +324,9 @@ struct Server {
     // Admission of one request into slot b; called by the worker only.
     int admit(Request *r, int b) {
         cudaStream_t s = ctx->stream;
-        // a host submission is staged in the pool; a device one was copied
-        // to its own buffer at submission
-        const bool host = r->d_buf == nullptr;
-        // staging: the host CSC, and the anti-transpose's temporaries
-        const int64_t tmp_ints = r->dual ? (int64_t)((dual_tmp_bytes(r->m, r->nnz) + 255) / 4) + 64 : 0;
-        const int64_t csc_ints = host ? 2 * (r->m + 1) + r->nnz + 4 : 0;
-        const int64_t stage_ints = csc_ints + tmp_ints;
+        // the request's CSC is the device copy made at submission; staging
+        // holds the anti-transpose's temporaries
+        const int64_t stage_ints = r->dual ? (int64_t)((dual_tmp_bytes(r->m, r->nnz) + 255) / 4) + 64 : 0;
         const int64_t reg_ints = region_ints(r->m, r->nnz);
         const int64_t c0 = cols.alloc(std::max<int64_t>(r->m, 1), 1);
         if (c0 < 0) return 1;
@@ -345,21 +339,15 @@ struct Server {
             return 1;
         }
         r->c0 = c0; r->reg = reg; r->reg_ints = reg_ints; r->slot = b;
-        int64_t *d_colptr = static_cast<int64_t *>(r->d_buf);
-        int32_t *d_rows = reinterpret_cast<int32_t *>(d_colptr + r->m + 1);
-        if (host) {
-            d_colptr = reinterpret_cast<int64_t *>(a.pool + stg);
-            d_rows = a.pool + stg + 2 * (r->m + 1);
-            cudaMemcpyAsync(d_colptr, r->colptr.data(), sizeof(int64_t) * (r->m + 1), cudaMemcpyHostToDevice, s);
-            if (r->nnz) cudaMemcpyAsync(d_rows, r->rows.data(), sizeof(int32_t) * r->nnz, cudaMemcpyHostToDevice, s);
-        }
+        const int64_t *d_colptr = static_cast<const int64_t *>(r->d_buf);
+        const int32_t *d_rows = reinterpret_cast<const int32_t *>(d_colptr + r->m + 1);
         const int8_t asc = r->dual ? 1 : 0;
         cudaMemcpyAsync(const_cast<int8_t *>(a.iasc) + b, &asc, 1, cudaMemcpyHostToDevice, s);
         if (r->m > 0 && r->dual) {
             // the anti-transpose, straight into the request's columns and
             // region (rows shifted into its column range)
             k_srv_init_cols<<<grid(r->m), 256, 0, s>>>(r->m, c0, b, a);
-            void *tmp = a.pool + stg + ((csc_ints + 63) & ~63ll);
+            void *tmp = a.pool + stg;
             dual_build_store(s, ctx->sm_count, d_colptr, d_rows, r->m, r->nnz, a.pool + reg, reg, (int)c0,
                              a.seg + c0, a.low + c0, const_cast<int8_t *>(a.dim) + c0, a.rec + c0,
                              const_cast<int32_t *>(a.beta) + c0, tmp, nullptr);
@@ -375,15 +363,13 @@ struct Server {
                                          (unsigned long long)(reg + reg_ints));
         if (r->m > 0) launch_phase0(a, c0, c0 + r->m, grid(r->m), s);
         if (stage_ints) {
-            // the staged input and temporaries are read by the kernels above:
-            // their region is released after the sweep's synchronisation
+            // the temporaries are used by the kernels above: their region is
+            // released after the sweep's synchronisation
             staged.emplace_back(stg, stage_ints);
         }
-        if (!host) {
-            // the device copy is freed in stream order after those kernels
-            cudaFreeAsync(r->d_buf, s);
-            r->d_buf = nullptr;
-        }
+        // the device copy is freed in stream order after those kernels
+        cudaFreeAsync(r->d_buf, s);
+        r->d_buf = nullptr;
         r->t_admit = now_ms();
         slots[b] = r;
         admitted++;
@@ -434,8 +420,6 @@ struct Server {
                 pool.release(r->reg, r->reg_ints);
                 slots[r->slot] = nullptr;
                 r->t_done = t;
-                r->colptr.clear(); r->colptr.shrink_to_fit();
-                r->rows.clear(); r->rows.shrink_to_fit();
                 r->done = true;
                 completed++;
             }
@@ -707,59 +691,23 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     return OPH_OK;
 }
 
-__attribute__((visibility("default"))) int oph_server_submit(oph_server *sv, int64_t m, const int64_t *colptr,
-                                                             const int32_t *rows, int64_t *ticket) {
-    if (!sv || m < 0 || !colptr || !ticket || colptr[0] != 0) return OPH_ERR_BAD_INPUT;
-    const int64_t nnz = colptr[m];
-    if (nnz < 0 || (nnz > 0 && !rows)) return OPH_ERR_BAD_INPUT;
-    if (m > sv->mcap || sv->region_ints(m, nnz) + 2 * (m + 1) + nnz > sv->pool_ints) return OPH_ERR_OOM;
-    // the same structural checks as the single-matrix path, on the host
-    for (int64_t j = 0; j < m; j++) {
-        if (colptr[j + 1] < colptr[j]) return OPH_ERR_BAD_INPUT;
-        int prev = -1;
-        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) {
-            if (rows[k] <= prev || rows[k] >= m) return OPH_ERR_BAD_INPUT;
-            prev = rows[k];
-        }
-        if (colptr[j + 1] - colptr[j] > MAXC - 1) return OPH_ERR_BAD_INPUT;
-    }
-    Request *r = new Request();
-    r->m = m;
-    r->nnz = nnz;
-    r->dual = host_prefers_dual(m, colptr, rows);
-    r->colptr.assign(colptr, colptr + m + 1);
-    if (nnz) r->rows.assign(rows, rows + nnz);
-    r->t_submit = now_ms();
-    {
-        std::lock_guard<std::mutex> lk(sv->mu);
-        if (sv->error) {
-            delete r;
-            return sv->error;
-        }
-        r->ticket = sv->next_ticket++;
-        sv->all[r->ticket] = r;
-        sv->pending.push_back(r);
-        *ticket = r->ticket;
-    }
-    sv->cv_work.notify_one();
-    return OPH_OK;
-}
+}  // extern "C"
 
-__attribute__((visibility("default"))) int oph_server_submit_device(oph_server *sv, int64_t m,
-                                                                    const int64_t *d_colptr, const int32_t *d_rows,
-                                                                    int64_t *ticket) {
-    if (!sv || m < 0 || !d_colptr || !ticket) return OPH_ERR_BAD_INPUT;
-    OPH_CUDA_TRY(cudaSetDevice(sv->ctx->device));
+namespace {
+
+// The server's own device copy of a submitted CSC (from host or device
+// memory; the caller may free its buffers on return), its structural checks
+// and its grading on the device (the matrix a single-matrix pms reduction
+// would choose), then the request queued.  The submitting thread does no
+// O(nnz) host work beyond the copy; the work runs on the submission stream,
+// beside the worker's sweeps.
+int submit_copy(oph_server *sv, int64_t m, int64_t nnz, const int64_t *colptr, const int32_t *rows,
+                cudaMemcpyKind kind, int64_t *ticket) {
+    // the request's region and, at admission, its anti-transpose's
+    // temporaries must fit the arena's pool
+    const int64_t tmp_ints = (int64_t)((dual_tmp_bytes(m, nnz) + 255) / 4) + 64;
+    if (m > sv->mcap || sv->region_ints(m, nnz) + tmp_ints > sv->pool_ints) return OPH_ERR_OOM;
     cudaStream_t s = sv->sub_stream;
-    int64_t ends[2] = {0, 0};
-    OPH_CUDA_TRY(cudaMemcpyAsync(&ends[0], d_colptr, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    OPH_CUDA_TRY(cudaMemcpyAsync(&ends[1], d_colptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    OPH_CUDA_TRY(cudaStreamSynchronize(s));
-    const int64_t nnz = ends[1];
-    if (ends[0] != 0 || nnz < 0 || (nnz > 0 && !d_rows)) return OPH_ERR_BAD_INPUT;
-    if (m > sv->mcap || sv->region_ints(m, nnz) + 2 * (m + 1) + nnz > sv->pool_ints) return OPH_ERR_OOM;
-    // the server's own copy (the caller may free its buffers on return), and
-    // the same structural checks as oph_server_submit, on the device
     const size_t bytes = sizeof(int64_t) * (m + 1) + sizeof(int32_t) * nnz + sizeof(int);
     void *buf = nullptr;
     if (cudaMallocAsync(&buf, bytes, s) != cudaSuccess) {
@@ -770,8 +718,8 @@ __attribute__((visibility("default"))) int oph_server_submit_device(oph_server *
     int32_t *rw = reinterpret_cast<int32_t *>(cp + m + 1);
     int *bad = reinterpret_cast<int *>(rw + nnz);
     int h_bad = 0;
-    cudaMemcpyAsync(cp, d_colptr, sizeof(int64_t) * (m + 1), cudaMemcpyDeviceToDevice, s);
-    if (nnz) cudaMemcpyAsync(rw, d_rows, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(cp, colptr, sizeof(int64_t) * (m + 1), kind, s);
+    if (nnz) cudaMemcpyAsync(rw, rows, sizeof(int32_t) * nnz, kind, s);
     cudaMemsetAsync(bad, 0, sizeof(int), s);
     if (m > 0) k_srv_check<<<sv->grid(m), 256, 0, s>>>(cp, rw, m, nnz, bad);
     cudaMemcpyAsync(&h_bad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
@@ -781,7 +729,6 @@ __attribute__((visibility("default"))) int oph_server_submit_device(oph_server *
         cudaStreamSynchronize(s);
         return e != cudaSuccess ? OPH_ERR_CUDA : OPH_ERR_BAD_INPUT;
     }
-    // the matrix plain pms would reduce for this request, graded on the device
     bool use = false, bad_g = false;
     void *gtmp = nullptr;
     if (m > 0 && cudaMallocAsync(&gtmp, dual_grade_tmp_bytes(m), s) == cudaSuccess) {
@@ -811,6 +758,34 @@ __attribute__((visibility("default"))) int oph_server_submit_device(oph_server *
     }
     sv->cv_work.notify_one();
     return OPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+__attribute__((visibility("default"))) int oph_server_submit(oph_server *sv, int64_t m, const int64_t *colptr,
+                                                             const int32_t *rows, int64_t *ticket) {
+    if (!sv || m < 0 || !colptr || !ticket || colptr[0] != 0) return OPH_ERR_BAD_INPUT;
+    const int64_t nnz = colptr[m];
+    if (nnz < 0 || (nnz > 0 && !rows)) return OPH_ERR_BAD_INPUT;
+    OPH_CUDA_TRY(cudaSetDevice(sv->ctx->device));
+    return submit_copy(sv, m, nnz, colptr, rows, cudaMemcpyHostToDevice, ticket);
+}
+
+__attribute__((visibility("default"))) int oph_server_submit_device(oph_server *sv, int64_t m,
+                                                                    const int64_t *d_colptr, const int32_t *d_rows,
+                                                                    int64_t *ticket) {
+    if (!sv || m < 0 || !d_colptr || !ticket) return OPH_ERR_BAD_INPUT;
+    OPH_CUDA_TRY(cudaSetDevice(sv->ctx->device));
+    cudaStream_t s = sv->sub_stream;
+    int64_t ends[2] = {0, 0};
+    OPH_CUDA_TRY(cudaMemcpyAsync(&ends[0], d_colptr, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaMemcpyAsync(&ends[1], d_colptr + m, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    const int64_t nnz = ends[1];
+    if (ends[0] != 0 || nnz < 0 || (nnz > 0 && !d_rows)) return OPH_ERR_BAD_INPUT;
+    return submit_copy(sv, m, nnz, d_colptr, d_rows, cudaMemcpyDeviceToDevice, ticket);
 }
 
 __attribute__((visibility("default"))) int oph_server_wait(oph_server *sv, int64_t ticket, int32_t *low,
