@@ -1667,8 +1667,8 @@ static void launch_track(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, 
     k_track_sum<<<g.m, 256, 0, s>>>(a, t->low_true, t->ess_hat, t->acc + 4 * slot, 1);
 }
 
-void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int parity) {
-    launch_sweep_ev(a, g, s, nullptr, parity);
+void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int parity, cudaEvent_t *ev) {
+    launch_sweep_ev(a, g, s, ev, parity);
 }
 
 // Kernels one sweep launches (launch_sweep_ev): Phase I (six with the

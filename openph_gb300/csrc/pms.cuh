@@ -76,8 +76,10 @@ struct SweepGrids {
 
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g);
 // One sweep (Phase I, Phase II tiers, sweep counter) on `stream`; with a
-// compacted list, `parity` selects which of the two arrays is current.
-void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t stream, int parity = 0);
+// compacted list, `parity` selects which of the two arrays is current; ev
+// (optional, 6 events): before Phase I, after Phase I, after each tier.
+void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t stream, int parity = 0,
+                  cudaEvent_t *ev = nullptr);
 // Phase 0 over columns [c0, c1).
 void launch_phase0(const PmsArgs &a, int64_t c0, int64_t c1, int grid, cudaStream_t stream);
 

@@ -462,8 +462,12 @@ struct Server {
     void run() {
         cudaSetDevice(ctx->device);
         cudaStream_t s = ctx->stream;
-        // OPH_TRACE=1: one line per sweep on stderr (diagnostics only)
-        const bool trace = getenv("OPH_TRACE") != nullptr;
+        // OPH_TRACE=1: one line per sweep on stderr; OPH_TRACE=2 adds the
+        // device time of admission and of each phase (diagnostics only)
+        const int trace = getenv("OPH_TRACE") ? atoi(getenv("OPH_TRACE")) : 0;
+        cudaEvent_t tev[8] = {};
+        if (trace > 1)
+            for (auto &e : tev) cudaEventCreate(&e);
         for (;;) {
             const double t_round = now_ms();
             const int64_t admitted_before = admitted;
@@ -478,6 +482,7 @@ struct Server {
                 for (auto &rc : retired_cols) cols.release(rc.first, rc.second);
                 retired_cols.clear();
             }
+            bool tev_started = false;
             for (;;) {
                 Request *r = nullptr;
                 {
@@ -491,6 +496,10 @@ struct Server {
                 int b = -1;
                 for (int k = 0; k < max_slots; k++)
                     if (!slots[k]) { b = k; break; }
+                if (trace > 1 && !tev_started) {
+                    cudaEventRecord(tev[6], s);
+                    tev_started = true;
+                }
                 if (b < 0 || admit(r, b) != 0) break;  // no room now: retry after the next sweep
                 {
                     std::lock_guard<std::mutex> lk(mu);
@@ -540,8 +549,9 @@ struct Server {
             gg.m = grid(hi);
             gg.t = (int)std::max<int64_t>(1, std::min<int64_t>(sa.ntiles, (int64_t)ctx->sm_count * 8));
             cudaMemsetAsync(a.ireps, 0, sizeof(int) * max_slots, s);
+            if (trace > 1 && !tev_started) cudaEventRecord(tev[6], s);
             k_srv_sweep_reset<<<1, 1, 0, s>>>(a.st);
-            launch_sweep(sa, gg, s, lp);  // compacts list lp into the other one
+            launch_sweep(sa, gg, s, lp, trace > 1 ? tev : nullptr);  // compacts list lp into the other one
             lp ^= 1;
             cudaMemcpyAsync(h_ireps, a.ireps, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
             cudaMemcpyAsync(h_iover, a.iover, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
@@ -578,6 +588,13 @@ struct Server {
                                 "round %.3f ms (sweep+admit %.3f, retire %.3f)\n",
                         (long long)sweeps, (long long)hi, active, (long long)(admitted - admitted_before),
                         done.size(), now_ms() - t_round, t_swept - t_round, now_ms() - t_swept);
+            if (trace > 1) {
+                float t[6] = {0, 0, 0, 0, 0, 0};
+                cudaEventElapsedTime(&t[0], tev[6], tev[0]);
+                for (int q = 0; q < 5; q++) cudaEventElapsedTime(&t[q + 1], tev[q], tev[q + 1]);
+                fprintf(stderr, "  device ms: admit+merge %.3f p1 %.3f narrow %.3f t1 %.3f t2 %.3f t3 %.3f\n", t[0],
+                        t[1], t[2], t[3], t[4], t[5]);
+            }
         }
     }
 };
