@@ -1115,6 +1115,17 @@ __global__ void __launch_bounds__(BLOCK) k_p2_tier1(PmsArgs a, int tier) {
     p2_tier_body<G, CAP, BLOCK, STAGE, LAZY>(a, tier);
 }
 
+// The shared-memory window of tier 3 (per CTA): 200 KB, 1,638,400 rows
+// below a column's low.  A column whose rows all lie in it is reduced there:
+// an addition then costs O(|P|) shared toggles and a shared search for the
+// next low, where the merge path rewrites all of T and the global bitmap
+// pays an L2 round trip for each.
+constexpr int SBM_WORDS = 51200;
+constexpr size_t SBM_BYTES = sizeof(uint32_t) * SBM_WORDS;
+
+// True when column j's rows (first T0, low lj) lie in a shared window.
+__device__ __forceinline__ bool fits_sbm(int T0, int lj) { return (long long)lj - T0 < 32ll * SBM_WORDS - 32; }
+
 // Tiers 2 and 3: the whole CTA on one column.  With cap > 0 the column and
 // the staged pivot live in shared memory (A/B/C of cap ints); with cap == 0
 // they live in pool-allocated buffers that grow as needed.
@@ -1224,7 +1235,7 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
     if (a.st->converged) return;
     extern __shared__ int smem[];
     __shared__ int scratch[2 * (BLOCK / 32)];
-    __shared__ int s_idx;
+    __shared__ int s_idx, s_route;
     int32_t *in_list = tier == 0 ? a.t0_list : (tier & 1) ? a.widelist : a.worklist;
     int32_t *out_list = (tier & 1) ? a.worklist : a.widelist;
     const int count = tier == 0 ? *a.t0_count : a.st->t_count[tier];
@@ -1235,7 +1246,23 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
         const int idx = s_idx;
         __syncthreads();
         if (idx >= count) break;
-        reduce_column_block(a, in_list[idx], smem, smem + CAP, smem + 2 * CAP, CAP, scratch, out_list,
+        const int j = in_list[idx];
+        if (tier == 2) {
+            // a column whose rows fit tier 3's shared window is reduced there:
+            // its additions toggle bits instead of rewriting the column (one
+            // thread decides: clear[j] may change under other chains)
+            if (threadIdx.x == 0) {
+                const int lj = a.low[j];
+                const long long sj = a.seg[j];
+                s_route = lj >= 0 && !a.clear[j] && fits_sbm(a.pool[sj] > 0 ? a.pool[sj + SEG_HDR] : lj, lj);
+                if (s_route) out_list[atomicAdd(&a.st->t_count[3], 1)] = j;
+            }
+            __syncthreads();
+            const bool routed = s_route;
+            __syncthreads();
+            if (routed) continue;
+        }
+        reduce_column_block(a, j, smem, smem + CAP, smem + 2 * CAP, CAP, scratch, out_list,
                             tier < 3 ? &a.st->t_count[tier + 1] : nullptr, adds, slots);
     }
     if (threadIdx.x == 0) tier_stats(a, tier, adds, slots);
@@ -1252,18 +1279,33 @@ __global__ void __launch_bounds__(BLOCK) k_p2_block(PmsArgs a, int tier) {
 // the matrix) sends the column to the merge path instead.
 constexpr int64_t BM_MAX_WORDS = 1 << 18;
 constexpr int BM_BLOCK = 1024;
+// A 16-byte load of bitmap words: through L2 for the global bitmap (other
+// blocks never touch a CTA's scratch, but L1 is not kept coherent with the
+// atomics), plain for the shared one.
+template <bool SM>
+__device__ __forceinline__ uint4 bm_load4(const uint32_t *p) {
+    if (SM) return *reinterpret_cast<const uint4 *>(p);
+    return __ldcg(reinterpret_cast<const uint4 *>(p));
+}
+template <bool SM>
+__device__ __forceinline__ uint32_t bm_load(const uint32_t *p) {
+    if (SM) return *p;
+    return __ldcg(p);
+}
+
 
 // Rows of words [lo, top] in ascending order into dst (when not null), the
 // words zeroed; every set bit lies in that range.  Four words per thread
 // (lo rounded down to a multiple of 4, the per-CTA scratch a multiple of 4
 // words long).  Returns the number of rows.
+template <bool SM>
 __device__ int bitmap_extract(uint32_t *bm, int lo, int top, int w0, int *dst, int *red) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int out = 0;
     for (int base = lo & ~3; base <= top; base += 4 * (int)blockDim.x) {
         const int w = base + 4 * (int)threadIdx.x;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (w <= top) v = __ldcg(reinterpret_cast<const uint4 *>(bm + w));
+        if (w <= top) v = bm_load4<SM>(bm + w);
         const int c = __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
         int incl = c;
         for (int o = 1; o < 32; o <<= 1) {
@@ -1295,7 +1337,9 @@ __device__ int bitmap_extract(uint32_t *bm, int lo, int top, int w0, int *dst, i
 
 // Returns true when the column needs the merge path (its state written back
 // first).
-__device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long long &adds, long long &slots) {
+template <bool SM>
+__device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int64_t bm_words, long long &adds,
+                                     long long &slots) {
     __shared__ int s_red[32];
     __shared__ int s_small[4];
     __shared__ long long s_off;
@@ -1310,7 +1354,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
     int n = a.pool[sj];
     const int capj = a.pool[sj + 1];
     const int *T = a.pool + sj + SEG_HDR;
-    const long long nbits = 32ll * a.bm_words;
+    const long long nbits = 32ll * bm_words;
     // the window's first row: a multiple of 32 with lj - w0 < nbits
     const int w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 31) & ~31ll) : 0;
     if (n > 0 && T[0] < w0) return true;
@@ -1360,13 +1404,13 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
                 for (int c0 = ((lj - w0) >> 5) & ~3; c0 >= 0 && next < 0; c0 -= 128) {
                     const int w = c0 - 4 * lane;
                     uint4 v = make_uint4(0u, 0u, 0u, 0u);
-                    if (w >= 0) v = __ldcg(reinterpret_cast<const uint4 *>(bm + w));
+                    if (w >= 0) v = bm_load4<SM>(bm + w);
                     const int hi = v.w ? w + 3 : v.z ? w + 2 : v.y ? w + 1 : v.x ? w : -1;
                     const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
                     if (nz) {
                         const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
                         const int hw = __shfl_sync(0xffffffffu, hi, src);
-                        next = hw * 32 + 31 - __clz(__ldcg(bm + hw));
+                        next = hw * 32 + 31 - __clz(bm_load<SM>(bm + hw));
                     }
                 }
             }
@@ -1402,7 +1446,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
         dst = s_off;
     }
     const int top = n > 0 ? (lj - w0) >> 5 : -1;
-    bitmap_extract(bm, (lo_row - w0) >> 5, top, w0, stored ? a.pool + dst + SEG_HDR : nullptr, s_red);
+    bitmap_extract<SM>(bm, (lo_row - w0) >> 5, top, w0, stored ? a.pool + dst + SEG_HDR : nullptr, s_red);
     if (!stored) return false;
     if (tid == 0) {
         a.pool[dst] = n;
@@ -1428,11 +1472,16 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, long
 template <int BLOCK>
 __global__ void __launch_bounds__(BLOCK) k_p2_bitmap(PmsArgs a, int tier) {
     if (a.st->converged) return;
-    __shared__ int scratch[2 * (BLOCK / 32)];
-    __shared__ int s_idx;
-    const int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
     const int count = a.st->t_count[tier];
+    if (count == 0) return;
+    extern __shared__ __align__(16) uint32_t sbm[];  // SBM_WORDS, zero between columns
+    __shared__ int scratch[2 * (BLOCK / 32)];
+    __shared__ int s_idx, s_fit;
+    const int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
     uint32_t *bm = a.bm ? a.bm + (size_t)blockIdx.x * a.bm_words : nullptr;
+    for (int q = 4 * threadIdx.x; q < SBM_WORDS; q += 4 * BLOCK)
+        *reinterpret_cast<uint4 *>(sbm + q) = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
     long long adds = 0, slots = 0;
     for (;;) {
         if (threadIdx.x == 0) s_idx = atomicAdd(&a.st->t_cursor[tier], 1);
@@ -1441,8 +1490,19 @@ __global__ void __launch_bounds__(BLOCK) k_p2_bitmap(PmsArgs a, int tier) {
         __syncthreads();
         if (idx >= count) break;
         const int j = in_list[idx];
-        if (!bm || reduce_column_bitmap(a, j, bm, adds, slots))
-            reduce_column_block(a, j, nullptr, nullptr, nullptr, 0, scratch, nullptr, nullptr, adds, slots);
+        // the shared window when the column's rows fit it, else (or when a
+        // pivot reaches below it) the global bitmap, else the merge path
+        if (threadIdx.x == 0) {
+            const int lj = a.low[j];
+            const long long sj = a.seg[j];
+            s_fit = lj >= 0 && fits_sbm(a.pool[sj] > 0 ? a.pool[sj + SEG_HDR] : lj, lj);
+        }
+        __syncthreads();
+        const bool fit = s_fit;
+        bool fell = true;
+        if (fit) fell = reduce_column_bitmap<true>(a, j, sbm, SBM_WORDS, adds, slots);
+        if (fell && bm) fell = reduce_column_bitmap<false>(a, j, bm, a.bm_words, adds, slots);
+        if (fell) reduce_column_block(a, j, nullptr, nullptr, nullptr, 0, scratch, nullptr, nullptr, adds, slots);
     }
     if (threadIdx.x == 0) tier_stats(a, tier, adds, slots);
 }
@@ -1547,9 +1607,17 @@ int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     g->g1 = fill_grid(ctx, k_p2_tier1<T1_G, T1_CAP, T1_BLOCK, T1_STAGE, T1_LAZY>, T1_BLOCK, g->s1, done1);
     g->g2 = fill_grid(ctx, k_p2_block<T2_CAP, T2_BLOCK>, T2_BLOCK, g->s2, done2);
     g->g3 = ctx->sm_count;  // tier 3: one 1024-thread CTA per SM
+    static int done3[64];
+    if (!done3[ctx->device & 63]) {
+        if (cudaFuncSetAttribute(k_p2_bitmap<BM_BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)SBM_BYTES) != cudaSuccess)
+            g->g3 = -1;
+        else
+            done3[ctx->device & 63] = 1;
+    }
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
     g->t = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 8));
-    if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0 || g->gs < 0) {
+    if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0 || g->gs < 0 || g->g3 < 0) {
         fprintf(stderr, "openph_gb300: Phase II kernel set-up failed: %s\n", cudaGetErrorString(cudaGetLastError()));
         return OPH_ERR_CUDA;
     }
@@ -1655,7 +1723,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
     if (ev) cudaEventRecord(ev[3], s);
     k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
     if (ev) cudaEventRecord(ev[4], s);
-    k_p2_bitmap<BM_BLOCK><<<g.g3, BM_BLOCK, 0, s>>>(a, 3);
+    k_p2_bitmap<BM_BLOCK><<<g.g3, BM_BLOCK, SBM_BYTES, s>>>(a, 3);
     k_count_sweep<<<1, 1, 0, s>>>(a.st);
     if (ev) cudaEventRecord(ev[5], s);
 }
