@@ -1115,12 +1115,17 @@ __global__ void __launch_bounds__(BLOCK) k_p2_tier1(PmsArgs a, int tier) {
     p2_tier_body<G, CAP, BLOCK, STAGE, LAZY>(a, tier);
 }
 
-// The shared-memory window of tier 3 (per CTA): 200 KB, 1,638,400 rows
-// below a column's low.  A column whose rows all lie in it is reduced there:
+// The shared-memory window of tier 3 (per CTA): 96 KB, 786,432 rows below a
+// column's low (a larger window left too little L1 for the pivots' rows: the
+// 5M-column torus lost 6%, and the lower-star image and the batch gained
+// nothing).  A column whose rows all lie in it is reduced there:
 // an addition then costs O(|P|) shared toggles and a shared search for the
 // next low, where the merge path rewrites all of T and the global bitmap
 // pays an L2 round trip for each.
-constexpr int SBM_WORDS = 51200;
+#ifndef OPH_SBM_WORDS
+#define OPH_SBM_WORDS 24576
+#endif
+constexpr int SBM_WORDS = OPH_SBM_WORDS;
 constexpr size_t SBM_BYTES = sizeof(uint32_t) * SBM_WORDS;
 
 // True when column j's rows (first T0, low lj) lie in a shared window.
