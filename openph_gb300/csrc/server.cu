@@ -106,6 +106,7 @@ struct Request {
     bool done = false;
     bool dual = false;  // reduced through its anti-transpose
     int64_t c0 = -1, reg = -1, reg_ints = 0;
+    int64_t ring_off = -1;  // low then ess in the pinned result ring (ints), or -1
 };
 
 // ------------------------------------------------------------------ kernels
@@ -298,6 +299,12 @@ struct Server {
     std::vector<std::pair<int64_t, int64_t>> admitted_rng;
     int64_t *d_rng = nullptr, *h_rng = nullptr;
     std::vector<std::pair<int64_t, int64_t>> retired_cols;
+    // results of retired requests wait for their caller in a pinned ring (a
+    // real asynchronous copy: the worker never blocks on a large result);
+    // oph_server_wait copies them out and frees their space.  A result that
+    // does not fit goes to the request's own host arrays.
+    int32_t *h_ring = nullptr;
+    RangeAlloc ring;
     RangeAlloc cols, pool;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -386,8 +393,6 @@ struct Server {
         for (size_t k = 0; k < done.size(); k++) {
             Request *r = done[k];
             const int64_t m = r->m;
-            r->low.resize(m);
-            r->ess.resize(m);
             if (m == 0) continue;
             int64_t out = pool.alloc(2 * m + 4, 64);
             if (out >= 0) outs.emplace_back(out, 2 * m + 4);
@@ -404,8 +409,18 @@ struct Server {
         for (size_t k = 0; k < done.size(); k++) {
             Request *r = done[k];
             if (r->m == 0) continue;
-            cudaMemcpyAsync(r->low.data(), dptr[k], sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
-            cudaMemcpyAsync(r->ess.data(), dptr[k] + r->m, sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
+            if (h_ring) {
+                std::lock_guard<std::mutex> lk(mu);
+                r->ring_off = ring.alloc(2 * r->m, 16);
+            }
+            if (r->ring_off >= 0) {
+                cudaMemcpyAsync(h_ring + r->ring_off, dptr[k], sizeof(int32_t) * 2 * r->m, cudaMemcpyDeviceToHost, s);
+            } else {
+                r->low.resize(r->m);
+                r->ess.resize(r->m);
+                cudaMemcpyAsync(r->low.data(), dptr[k], sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
+                cudaMemcpyAsync(r->ess.data(), dptr[k] + r->m, sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
+            }
             k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
         }
         cudaStreamSynchronize(s);
@@ -668,12 +683,22 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     if (ok) ok = cudaMallocHost((void **)&sv->h_ireps, 4 * (size_t)max_active) == cudaSuccess &&
                  cudaMallocHost((void **)&sv->h_iover, 4 * (size_t)max_active) == cudaSuccess &&
                  cudaMallocHost((void **)&sv->h_rng, sizeof(int64_t) * (2 * (size_t)max_active + 1)) == cudaSuccess;
+    // the result ring: 1/256 of the budget, 32 MB .. 512 MB (without it,
+    // results are copied to pageable host arrays)
+    const int64_t ring_ints = std::min<int64_t>(std::max<int64_t>(budget_bytes / 256, 32ll << 20), 512ll << 20) / 4;
+    if (ok && cudaMallocHost((void **)&sv->h_ring, sizeof(int32_t) * ring_ints) == cudaSuccess) {
+        sv->ring.init(ring_ints);
+    } else {
+        sv->h_ring = nullptr;
+        cudaGetLastError();
+    }
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->sub_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
         if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
         if (sv->h_iover) cudaFreeHost(sv->h_iover);
         if (sv->h_rng) cudaFreeHost(sv->h_rng);
+        if (sv->h_ring) cudaFreeHost(sv->h_ring);
         if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
         oph_context_destroy(raw);
         delete sv;
@@ -819,8 +844,13 @@ __attribute__((visibility("default"))) int oph_server_wait(oph_server *sv, int64
     lk.unlock();
     const int rc = r->status;
     if (rc == OPH_OK && r->m > 0) {
-        if (low) memcpy(low, r->low.data(), sizeof(int32_t) * r->m);
-        if (ess) memcpy(ess, r->ess.data(), sizeof(int32_t) * r->m);
+        const int32_t *src = r->ring_off >= 0 ? sv->h_ring + r->ring_off : nullptr;
+        if (low) memcpy(low, src ? src : r->low.data(), sizeof(int32_t) * r->m);
+        if (ess) memcpy(ess, src ? src + r->m : r->ess.data(), sizeof(int32_t) * r->m);
+    }
+    if (r->ring_off >= 0) {
+        std::lock_guard<std::mutex> lk2(sv->mu);
+        sv->ring.release(r->ring_off, 2 * r->m);
     }
     if (info) {
         info->latency_ms = r->t_done - r->t_submit;
@@ -869,6 +899,7 @@ __attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
     if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
     if (sv->h_iover) cudaFreeHost(sv->h_iover);
     if (sv->h_rng) cudaFreeHost(sv->h_rng);
+    if (sv->h_ring) cudaFreeHost(sv->h_ring);
     oph_context_destroy(reinterpret_cast<oph_context *>(sv->ctx));
     delete sv;
     return OPH_OK;
