@@ -107,6 +107,7 @@ struct Request {
     bool dual = false;  // reduced through its anti-transpose
     int64_t c0 = -1, reg = -1, reg_ints = 0;
     int64_t ring_off = -1;  // low then ess in the pinned result ring (ints), or -1
+    bool listed = false;    // in the Phase I list: its sweeps have begun
 };
 
 // ------------------------------------------------------------------ kernels
@@ -286,7 +287,9 @@ __global__ void k_srv_sweep_reset(DevStatus *st) {
 // ------------------------------------------------------------------ server
 struct Server {
     Context *ctx = nullptr;  // owns the stream and the device buffers
-    cudaStream_t sub_stream = nullptr;  // device submissions: copy and check
+    cudaStream_t sub_stream = nullptr;  // submissions: copy, check, grade
+    cudaStream_t adm_stream = nullptr;  // admissions overlapping a sweep
+    cudaEvent_t adm_done = nullptr;     //   and their completion
     int64_t budget = 0, mcap = 0, pool_ints = 0;
     int max_slots = 0;
     PmsArgs a{};
@@ -329,8 +332,7 @@ struct Server {
     }
 
     // Admission of one request into slot b; called by the worker only.
-    int admit(Request *r, int b) {
-        cudaStream_t s = ctx->stream;
+    int admit(Request *r, int b, cudaStream_t s) {
         // the request's CSC is the device copy made at submission; staging
         // holds the anti-transpose's temporaries
         const int64_t stage_ints = r->dual ? (int64_t)((dual_tmp_bytes(r->m, r->nnz) + 255) / 4) + 64 : 0;
@@ -474,11 +476,37 @@ struct Server {
         cv_done.notify_all();
     }
 
+    // Admits queued requests, first come first served, on `s` while they
+    // fit (slots, columns, pool); returns how many.
+    int admit_pending(cudaStream_t s, int &active, bool wait_for_work) {
+        int n = 0;
+        for (;;) {
+            Request *r = nullptr;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                if (wait_for_work && active == 0) cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+                if (pending.empty()) break;
+                r = pending.front();
+            }
+            int b = -1;
+            for (int k = 0; k < max_slots; k++)
+                if (!slots[k]) { b = k; break; }
+            if (b < 0 || admit(r, b, s) != 0) break;  // no room now: retry after the next sweep
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                pending.pop_front();
+            }
+            active++;
+            n++;
+        }
+        return n;
+    }
+
     void run() {
         cudaSetDevice(ctx->device);
         cudaStream_t s = ctx->stream;
         // OPH_TRACE=1: one line per sweep on stderr; OPH_TRACE=2 adds the
-        // device time of admission and of each phase (diagnostics only)
+        // device time of the merge and of each phase (diagnostics only)
         const int trace = getenv("OPH_TRACE") ? atoi(getenv("OPH_TRACE")) : 0;
         cudaEvent_t tev[8] = {};
         if (trace > 1)
@@ -486,56 +514,42 @@ struct Server {
         for (;;) {
             const double t_round = now_ms();
             const int64_t admitted_before = admitted;
-            // admission, first come first served
             int active = 0;
             for (auto *r : slots) active += r != nullptr;
             if (active == 0) {
                 // nothing on the device: the list starts empty (retired
-                // columns left in it go too), and every range is free
+                // columns left in it go too), every range is free, and the
+                // first requests are admitted here, before the sweep
                 cudaMemsetAsync(&a.st->ucount[lp], 0, sizeof(int), s);
-                std::lock_guard<std::mutex> lk(mu);
-                for (auto &rc : retired_cols) cols.release(rc.first, rc.second);
-                retired_cols.clear();
-            }
-            bool tev_started = false;
-            for (;;) {
-                Request *r = nullptr;
                 {
-                    std::unique_lock<std::mutex> lk(mu);
-                    if (active == 0)
-                        cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+                    std::lock_guard<std::mutex> lk(mu);
+                    for (auto &rc : retired_cols) cols.release(rc.first, rc.second);
+                    retired_cols.clear();
+                    if (stop && pending.empty()) return;
+                }
+                admit_pending(s, active, true);
+                {
+                    std::lock_guard<std::mutex> lk(mu);
                     if (stop && pending.empty() && active == 0) return;
-                    if (pending.empty()) break;
-                    r = pending.front();
                 }
-                int b = -1;
-                for (int k = 0; k < max_slots; k++)
-                    if (!slots[k]) { b = k; break; }
-                if (trace > 1 && !tev_started) {
-                    cudaEventRecord(tev[6], s);
-                    tev_started = true;
+                if (active == 0) {
+                    if (!pending.empty()) {
+                        // the head request cannot fit even in an empty arena
+                        std::lock_guard<std::mutex> lk(mu);
+                        Request *r = pending.front();
+                        pending.pop_front();
+                        r->status = OPH_ERR_OOM;
+                        r->done = true;
+                        cv_done.notify_all();
+                    }
+                    continue;
                 }
-                if (b < 0 || admit(r, b) != 0) break;  // no room now: retry after the next sweep
-                {
-                    std::lock_guard<std::mutex> lk(mu);
-                    pending.pop_front();
-                }
-                active++;
             }
-            if (active == 0) {
-                if (!pending.empty()) {
-                    // the head request cannot fit even in an empty arena
-                    std::lock_guard<std::mutex> lk(mu);
-                    Request *r = pending.front();
-                    pending.pop_front();
-                    r->status = OPH_ERR_OOM;
-                    r->done = true;
-                    cv_done.notify_all();
-                }
-                continue;
-            }
-            // the admitted ranges into the Phase I list (column order)
+            if (trace > 1) cudaEventRecord(tev[6], s);
+            // the ranges admitted since the last sweep into the Phase I list
+            // (column order), after their set-up on the admission stream
             if (!admitted_rng.empty()) {
+                cudaStreamWaitEvent(s, adm_done, 0);
                 std::sort(admitted_rng.begin(), admitted_rng.end());
                 const int K = (int)admitted_rng.size();
                 int64_t acc = 0;
@@ -552,8 +566,10 @@ struct Server {
                 lp ^= 1;
                 admitted_rng.clear();
             }
+            for (auto *r : slots)
+                if (r) r->listed = true;
             const size_t retired_before = retired_cols.size();
-            // one sweep over every active request
+            // one sweep over every listed request
             int64_t hi = 0;
             for (auto *r : slots)
                 if (r) hi = std::max(hi, r->c0 + std::max<int64_t>(r->m, 1));
@@ -564,13 +580,18 @@ struct Server {
             gg.m = grid(hi);
             gg.t = (int)std::max<int64_t>(1, std::min<int64_t>(sa.ntiles, (int64_t)ctx->sm_count * 8));
             cudaMemsetAsync(a.ireps, 0, sizeof(int) * max_slots, s);
-            if (trace > 1 && !tev_started) cudaEventRecord(tev[6], s);
             k_srv_sweep_reset<<<1, 1, 0, s>>>(a.st);
             launch_sweep(sa, gg, s, lp, trace > 1 ? tev : nullptr);  // compacts list lp into the other one
             lp ^= 1;
             cudaMemcpyAsync(h_ireps, a.ireps, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
             cudaMemcpyAsync(h_iover, a.iover, sizeof(int) * max_slots, cudaMemcpyDeviceToHost, s);
-            if (cudaStreamSynchronize(s) != cudaSuccess) {
+            // while the sweep runs: the requests that arrived meanwhile are set
+            // up on the admission stream (their columns, records and pool
+            // regions are disjoint from every listed request's); they join
+            // the list before the next sweep
+            admit_pending(adm_stream, active, false);
+            cudaEventRecord(adm_done, adm_stream);
+            if (cudaStreamSynchronize(s) != cudaSuccess || cudaStreamSynchronize(adm_stream) != cudaSuccess) {
                 fail_all(OPH_ERR_CUDA);
                 return;
             }
@@ -584,10 +605,10 @@ struct Server {
             }
             sweeps++;
             for (auto *r : slots)
-                if (r) r->sweeps++;
+                if (r && r->listed) r->sweeps++;
             // regrow first: an overflowed request is not converged
             for (int b = 0; b < max_slots; b++)
-                if (slots[b] && h_iover[b]) {
+                if (slots[b] && slots[b]->listed && h_iover[b]) {
                     if (regrow(slots[b]) != OPH_OK) {
                         fail_all(OPH_ERR_OOM);
                         return;
@@ -595,7 +616,7 @@ struct Server {
                 }
             std::vector<Request *> done;
             for (int b = 0; b < max_slots; b++)
-                if (slots[b] && h_ireps[b] == 0 && !h_iover[b]) done.push_back(slots[b]);
+                if (slots[b] && slots[b]->listed && h_ireps[b] == 0 && !h_iover[b]) done.push_back(slots[b]);
             const double t_swept = now_ms();
             retire_all(done);
             if (trace)
@@ -694,12 +715,16 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     }
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->sub_stream, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) ok = cudaStreamCreateWithFlags(&sv->adm_stream, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) ok = cudaEventCreateWithFlags(&sv->adm_done, cudaEventDisableTiming) == cudaSuccess;
     if (!ok) {
         if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
         if (sv->h_iover) cudaFreeHost(sv->h_iover);
         if (sv->h_rng) cudaFreeHost(sv->h_rng);
         if (sv->h_ring) cudaFreeHost(sv->h_ring);
         if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
+        if (sv->adm_stream) cudaStreamDestroy(sv->adm_stream);
+        if (sv->adm_done) cudaEventDestroy(sv->adm_done);
         oph_context_destroy(raw);
         delete sv;
         return OPH_ERR_OOM;
@@ -773,7 +798,7 @@ int submit_copy(oph_server *sv, int64_t m, int64_t nnz, const int64_t *colptr, c
     }
     bool use = false, bad_g = false;
     void *gtmp = nullptr;
-    if (m > 0 && cudaMallocAsync(&gtmp, dual_grade_tmp_bytes(m), s) == cudaSuccess) {
+    if (m >= DUAL_MIN_M && cudaMallocAsync(&gtmp, dual_grade_tmp_bytes(m), s) == cudaSuccess) {
         if (dual_grade(s, sv->ctx->sm_count, cp, rw, m, nnz, OPH_DUAL_AUTO, gtmp, &use, &bad_g, nullptr) != OPH_OK)
             use = false;
         cudaFreeAsync(gtmp, s);
@@ -896,6 +921,8 @@ __attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
         delete kv.second;
     }
     if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);
+    if (sv->adm_stream) cudaStreamDestroy(sv->adm_stream);
+    if (sv->adm_done) cudaEventDestroy(sv->adm_done);
     if (sv->h_ireps) cudaFreeHost(sv->h_ireps);
     if (sv->h_iover) cudaFreeHost(sv->h_iover);
     if (sv->h_rng) cudaFreeHost(sv->h_rng);
