@@ -1423,21 +1423,18 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
     // and the set bit below it.  The next low is most often known before the
     // toggles: with t1 the highest set bit below the low and p2 the pivot's
     // second row, it is max(t1, p2) unless the two are equal (and cancel).
-    // Then the last warp, which does no toggling, fetches that row's pivot
-    // record while the others toggle (its fields and an acquire of its
-    // column in flight together), taking the record's round trips off the
-    // chain.
+    // Then thread 0 fetches that row's pivot record (an acquire of its
+    // column, then its fields) while the CTA toggles, taking the record's
+    // round trip off the chain.
     const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    const int ntog = 32 * (nw - 1);  // the toggling threads (the last warp fetches)
     int t1 = n >= 2 ? T[n - 2] - w0 : -1;
-    bool acquired = false;  // h / e came from the fetch: final, and acquired
     for (int par = 0;; par ^= 1) {
         int np;
         const int *P = nullptr;
         if (rec_complete(h, e)) {
             np = h.y;  // rows in the record, which every thread holds
         } else {
-            const int4 h2 = acquired ? h : rec_header(&a.rec[lj], h);
+            const int4 h2 = rec_header(&a.rec[lj], h);
             np = h2.y;
             P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
         }
@@ -1447,7 +1444,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             break;
         }
         lo_row = min(lo_row, p0);
-        if (tid == ntog) {
+        if (tid == 0) {
             const int p2 = np >= 2 ? (P ? P[np - 2] : rec_entry(e, np - 2)) - w0 : -1;
             const int known = t1 != p2 || t1 < 0;
             const int cand = t1 != p2 ? max(t1, p2) : -1;
@@ -1455,21 +1452,16 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             s_pred[par][1] = cand;
             if (known && cand >= 0) {
                 const PivRec *r = a.rec + w0 + cand;
-                int4 hh = __ldcg(reinterpret_cast<const int4 *>(r));
-                int4 ee = __ldcg(reinterpret_cast<const int4 *>(r) + 1);
                 const int col = ld_acquire_i32(&r->col);
-                if (col >= 0 && !(hh.y > 0 && (unsigned)hh.w != SEG4_NONE && (hh.y > 4 || rec_complete(hh, ee)))) {
-                    // a field read before the acquire still held its marker
-                    hh = __ldcg(reinterpret_cast<const int4 *>(r));
-                    ee = __ldcg(reinterpret_cast<const int4 *>(r) + 1);
-                }
-                hh.x = col;
+                int4 hh = __ldcg(reinterpret_cast<const int4 *>(r));
+                const int4 ee = __ldcg(reinterpret_cast<const int4 *>(r) + 1);
+                hh.x = col;  // the fields read after the acquire are final when col is set
                 *reinterpret_cast<int4 *>(s_rec[par]) = hh;
                 *reinterpret_cast<int4 *>(s_rec[par] + 4) = ee;
             }
         }
         int d = 0;
-        for (int k = tid; k < np && tid < ntog; k += ntog) {
+        for (int k = tid; k < np; k += blockDim.x) {
             const int r = (P ? P[k] : rec_entry(e, k & 3)) - w0;
             const uint32_t bit = 1u << (r & 31);
             d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
@@ -1511,8 +1503,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             break;
         }
         lj = w0 + next;
-        acquired = s_pred[par][0] && s_pred[par][1] == next;
-        if (acquired) {
+        if (s_pred[par][0] && s_pred[par][1] == next) {
             h = *reinterpret_cast<const int4 *>(s_rec[par]);
             e = *reinterpret_cast<const int4 *>(s_rec[par] + 4);
         } else {
