@@ -1342,60 +1342,12 @@ __device__ int bitmap_extract(uint32_t *bm, int lo, int top, int w0, int *dst, i
 
 // Returns true when the column needs the merge path (its state written back
 // first).
-// The two highest set bits of the bitmap below bit `pos` (pos < 32 x its
-// words), -1 where there are fewer; called by a whole warp: 16-byte loads,
-// 128 words a step from the top.
-template <bool SM>
-__device__ __forceinline__ int2 bm_top2_below(const uint32_t *bm, int pos) {
-    const int lane = threadIdx.x & 31;
-    const int wl = pos >> 5;
-    const uint32_t ml = (1u << (pos & 31)) - 1u;
-    int first = -1, second = -1;
-    for (int c0 = wl & ~3; c0 >= 0 && second < 0; c0 -= 128) {
-        const int w = c0 - 4 * lane;
-        uint32_t q[4] = {0u, 0u, 0u, 0u};
-        if (w >= 0) {
-            const uint4 v = bm_load4<SM>(bm + w);
-            q[0] = v.x;
-            q[1] = v.y;
-            q[2] = v.z;
-            q[3] = v.w;
-        }
-        int t1 = -1, t2 = -1;  // this lane's two highest bits
-#pragma unroll
-        for (int k = 3; k >= 0; k--) {
-            uint32_t x = w + k > wl ? 0u : w + k == wl ? q[k] & ml : q[k];
-            for (int rep = 0; rep < 2 && x && t2 < 0; rep++) {
-                const int hb = 31 - __clz(x);
-                if (t1 < 0) t1 = (w + k) * 32 + hb;
-                else t2 = (w + k) * 32 + hb;
-                x &= ~(1u << hb);
-            }
-        }
-        unsigned nz = __ballot_sync(0xffffffffu, t1 >= 0);
-        while (nz && second < 0) {
-            const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
-            const int a1 = __shfl_sync(0xffffffffu, t1, src), a2 = __shfl_sync(0xffffffffu, t2, src);
-            if (first < 0) {
-                first = a1;
-                second = a2;
-            } else {
-                second = a1;
-            }
-            nz &= nz - 1;
-        }
-    }
-    return make_int2(first, second);
-}
-
 template <bool SM>
 __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int64_t bm_words, long long &adds,
                                      long long &slots) {
     __shared__ int s_red[32];
     __shared__ int s_small[4];
     __shared__ long long s_off;
-    __shared__ int s_pred[2][2];            // per parity of the addition: known, next low
-    __shared__ __align__(16) int s_rec[2][8];  //   and its pivot record, fetched ahead
     const int tid = threadIdx.x;
     if (a.clear[j]) return false;
     int lj = a.low[j];
@@ -1420,15 +1372,9 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
     bool made_pivot = false, fell_back = false;
     // Two CTA barriers per addition: the whole CTA toggles the pivot's bits
     // and leaves per-warp counts; warp 0 totals them and finds the next low
-    // and the set bit below it.  The next low is most often known before the
-    // toggles: with t1 the highest set bit below the low and p2 the pivot's
-    // second row, it is max(t1, p2) unless the two are equal (and cancel).
-    // Then thread 0 fetches that row's pivot record (an acquire of its
-    // column, then its fields) while the CTA toggles, taking the record's
-    // round trip off the chain.
+    // (128 words a step, 16-byte loads) for everyone.
     const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    int t1 = n >= 2 ? T[n - 2] - w0 : -1;
-    for (int par = 0;; par ^= 1) {
+    for (;;) {
         int np;
         const int *P = nullptr;
         if (rec_complete(h, e)) {
@@ -1444,22 +1390,6 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             break;
         }
         lo_row = min(lo_row, p0);
-        if (tid == 0) {
-            const int p2 = np >= 2 ? (P ? P[np - 2] : rec_entry(e, np - 2)) - w0 : -1;
-            const int known = t1 != p2 || t1 < 0;
-            const int cand = t1 != p2 ? max(t1, p2) : -1;
-            s_pred[par][0] = known;
-            s_pred[par][1] = cand;
-            if (known && cand >= 0) {
-                const PivRec *r = a.rec + w0 + cand;
-                const int col = ld_acquire_i32(&r->col);
-                int4 hh = __ldcg(reinterpret_cast<const int4 *>(r));
-                const int4 ee = __ldcg(reinterpret_cast<const int4 *>(r) + 1);
-                hh.x = col;  // the fields read after the acquire are final when col is set
-                *reinterpret_cast<int4 *>(s_rec[par]) = hh;
-                *reinterpret_cast<int4 *>(s_rec[par] + 4) = ee;
-            }
-        }
         int d = 0;
         for (int k = tid; k < np; k += blockDim.x) {
             const int r = (P ? P[k] : rec_entry(e, k & 3)) - w0;
@@ -1473,27 +1403,29 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             int t = lane < nw ? s_red[lane] : 0;
             for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
             const int nn = n + t;
-            int next = -1, below = -1;
+            int next = -1;
             if (nn > 0) {
-                if (s_pred[par][0] && s_pred[par][1] >= 0) {
-                    next = s_pred[par][1];
-                    below = bm_top2_below<SM>(bm, next).x;
-                } else {
-                    // lj's bit went with the pivot's top: the next low lies below it
-                    const int2 t2 = bm_top2_below<SM>(bm, lj - w0);
-                    next = t2.x;
-                    below = t2.y;
+                // lj's bit went with the pivot's top: the next low lies below it
+                for (int c0 = ((lj - w0) >> 5) & ~3; c0 >= 0 && next < 0; c0 -= 128) {
+                    const int w = c0 - 4 * lane;
+                    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                    if (w >= 0) v = bm_load4<SM>(bm + w);
+                    const int hi = v.w ? w + 3 : v.z ? w + 2 : v.y ? w + 1 : v.x ? w : -1;
+                    const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
+                    if (nz) {
+                        const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
+                        const int hw = __shfl_sync(0xffffffffu, hi, src);
+                        next = hw * 32 + 31 - __clz(bm_load<SM>(bm + hw));
+                    }
                 }
             }
             if (lane == 0) {
                 s_small[0] = nn;
-                s_small[1] = next;   // -1: zero column (or, never, no bit left)
-                s_small[2] = below;  // the set bit below it
+                s_small[1] = next;  // -1: zero column (or, never, no bit left)
             }
         }
         __syncthreads();
         const int nn = s_small[0], next = s_small[1];
-        t1 = s_small[2];
         slots += n + np + nn;
         adds++;
         n = nn;
@@ -1503,12 +1435,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             break;
         }
         lj = w0 + next;
-        if (s_pred[par][0] && s_pred[par][1] == next) {
-            h = *reinterpret_cast<const int4 *>(s_rec[par]);
-            e = *reinterpret_cast<const int4 *>(s_rec[par] + 4);
-        } else {
-            rec_load(&a.rec[lj], h, e);
-        }
+        rec_load(&a.rec[lj], h, e);
         mark_clear<false>(a, lj, tid == 0);
         if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
         if (h.x < 0 || h.x >= j) break;
