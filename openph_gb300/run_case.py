@@ -1,6 +1,6 @@
 """Reduce one generated workload a few times on the GPU (for profiler runs).
 
-    python -m openph_gb300.run_case [--workload rips_torus|lower_star|rips_cube|batch]
+    python -m openph_gb300.run_case [--workload rips_torus|lower_star|rips_cube|batch|rips_device|lower_star_device]
                                     [--target-m M] [--algo pms] [--steps K]
                                     [--tier0 LANES,CAP] [--profile] [--dual MODE]
 
@@ -17,6 +17,8 @@ import numpy as np
 
 def make(workload: str, target_m: int, seed: int):
     from . import complexes as cx
+    if workload in ("rips_device", "lower_star_device"):
+        return None  # built on the GPU in main()
     if workload == "rips_torus":
         return cx.rips_torus(400, target_m, seed=seed)
     if workload == "lower_star":
@@ -38,7 +40,9 @@ def _prof(ctx, args) -> dict:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="rips_torus", help="rips_torus, lower_star, rips_cube or batch")
+    ap.add_argument("--workload", default="rips_torus",
+                    help="rips_torus, lower_star, rips_cube, batch, or rips_device / lower_star_device (built on "
+                         "the GPU first)")
     ap.add_argument("--target-m", type=int, default=1_000_000)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--algo", default="pms")
@@ -58,6 +62,28 @@ def main():
         ctx.set_tier0(*map(int, args.tier0.split(",")))
     ctx.set_profile(args.profile)
     ctx.set_dual(args.dual)
+    if args.workload in ("rips_device", "lower_star_device"):
+        # the complex built on the GPU (the generator kernels), then reduced
+        from . import complexes as cx
+        out = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            if args.workload == "rips_device":
+                pts = cx.points_torus(400, seed=args.seed)
+                thr = cx.rips_threshold(pts, args.target_m)
+                dm = cx.rips_device(torch.from_numpy(pts).to(dev), thr, ctx=ctx, device=dev)
+            else:
+                side = int(round((args.target_m / 6) ** 0.5))
+                img = cx.image_smoothed(side, side, seed=args.seed)
+                dm = cx.lower_star_device(torch.from_numpy(img).to(dev), ctx=ctx, device=dev)
+            m = int(dm.colptr.shape[0]) - 1
+            d_low = torch.empty(max(m, 1), dtype=torch.int32, device=dev)
+            out.append(ctx.reduce_device(m, dm.colptr.data_ptr(), dm.rows.data_ptr(), d_low.data_ptr(), None, None,
+                                         args.algo))
+        print(json.dumps({"workload": args.workload, "m": m, "device_ms": [o["device_ms"] for o in out],
+                          "sweeps": out[-1]["sweeps"], "dual": out[-1]["dual"]}))
+        ctx.close()
+        return
     if args.workload == "batch":
         # --target-m is the number of complexes; one segmented pass each step
         col_off, colptr, rows = (torch.from_numpy(x).to(dev) for x in bm[:3])
