@@ -15,17 +15,22 @@
 //   col   the column whose final low is row i (the reference's arglow[i],
 //         src/cuda/algorithms/pms/pms_functions.cu:87-112), -1 = none yet
 //   np    that column's length, seg4 its segment / 4
-//   e[4]  its first four rows
+//   e[4]  its four highest rows, ascending (all its rows, then markers,
+//         when it has at most four)
 //   left  the first input column holding row i (beta.cu:2-15)
 // so one 32-byte read per column addition yields the beta check, the pivot
 // test and, for a pivot of at most four entries (most pivots are apparent
 // pairs of three), the pivot's rows too: one dependent round trip per
-// addition instead of three.  Every field changes at most once per
+// addition instead of three.  For a wider pivot the highest rows tell a
+// reader the next low of the sum before it has read the pivot's segment
+// (the larger of the column's and the pivot's second rows, when they
+// differ).  Every field changes at most once per
 // reduction, from a marker (col -1, np 0, seg4 SEG4_NONE, e -1) to its final
 // value; the publisher writes col last behind a fence.  A reader that sees
 // col set but needs the segment takes an acquire load of col (ordering its
 // reads of the segment) and re-reads np / seg4 only if its first read still
-// showed a marker (rec_header).
+// showed a marker (rec_header), or reads the header with acquire in the
+// first place (rec_load_acq: one round trip).
 #pragma once
 #include <cooperative_groups.h>
 #include <cstdint>
@@ -55,8 +60,8 @@ struct DevStatus {
     int wl_count;                  // Phase II worklist size (tier 0 input)
     int s_cursor;                  // scalar tier: work-queue cursor
     int s_out;                     //   and the columns it hands to tier 0
-    int t_count[4];                // Phase II tier queues: columns queued per tier
-    int t_cursor[4];               //   and the work-queue cursor of each tier
+    int t_count[5];                // Phase II tier queues: columns queued per tier (tier 4: the
+    int t_cursor[5];               //   cluster tier) and the work-queue cursor of each tier
     int reps;                      // repeated lows seen by the last Phase I
     int resume_dim;                // sequential walkers: where to resume after a regrow
     long long resume_pos;          //   (column or row index; -1 = finished)
@@ -102,6 +107,22 @@ __device__ __forceinline__ int ld_acquire_i32(const int *p) {
     asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ int4 ld_acquire_v4(const int4 *p) {
+    int4 v;
+    asm volatile("ld.acquire.gpu.global.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ int4 ld_relaxed_v4(const int4 *p) {
+    int4 v;
+    asm volatile("ld.relaxed.gpu.global.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_release_i32(int *p, int v) {
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -123,23 +144,65 @@ __device__ __forceinline__ int4 rec_header(const PivRec *r, const int4 &h) {
 __device__ __forceinline__ int rec_entry(const int4 &e, int k) {
     return k == 0 ? e.x : k == 1 ? e.y : k == 2 ? e.z : e.w;
 }
+// The record of a row in one round trip, its header read with acquire: when
+// col is set, every field is final and the pivot's segment may be read.
+// The entries go first (relaxed, not held back by the acquire); an entry
+// still showing its marker, or a header field that does, is read again
+// after the acquire, when the publisher's writes are visible.
+__device__ __forceinline__ bool rec_torn(const int4 &h, const int4 &e) {
+    const int need = h.y < 4 ? h.y : 4;
+    return h.y <= 0 || (unsigned)h.w == SEG4_NONE || e.x < 0 || (need > 1 && e.y < 0) || (need > 2 && e.z < 0) ||
+           (need > 3 && e.w < 0);
+}
+__device__ __forceinline__ void rec_load_acq(const PivRec *r, int4 &h, int4 &e) {
+    const int4 *p = reinterpret_cast<const int4 *>(r);
+    e = __ldcg(p + 1);
+    h = ld_acquire_v4(p);
+    if (h.x >= 0 && rec_torn(h, e)) {
+        h = __ldcg(p);
+        e = __ldcg(p + 1);
+    }
+}
+// A record fetched ahead without holding the fetching thread back: a strong
+// relaxed read now (rec_fetch), and, where it is used, an acquire fence when
+// it showed a pivot (rec_settle): the pair acts as rec_load_acq.
+__device__ __forceinline__ void rec_fetch(const PivRec *r, int4 &h, int4 &e) {
+    const int4 *p = reinterpret_cast<const int4 *>(r);
+    e = ld_relaxed_v4(p + 1);
+    h = ld_relaxed_v4(p);
+}
+__device__ __forceinline__ void rec_settle(const PivRec *r, int4 &h, int4 &e) {
+    if (h.x < 0) return;
+    fence_acq_rel();
+    if (rec_torn(h, e)) {
+        const int4 *p = reinterpret_cast<const int4 *>(r);
+        h = __ldcg(p);
+        e = __ldcg(p + 1);
+    }
+}
 
-// Publish column `col` (length n, segment seg, first rows in `rows`) as the
-// pivot of row `row`.  Called by one thread after the column's rows are
-// visible to it (its own writes, or writes ordered before by a barrier).
-// ORDERED = false when the readers run in a later kernel (Phase 0 / I).
+// Publish column `col` (length n, segment seg) as the pivot of row `row`;
+// `top` holds its min(n, 4) highest rows, ascending.  Called by one thread
+// after the column's rows are visible to it (its own writes, or writes
+// ordered before by a barrier).  ORDERED = false when the readers run in a
+// later kernel (Phase 0 / I).
 template <bool ORDERED = true>
-__device__ __forceinline__ void rec_publish(PivRec *rec, int row, int col, int n, long long seg, const int *rows) {
+__device__ __forceinline__ void rec_publish_top(PivRec *rec, int row, int col, int n, long long seg, const int *top) {
     PivRec *r = rec + row;
     r->np = n;
     r->seg4 = (unsigned)(seg >> 2);
-    for (int k = 0; k < 4; k++) r->e[k] = k < n ? rows[k] : -1;
+    for (int k = 0; k < 4; k++) r->e[k] = k < n ? top[k] : -1;
     if (ORDERED) {
         fence_acq_rel();
         st_release_i32(&r->col, col);
     } else {
         r->col = col;
     }
+}
+// The same from the column's n rows.
+template <bool ORDERED = true>
+__device__ __forceinline__ void rec_publish(PivRec *rec, int row, int col, int n, long long seg, const int *rows) {
+    rec_publish_top<ORDERED>(rec, row, col, n, seg, rows + (n > 4 ? n - 4 : 0));
 }
 
 __device__ __forceinline__ int round4(int n) { return (n + 3) & ~3; }

@@ -91,7 +91,7 @@ __global__ void k_p1_first(PmsArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.st->reps = 0;
         a.st->wl_count = 0;
-        for (int t = 0; t < 4; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
+        for (int t = 0; t < 5; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
         a.st->s_cursor = 0;
         a.st->s_out = 0;
         if (OPH_COUNTS) a.st->diag[5] = 0;  // the eager tier's longest chain, per sweep
@@ -935,10 +935,11 @@ __global__ void __launch_bounds__(BLOCK) k_p2_scalar(PmsArgs a, ScalarQ sq) {
                     a.seg[j] = dst;
                     a.low[j] = lj;
                     if (fin == 3) {
-                        int first[4];
-                        for (int k = 0; k < 4; k++) first[k] = k < n ? col[k * 32] : -1;
+                        int top[4];
+                        const int k0 = n > 4 ? n - 4 : 0;
+                        for (int k = 0; k < 4; k++) top[k] = k0 + k < n ? col[(k0 + k) * 32] : -1;
                         a.classes[j] = -1;
-                        rec_publish(a.rec, lj, j, n, dst, first);
+                        rec_publish_top(a.rec, lj, j, n, dst, top);
                     }
                     handoff = fin == 1;
                 }
@@ -1131,6 +1132,29 @@ constexpr size_t SBM_BYTES = sizeof(uint32_t) * SBM_WORDS;
 // True when column j's rows (first T0, low lj) lie in a shared window.
 __device__ __forceinline__ bool fits_sbm(int T0, int lj) { return (long long)lj - T0 < 32ll * SBM_WORDS - 32; }
 
+// The start of a CTA's column: its low and that row's pivot record, read by
+// one thread and shared, so that every thread of the CTA takes the same
+// branches around its barriers (the clear flag and the record can change
+// under other chains between two threads' reads).  True when an addition is
+// due: not cleared, a low whose pivot lies to the left.
+__device__ __forceinline__ bool col_start(const PmsArgs &a, int j, int &lj, int4 &h, int4 &e) {
+    __shared__ __align__(16) int4 s_he[2];
+    __shared__ int s_lj;
+    if (threadIdx.x == 0) {
+        const int l = a.clear[j] ? -1 : a.low[j];
+        int4 hh = make_int4(-1, 0, 0, 0), ee = make_int4(-1, -1, -1, -1);
+        if (l >= 0) rec_load_acq(&a.rec[l], hh, ee);
+        s_lj = l;
+        s_he[0] = hh;
+        s_he[1] = ee;
+    }
+    __syncthreads();  // rewritten only by the next column's call, behind the caller's queue barriers
+    lj = s_lj;
+    h = s_he[0];
+    e = s_he[1];
+    return lj >= 0 && h.x >= 0 && h.x < j;
+}
+
 // Tiers 2 and 3: the whole CTA on one column.  With cap > 0 the column and
 // the staged pivot live in shared memory (A/B/C of cap ints); with cap == 0
 // they live in pool-allocated buffers that grow as needed.
@@ -1138,13 +1162,11 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
                                     int32_t *out_list, int *out_cnt, long long &adds, long long &slots) {
     __shared__ long long s_off;
     __shared__ int s_small[4];
+    __shared__ __align__(16) int4 s_rec[2];
     const int tid = threadIdx.x;
-    if (a.clear[j]) return;
-    int lj = a.low[j];
-    if (lj < 0) return;
+    int lj;
     int4 h, e;
-    rec_load(&a.rec[lj], h, e);
-    if (h.x < 0 || h.x >= j) return;
+    if (!col_start(a, j, lj, h, e)) return;
     const long long sj = a.seg[j];
     int n = a.pool[sj];
     const int capj = a.pool[sj + 1];
@@ -1167,18 +1189,27 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
         block_copy(A, a.pool + sj + SEG_HDR, n);
     }
     bool made_pivot = false, handed = false;
+    // The record came with acquire (rec_load_acq), so a wide pivot's rows are
+    // read straight from its segment.  When the next low is known before the
+    // merge (the larger of the column's and the pivot's second rows, when
+    // they differ), thread 0 fetches its record during the copy and the
+    // merge and settles it after: one round trip per addition off the chain.
+    int t1 = n >= 2 ? A[n - 2] : -1;
     for (;;) {
-        int np;
+        const int np = h.y;
+        const bool inrec = np <= 4;
+        const int p2 = np >= 2 ? (inrec ? rec_entry(e, np - 2) : e.z) : -1;
+        const bool known = t1 != p2 || t1 < 0;
+        const int pnext = known ? max(t1, p2) : -1;
+        int4 hh = make_int4(-1, 0, 0, 0), ee = make_int4(-1, -1, -1, -1);
+        if (tid == 0 && pnext >= 0) rec_fetch(&a.rec[pnext], hh, ee);
         const int *P;
-        if (rec_complete(h, e)) {
-            np = h.y;
+        if (inrec) {
             if (tid < np) s_small[tid] = rec_entry(e, tid);
             __syncthreads();
             P = s_small;
         } else {
-            const int4 h2 = rec_header(&a.rec[lj], h);
-            np = h2.y;
-            P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
+            P = a.pool + 4ll * (unsigned)h.w + SEG_HDR;
         }
         if (n + np > bcap) {
             if (smem_mode) { handed = true; break; }
@@ -1201,10 +1232,24 @@ __device__ void reduce_column_block(const PmsArgs &a, int j, int *sA, int *sB, i
         int *t = A; A = B; B = t;
         lj = n ? A[n - 1] : -1;
         if (lj < 0) break;
-        rec_load(&a.rec[lj], h, e);
+        if (known && lj == pnext) {
+            if (tid == 0) {
+                rec_settle(&a.rec[lj], hh, ee);
+                s_rec[0] = hh;
+                s_rec[1] = ee;
+            }
+        } else if (tid == 0) {
+            rec_load_acq(&a.rec[lj], hh, ee);
+            s_rec[0] = hh;
+            s_rec[1] = ee;
+        }
+        __syncthreads();  // rewritten only after the next merge's barriers
+        h = s_rec[0];
+        e = s_rec[1];
         mark_clear<false>(a, lj, tid == 0);  // few columns: no hot flags
         if (h.z == j) { made_pivot = true; break; }
         if (h.x < 0 || h.x >= j) break;
+        t1 = n >= 2 ? A[n - 2] : -1;
     }
     long long dst = sj;
     int dcap = capj;
@@ -1340,21 +1385,62 @@ __device__ int bitmap_extract(uint32_t *bm, int lo, int top, int w0, int *dst, i
     return out;
 }
 
+// The highest set bit of the bitmap strictly below bit `pos` (relative to
+// the window), -1 when there is none: a warp's search from the top, 128
+// words a step, 16-byte loads (the words above pos's own are clear or
+// masked).
+template <bool SM>
+__device__ __forceinline__ int bm_below(const uint32_t *bm, int pos) {
+    const int lane = threadIdx.x & 31;
+    if (pos <= 0) return -1;
+    const int wl = (pos - 1) >> 5;
+    const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));  // bits 0 .. (pos - 1) & 31
+    for (int c0 = wl & ~3; c0 >= 0; c0 -= 128) {
+        const int w = c0 - 4 * lane;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (w >= 0) v = bm_load4<SM>(bm + w);
+        const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
+        const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
+        const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
+        const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
+        const int hi = q3 ? (w + 3) * 32 + 31 - __clz(q3)
+                     : q2 ? (w + 2) * 32 + 31 - __clz(q2)
+                     : q1 ? (w + 1) * 32 + 31 - __clz(q1)
+                     : q0 ? w * 32 + 31 - __clz(q0) : -1;
+        const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
+        if (nz) return __shfl_sync(0xffffffffu, hi, __ffs(nz) - 1);  // the lowest lane holds the highest words
+    }
+    return -1;
+}
+
 // Returns true when the column needs the merge path (its state written back
 // first).
+//
+// One addition: the pivot's rows toggle their bits (warps 0 .. 30), warp 0
+// then counts the column and finds its next low and the set bit below that;
+// two CTA barriers.  The chain's latency is the round trips to L2, so they
+// are taken off it where the data allow:
+// * the record of the low is read with acquire in one round trip
+//   (rec_load_acq), and a wide pivot's rows are loaded in one more, the
+//   window check riding on the toggles (a row below the window undoes them);
+// * the next low is most often known before the toggles: with t1 the
+//   column's set bit below its low and p2 the pivot's second-highest row
+//   (the record holds the pivot's top rows), it is max(t1, p2) unless the
+//   two are equal and cancel.  Warp 31 then fetches that row's record while
+//   the other warps load and toggle the pivot, so an addition costs about
+//   one round trip instead of two.
 template <bool SM>
 __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int64_t bm_words, long long &adds,
                                      long long &slots) {
-    __shared__ int s_red[32];
+    __shared__ int s_red[32], s_fb[32];
     __shared__ int s_small[4];
+    __shared__ int s_lo;
+    __shared__ __align__(16) int4 s_rec[2][2];  // per parity of the addition: the prefetched record
     __shared__ long long s_off;
     const int tid = threadIdx.x;
-    if (a.clear[j]) return false;
-    int lj = a.low[j];
-    if (lj < 0) return false;
+    int lj;
     int4 h, e;
-    rec_load(&a.rec[lj], h, e);
-    if (h.x < 0 || h.x >= j) return false;
+    if (!col_start(a, j, lj, h, e)) return false;
     const long long sj = a.seg[j];
     int n = a.pool[sj];
     const int capj = a.pool[sj + 1];
@@ -1363,69 +1449,91 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
     // the window's first row: a multiple of 32 with lj - w0 < nbits
     const int w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 31) & ~31ll) : 0;
     if (n > 0 && T[0] < w0) return true;
-    int lo_row = n > 0 ? T[0] : lj;  // no set bit below it
+    int t1 = n >= 2 ? T[n - 2] : -1;  // the set bit below the low
+    if (tid == 0) s_lo = n > 0 ? T[0] : lj;  // no set bit below it
     for (int k = tid; k < n; k += blockDim.x) {
         const int r = T[k] - w0;
         atomicOr(bm + (r >> 5), 1u << (r & 31));
     }
     __syncthreads();
     bool made_pivot = false, fell_back = false;
-    // Two CTA barriers per addition: the whole CTA toggles the pivot's bits
-    // and leaves per-warp counts; warp 0 totals them and finds the next low
-    // (128 words a step, 16-byte loads) for everyone.
     const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    for (;;) {
-        int np;
-        const int *P = nullptr;
-        if (rec_complete(h, e)) {
-            np = h.y;  // rows in the record, which every thread holds
+    const int ntg = blockDim.x - 32;  // toggling threads: every warp but the last
+    for (int par = 0;; par ^= 1) {
+        const int np = h.y;
+        const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
+        const int p2 = np >= 2 ? (P ? e.z : rec_entry(e, np - 2)) : -1;
+        const bool known = t1 != p2 || t1 < 0;
+        const int pnext = known ? max(t1, p2) : -1;  // -1 when known: T = P, the sum is zero
+        if (wid == nw - 1) {
+            if (lane == 0 && pnext >= 0) {
+                int4 hh, ee;
+                rec_load_acq(&a.rec[pnext], hh, ee);
+                s_rec[par][0] = hh;
+                s_rec[par][1] = ee;
+            }
         } else {
-            const int4 h2 = rec_header(&a.rec[lj], h);
-            np = h2.y;
-            P = a.pool + 4ll * (unsigned)h2.w + SEG_HDR;
+            int d = 0;
+            bool below = false;
+            for (int k = tid; k < np; k += ntg) {
+                const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
+                if (r < 0) {
+                    below = true;
+                    continue;
+                }
+                if (k == 0) s_lo = min(s_lo, r + w0);  // only thread 0 writes it
+                const uint32_t bit = 1u << (r & 31);
+                d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
+            }
+            for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            const unsigned fb = __ballot_sync(0xffffffffu, below);
+            if (lane == 0) {
+                s_red[wid] = d;
+                s_fb[wid] = fb != 0u;
+            }
         }
-        const int p0 = P ? P[0] : rec_entry(e, 0);
-        if (p0 < w0) {  // the pivot reaches below the window
+        __syncthreads();
+        if (wid == 0) {
+            int t = lane < nw - 1 ? s_red[lane] : 0;
+            int f = lane < nw - 1 ? s_fb[lane] : 0;
+            for (int o = 16; o > 0; o >>= 1) {
+                t += __shfl_xor_sync(0xffffffffu, t, o);
+                f |= __shfl_xor_sync(0xffffffffu, f, o);
+            }
+            const int nn = n + t;
+            int next = -1, nb = -1;
+            if (!f && nn > 0) {
+                // lj's bit went with the pivot's top: the next low lies below it
+                next = known ? (pnext >= 0 ? pnext - w0 : -1) : bm_below<SM>(bm, lj - w0);
+                if (nn > 1 && next >= 0) nb = bm_below<SM>(bm, next);
+            }
+            if (lane == 0) {
+                if (!f && next >= 0 && !(known && w0 + next == pnext)) {
+                    int4 hh, ee;
+                    rec_load_acq(&a.rec[w0 + next], hh, ee);
+                    s_rec[par][0] = hh;
+                    s_rec[par][1] = ee;
+                }
+                s_small[0] = nn;
+                s_small[1] = next;  // -1: zero column (or, never, no bit left)
+                s_small[2] = nb;    // the set bit below it
+                s_small[3] = f;     // the pivot reaches below the window
+            }
+        }
+        __syncthreads();
+        const int nn = s_small[0], next = s_small[1], nb = s_small[2];
+        if (s_small[3]) {
+            // undo the toggles: the column is back to its state before this
+            // addition, which the merge path takes over
+            if (wid < nw - 1)
+                for (int k = tid; k < np; k += ntg) {
+                    const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
+                    if (r >= 0) atomicXor(bm + (r >> 5), 1u << (r & 31));
+                }
+            __syncthreads();
             fell_back = true;
             break;
         }
-        lo_row = min(lo_row, p0);
-        int d = 0;
-        for (int k = tid; k < np; k += blockDim.x) {
-            const int r = (P ? P[k] : rec_entry(e, k & 3)) - w0;
-            const uint32_t bit = 1u << (r & 31);
-            d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
-        }
-        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-        if (lane == 0) s_red[wid] = d;
-        __syncthreads();
-        if (wid == 0) {
-            int t = lane < nw ? s_red[lane] : 0;
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-            const int nn = n + t;
-            int next = -1;
-            if (nn > 0) {
-                // lj's bit went with the pivot's top: the next low lies below it
-                for (int c0 = ((lj - w0) >> 5) & ~3; c0 >= 0 && next < 0; c0 -= 128) {
-                    const int w = c0 - 4 * lane;
-                    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-                    if (w >= 0) v = bm_load4<SM>(bm + w);
-                    const int hi = v.w ? w + 3 : v.z ? w + 2 : v.y ? w + 1 : v.x ? w : -1;
-                    const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
-                    if (nz) {
-                        const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
-                        const int hw = __shfl_sync(0xffffffffu, hi, src);
-                        next = hw * 32 + 31 - __clz(bm_load<SM>(bm + hw));
-                    }
-                }
-            }
-            if (lane == 0) {
-                s_small[0] = nn;
-                s_small[1] = next;  // -1: zero column (or, never, no bit left)
-            }
-        }
-        __syncthreads();
-        const int nn = s_small[0], next = s_small[1];
         slots += n + np + nn;
         adds++;
         n = nn;
@@ -1435,11 +1543,14 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             break;
         }
         lj = w0 + next;
-        rec_load(&a.rec[lj], h, e);
+        t1 = nb >= 0 ? w0 + nb : -1;
+        h = s_rec[par][0];
+        e = s_rec[par][1];
         mark_clear<false>(a, lj, tid == 0);
         if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
         if (h.x < 0 || h.x >= j) break;
     }
+    const int lo_row = s_lo;
     long long dst = sj;
     int dcap = capj;
     bool stored = true;
@@ -1500,16 +1611,429 @@ __global__ void __launch_bounds__(BLOCK) k_p2_bitmap(PmsArgs a, int tier) {
         if (threadIdx.x == 0) {
             const int lj = a.low[j];
             const long long sj = a.seg[j];
-            s_fit = lj >= 0 && fits_sbm(a.pool[sj] > 0 ? a.pool[sj + SEG_HDR] : lj, lj);
+            s_fit = lj < 0 ? -1 : fits_sbm(a.pool[sj] > 0 ? a.pool[sj + SEG_HDR] : lj, lj);
         }
         __syncthreads();
+        if (s_fit < 0) continue;  // nothing left to add (s_fit is rewritten behind the next barrier pair)
         const bool fit = s_fit;
         bool fell = true;
         if (fit) fell = reduce_column_bitmap<true>(a, j, sbm, SBM_WORDS, adds, slots);
+        if (fell && a.cluster_tier) {
+            // wider than the shared window: the cluster tier's, next
+            if (threadIdx.x == 0) a.worklist[atomicAdd(&a.st->t_count[4], 1)] = j;
+            continue;
+        }
         if (fell && bm) fell = reduce_column_bitmap<false>(a, j, bm, a.bm_words, adds, slots);
         if (fell) reduce_column_block(a, j, nullptr, nullptr, nullptr, 0, scratch, nullptr, nullptr, adds, slots);
     }
     if (threadIdx.x == 0) tier_stats(a, tier, adds, slots);
+}
+
+// ------------------------------------------------------------ cluster tier
+// Tier 4: a column whose rows span more than one CTA's shared window (on a
+// Rips complex's anti-transpose the longest reduced cochains reach across
+// the whole matrix) is held as a bitmap spread over the shared memory of a
+// cluster of CL CTAs, CTA r holding rows [w0 + r CL_ROWS, w0 + (r+1) CL_ROWS).
+// Every CTA of the cluster loads its slice of the column and writes its part
+// of the result back; the chain of additions in between runs on the first
+// CTA, whose threads toggle the pivot's bits and search for the next low
+// through distributed shared memory (a few hundred cycles an access, where
+// the global bitmap costs an L2 round trip per toggle round and search step).
+#ifndef OPH_CL
+#define OPH_CL 8
+#endif
+constexpr int CL_SIZE = OPH_CL;
+constexpr int CL_WORDS = 49152;         // bitmap words per CTA (192 KB)
+constexpr int CL_ROWS = 32 * CL_WORDS;  // rows per CTA
+constexpr size_t CL_BYTES = sizeof(uint32_t) * CL_WORDS;
+constexpr int CL_BLOCK = 1024;
+
+// The next low of T xor P where the column's rows below its low that are
+// listed (t[0..tc), descending; every row of T at or above tfloor below the
+// low is listed, and `tall` when T has no other rows at all) and the
+// pivot's rows below its top that its record holds decide it: an absolute
+// row, -1 for a zero sum, -2 when they do not decide it.
+__device__ __forceinline__ int predict_next(const int (&t)[4], int tc, int tfloor, bool tall, const int4 &e, int np) {
+    int pr[3];
+    int pc;
+    bool pmore;
+    if (np <= 4) {
+        pc = np - 1;
+        pr[0] = np >= 2 ? rec_entry(e, np - 2) : -1;
+        pr[1] = np >= 3 ? rec_entry(e, np - 3) : -1;
+        pr[2] = np >= 4 ? e.x : -1;
+        pmore = false;
+    } else {
+        pr[0] = e.z;
+        pr[1] = e.y;
+        pr[2] = e.x;
+        pc = 3;
+        pmore = true;
+    }
+    int i = 0, k = 0;
+#pragma unroll
+    for (int step = 0; step < 8; step++) {
+        const bool ht = i < tc, hp = k < pc;
+        const int ti = i == 0 ? t[0] : i == 1 ? t[1] : i == 2 ? t[2] : t[3];
+        const int pk = k == 0 ? pr[0] : k == 1 ? pr[1] : pr[2];
+        if (ht && hp) {
+            if (ti != pk) return max(ti, pk);
+            i++;
+            k++;
+            continue;
+        }
+        if (ht) return pmore ? -2 : ti;           // P's remaining rows are unknown (or none)
+        if (hp) return pk >= tfloor ? pk : -2;    // T has no unlisted row at or above tfloor
+        return (tall && !pmore) ? -1 : -2;
+    }
+    return -2;
+}
+
+// The highest set bits (up to five) of the cluster bitmap below window row
+// `pos`, descending, as window rows in b0..b4; returns how many.  A warp's
+// search from the top, 128 words a step through distributed shared memory;
+// it stops at five bits, or one step after the step that found the first.
+// *floor: every set bit in [*floor, pos) was returned (0: the search reached
+// the bottom).
+__device__ __forceinline__ int cl_scan5(const cg::cluster_group &cl, uint32_t *cbm, int pos, int &b0, int &b1,
+                                        int &b2, int &b3, int &b4, int *floor) {
+    const int lane = threadIdx.x & 31;
+    int cnt = 0;
+    *floor = 0;
+    if (pos <= 0) return 0;
+    const int wl = (pos - 1) >> 5;
+    const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
+    bool last = false;
+    for (int c0 = wl & ~3; c0 >= 0; c0 -= 128) {
+        const int w = c0 - 4 * lane;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (w >= 0) {
+            const int q = w / CL_WORDS;
+            v = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(cbm, q) + (w - q * CL_WORDS));
+        }
+        const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
+        const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
+        const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
+        const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
+        unsigned nz = __ballot_sync(0xffffffffu, (q0 | q1 | q2 | q3) != 0u);
+        while (nz && cnt < 5) {
+            const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
+            nz &= nz - 1;
+            const int ws = __shfl_sync(0xffffffffu, w, src);
+#pragma unroll
+            for (int k = 3; k >= 0; k--) {
+                uint32_t x = __shfl_sync(0xffffffffu, k == 3 ? q3 : k == 2 ? q2 : k == 1 ? q1 : q0, src);
+                while (x && cnt < 5) {
+                    const int hb = 31 - __clz(x);
+                    const int r = (ws + k) * 32 + hb;
+                    x &= ~(1u << hb);
+                    if (cnt == 0) b0 = r;
+                    else if (cnt == 1) b1 = r;
+                    else if (cnt == 2) b2 = r;
+                    else if (cnt == 3) b3 = r;
+                    else b4 = r;
+                    cnt++;
+                }
+            }
+        }
+        if (cnt >= 5) {
+            *floor = b4;
+            return cnt;
+        }
+        if (last) {
+            *floor = c0 >= 124 ? (c0 - 124) * 32 : 0;
+            return cnt;
+        }
+        if (cnt > 0) last = true;
+    }
+    return cnt;
+}
+
+struct ClState {  // the leader's decision on the next queued column, copied into every CTA
+    int idx;      // queue position (>= the queue's count: no work left)
+    int go;       // 0: nothing to do, 1: the cluster bitmap, 2: the merge path (rows below the window)
+    int j, lj, n, w0, lo;
+};
+struct ClResult {  // the leader's chain, copied into every CTA
+    int n, lj, lo, made, fell, stored, dcap, pad;
+    long long dst;
+};
+
+template <int CL>
+__global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_cluster(PmsArgs a, int tier) {
+    if (a.st->converged) return;
+    const int count = a.st->t_count[tier];
+    if (count == 0) return;  // both read alike by every CTA: written by an earlier kernel
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = CL_BLOCK / 32;
+    extern __shared__ __align__(16) uint32_t cbm[];  // CL_WORDS, zero between columns
+    __shared__ ClState s_cs[2];      // per parity of the loop: written by the leader into every CTA
+    __shared__ ClResult s_res[2];
+    __shared__ int s_cnt[2][CL];     // (leader) set bits per slice
+    __shared__ int s_red[32], s_fb[32];
+    __shared__ int s_small[4];
+    __shared__ int s_tl[6];
+    __shared__ int s_lo;
+    __shared__ __align__(16) int4 s_rec[2][2];
+    __shared__ long long s_off;
+    __shared__ int scratch[2 * (CL_BLOCK / 32)];
+    const int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
+    for (int q = 4 * tid; q < CL_WORDS; q += 4 * CL_BLOCK)
+        *reinterpret_cast<uint4 *>(cbm + q) = make_uint4(0u, 0u, 0u, 0u);
+    cl.sync();  // every CTA of the cluster running, its slice zeroed
+    long long adds = 0, slots = 0;
+    for (int it = 0;; it ^= 1) {
+        if (rank == 0 && tid == 0) {
+            ClState c{};
+            c.idx = atomicAdd(&a.st->t_cursor[tier], 1);
+            if (c.idx < count) {
+                const int j = in_list[c.idx];
+                const int lj = a.clear[j] ? -1 : a.low[j];
+                c.j = j;
+                if (lj >= 0) {
+                    int4 h, e;
+                    rec_load_acq(&a.rec[lj], h, e);
+                    if (h.x >= 0 && h.x < j) {
+                        const long long sj = a.seg[j];
+                        const long long nbits = (long long)CL * CL_ROWS;
+                        c.lj = lj;
+                        c.n = a.pool[sj];
+                        c.w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 127) & ~127ll) : 0;
+                        c.lo = c.n > 0 ? a.pool[sj + SEG_HDR] : lj;
+                        c.go = c.lo < c.w0 ? 2 : 1;
+                    }
+                }
+            }
+            for (int q = 0; q < CL; q++) *cl.map_shared_rank(&s_cs[it], q) = c;
+        }
+        cl.sync();
+        const ClState c = s_cs[it];
+        if (c.idx >= count) break;
+        if (c.go == 0) continue;
+        if (c.go == 2) {
+            if (rank == 0)
+                reduce_column_block(a, c.j, nullptr, nullptr, nullptr, 0, scratch, nullptr, nullptr, adds, slots);
+            continue;
+        }
+        const int j = c.j, w0 = c.w0;
+        const long long sj = a.seg[j];
+        const int capj = a.pool[sj + 1];
+        const int *T = a.pool + sj + SEG_HDR;
+        // every CTA: its slice of the column
+        {
+            const int r0 = rank * CL_ROWS;
+            for (int k = tid; k < c.n; k += CL_BLOCK) {
+                const int r = T[k] - w0 - r0;
+                if ((unsigned)r < (unsigned)CL_ROWS) atomicOr(cbm + (r >> 5), 1u << (r & 31));
+            }
+        }
+        cl.sync();
+        if (rank == 0) {
+            // the chain, on this CTA: warps 0 .. nw-2 toggle the pivot's bits
+            // in whichever slice holds them, warp nw-1 fetches the record of
+            // the predicted next low meanwhile, warp 0 counts and searches;
+            // two CTA barriers per addition
+            int lj = c.lj, n = c.n;
+            int4 h, e;
+            if (tid == 0) {
+                rec_load_acq(&a.rec[lj], h, e);
+                s_rec[1][0] = h;
+                s_rec[1][1] = e;
+            }
+            __syncthreads();  // s_rec[1] is next written by the second addition
+            h = s_rec[1][0];
+            e = s_rec[1][1];
+            int t[4] = {-1, -1, -1, -1};
+            int tc = min(4, max(n - 1, 0));
+            for (int q = 0; q < tc; q++) t[q] = T[n - 2 - q];
+            int tfloor = n - 1 > 4 ? t[3] : 0;
+            bool tall = n - 1 <= 4;
+            bool made = false, fell = false;
+            if (tid == 0) s_lo = c.lo;
+            const int ntg = CL_BLOCK - 32;
+            if (h.x >= 0 && h.x < j) {
+                for (int par = 0;; par ^= 1) {
+                    const int np = h.y;
+                    const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
+                    const int pn = predict_next(t, tc, tfloor, tall, e, np);
+                    if (wid == nw - 1) {
+                        if (lane == 0 && pn >= 0) {
+                            int4 hh, ee;
+                            rec_load_acq(&a.rec[pn], hh, ee);
+                            s_rec[par][0] = hh;
+                            s_rec[par][1] = ee;
+                        }
+                    } else {
+                        int d = 0;
+                        bool below = false;
+                        for (int k = tid; k < np; k += ntg) {
+                            const int row = P ? __ldcg(P + k) : rec_entry(e, k);
+                            const int r = row - w0;
+                            if (r < 0) {
+                                below = true;
+                                continue;
+                            }
+                            if (k == 0) s_lo = min(s_lo, row);  // only thread 0 writes it
+                            const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
+                            uint32_t *wp = cl.map_shared_rank(cbm, q) + (lr >> 5);
+                            const uint32_t bit = 1u << (lr & 31);
+                            d += (atomicXor(wp, bit) & bit) ? -1 : 1;
+                        }
+                        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                        const unsigned fb = __ballot_sync(0xffffffffu, below);
+                        if (lane == 0) {
+                            s_red[wid] = d;
+                            s_fb[wid] = fb != 0u;
+                        }
+                    }
+                    __syncthreads();
+                    if (wid == 0) {
+                        int tt = lane < nw - 1 ? s_red[lane] : 0;
+                        int f = lane < nw - 1 ? s_fb[lane] : 0;
+                        for (int o = 16; o > 0; o >>= 1) {
+                            tt += __shfl_xor_sync(0xffffffffu, tt, o);
+                            f |= __shfl_xor_sync(0xffffffffu, f, o);
+                        }
+                        const int nn = n + tt;
+                        int b0 = -1, b1 = -1, b2 = -1, b3 = -1, b4 = -1, fl = 0, cnt = 0;
+                        if (!f && nn > 0) cnt = cl_scan5(cl, cbm, lj - w0, b0, b1, b2, b3, b4, &fl);
+                        const int next = cnt > 0 ? w0 + b0 : -1;
+                        if (lane == 0) {
+                            if (!f && next >= 0 && next != pn) {
+                                int4 hh, ee;
+                                rec_load_acq(&a.rec[next], hh, ee);
+                                s_rec[par][0] = hh;
+                                s_rec[par][1] = ee;
+                            }
+                            s_small[0] = nn;
+                            s_small[1] = next;  // -1: zero column
+                            s_small[2] = f;     // a pivot row below the window
+                            s_small[3] = cnt;
+                            s_tl[0] = b1 >= 0 ? w0 + b1 : -1;
+                            s_tl[1] = b2 >= 0 ? w0 + b2 : -1;
+                            s_tl[2] = b3 >= 0 ? w0 + b3 : -1;
+                            s_tl[3] = b4 >= 0 ? w0 + b4 : -1;
+                            s_tl[4] = w0 + fl;  // every row at or above it below the next low is listed
+                            s_tl[5] = fl == 0 && cnt < 5;  // the search reached the bottom: all rows listed
+                        }
+                    }
+                    __syncthreads();
+                    const int nn = s_small[0], next = s_small[1], cnt = s_small[3];
+                    if (s_small[2]) {
+                        // undo the toggles: the column is as before this
+                        // addition; the merge path takes over after the write-back
+                        if (wid < nw - 1)
+                            for (int k = tid; k < np; k += ntg) {
+                                const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
+                                if (r < 0) continue;
+                                const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
+                                atomicXor(cl.map_shared_rank(cbm, q) + (lr >> 5), 1u << (lr & 31));
+                            }
+                        __syncthreads();
+                        fell = true;
+                        break;
+                    }
+                    slots += n + np + nn;
+                    adds++;
+                    n = nn;
+                    if (next < 0) {
+                        n = 0;
+                        lj = -1;
+                        break;
+                    }
+                    lj = next;
+                    tc = max(cnt - 1, 0);
+                    t[0] = s_tl[0];
+                    t[1] = s_tl[1];
+                    t[2] = s_tl[2];
+                    t[3] = s_tl[3];
+                    tfloor = s_tl[4];
+                    tall = s_tl[5] != 0;
+                    h = s_rec[par][0];
+                    e = s_rec[par][1];
+                    mark_clear<false>(a, lj, tid == 0);
+                    if (h.z == j) {  // the beta check: row lj first appears in j
+                        made = true;
+                        break;
+                    }
+                    if (h.x < 0 || h.x >= j) break;
+                }
+            }
+            // the result, and the column's new segment when it outgrew its own
+            if (tid == 0) {
+                ClResult r{};
+                r.n = n;
+                r.lj = lj;
+                r.lo = s_lo;
+                r.made = made;
+                r.fell = fell;
+                r.stored = 1;
+                r.dst = sj;
+                r.dcap = capj;
+                if (n > capj) {
+                    r.dcap = round4(max(n + (n >> 1), 16));
+                    r.dst = col_alloc(a, j, SEG_HDR + r.dcap);
+                    r.stored = r.dst >= 0;  // pool exhausted: j keeps its pre-sweep state
+                }
+                for (int q = 0; q < CL; q++) *cl.map_shared_rank(&s_res[it], q) = r;
+            }
+        }
+        cl.sync();
+        // every CTA: its slice of the result, after the set bits of the
+        // slices below it, then the words zeroed
+        const ClResult r = s_res[it];
+        const int lo_w = (r.lo - w0) >> 5, top_w = r.n > 0 ? (r.lj - w0) >> 5 : -1;
+        const int s0 = rank * CL_WORDS;
+        const int a_w = max(lo_w, s0) - s0, b_w = min(top_w, s0 + CL_WORDS - 1) - s0;
+        {
+            int cnt = 0;
+            for (int w = (a_w & ~3) + 4 * tid; w <= b_w; w += 4 * CL_BLOCK) {
+                const uint4 v = *reinterpret_cast<const uint4 *>(cbm + w);
+                cnt += __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+            }
+            for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            if (lane == 0) s_red[wid] = cnt;
+            __syncthreads();
+            if (tid == 0) {
+                int tot = 0;
+                for (int q = 0; q < nw; q++) tot += s_red[q];
+                *cl.map_shared_rank(&s_cnt[it][rank], 0) = tot;
+            }
+        }
+        cl.sync();
+        int off = 0;
+        {
+            const int *cnts = cl.map_shared_rank(&s_cnt[it][0], 0);
+            for (int q = 0; q < rank; q++) off += cnts[q];
+        }
+        bitmap_extract<true>(cbm, a_w, b_w, w0 + rank * CL_ROWS, r.stored ? a.pool + r.dst + SEG_HDR + off : nullptr,
+                             s_red);
+        __threadfence();  // this slice's rows visible before the leader publishes the column
+        cl.sync();
+        if (rank == 0) {
+            if (r.stored) {
+                if (tid == 0) {
+                    a.pool[r.dst] = r.n;
+                    a.pool[r.dst + 1] = r.dcap;
+                    a.seg[j] = r.dst;
+                    a.low[j] = r.lj;
+                    if (r.made) {
+                        a.classes[j] = -1;
+                        fence_acq_rel();
+                        rec_publish(a.rec, r.lj, j, r.n, r.dst, a.pool + r.dst + SEG_HDR);
+                    }
+                }
+                if (r.fell) {
+                    __syncthreads();
+                    reduce_column_block(a, j, nullptr, nullptr, nullptr, 0, scratch, nullptr, nullptr, adds, slots);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (rank == 0 && tid == 0) tier_stats(a, 3, adds, slots);  // counted with the bitmap tier
+    cl.sync();  // no CTA leaves while another may still reach its shared memory
 }
 
 __global__ void k_count_sweep(DevStatus *st) {
@@ -1600,6 +2124,33 @@ int t0_candidate(int v, int *lanes, int *cap) {
     return 0;
 }
 
+// The cluster tier's grid: as many clusters as can be resident at once (at
+// most 16), each CL_SIZE CTAs of 1024 threads and CL_BYTES of shared memory;
+// 0 when the device runs no such cluster.
+static int cluster_grid(Context *ctx) {
+    static int done[64], grid[64];
+    const int d = ctx->device & 63;
+    if (done[d]) return grid[d];
+    done[d] = 1;
+    grid[d] = 0;
+    if (cudaFuncSetAttribute(k_p2_cluster<CL_SIZE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CL_BYTES) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(CL_SIZE * 16, 1, 1);
+    cfg.blockDim = dim3(CL_BLOCK, 1, 1);
+    cfg.dynamicSmemBytes = CL_BYTES;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, k_p2_cluster<CL_SIZE>, &cfg) != cudaSuccess || nc < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    grid[d] = CL_SIZE * std::min(nc, 16);
+    return grid[d];
+}
+
 int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
     static int done1[64], done2[64], dones[64];
     g->ss = (size_t)TS_BLOCK * TS_CAP * sizeof(int);
@@ -1620,6 +2171,7 @@ int sweep_grids(Context *ctx, int64_t m, int64_t ntiles, SweepGrids *g) {
         else
             done3[ctx->device & 63] = 1;
     }
+    g->g4 = cluster_grid(ctx);
     g->m = (int)std::max<int64_t>(1, std::min<int64_t>((m + 255) / 256, (int64_t)ctx->sm_count * 16));
     g->t = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * 8));
     if (g->g0 < 0 || g->g1 < 0 || g->g2 < 0 || g->gs < 0 || g->g3 < 0) {
@@ -1729,6 +2281,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
     k_p2_block<T2_CAP, T2_BLOCK><<<g.g2, T2_BLOCK, g.s2, s>>>(a, 2);
     if (ev) cudaEventRecord(ev[4], s);
     k_p2_bitmap<BM_BLOCK><<<g.g3, BM_BLOCK, SBM_BYTES, s>>>(a, 3);
+    if (a.cluster_tier) k_p2_cluster<CL_SIZE><<<g.g4, CL_BLOCK, CL_BYTES, s>>>(a, 4);
     k_count_sweep<<<1, 1, 0, s>>>(a.st);
     if (ev) cudaEventRecord(ev[5], s);
 }
@@ -1745,9 +2298,10 @@ void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int par
 }
 
 // Kernels one sweep launches (launch_sweep_ev): Phase I (six with the
-// compacted list, else five), the scalar tier, tiers 0-3, the counter.
+// compacted list, else five), the scalar tier, tiers 0-3, the cluster tier
+// when it runs, the counter.
 static int kernels_per_sweep(const PmsArgs &a) {
-    return (a.ulist ? 6 : 5) + (a.slist ? 1 : 0) + 4 + 1;
+    return (a.ulist ? 6 : 5) + (a.slist ? 1 : 0) + 4 + (a.cluster_tier ? 1 : 0) + 1;
 }
 
 // Sweeps replayed from a captured CUDA graph (0: launched one by one).
@@ -1882,6 +2436,7 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     // tier 3's bitmaps: a window of the whole matrix up to 2^23 rows per CTA,
     // zeroed here (each column leaves its words zeroed)
     a.bm_words = std::min<int64_t>(((m + 32) / 32 + 3) & ~3ll, BM_MAX_WORDS);
+    a.cluster_tier = g.g4 > 0 && !getenv("OPH_NO_CLUSTER");
     a.bm = (uint32_t *)ctx_alloc(ctx, S_BITMAP, sizeof(uint32_t) * (size_t)a.bm_words * g.g3);
     if (!a.bm) return OPH_ERR_OOM;
     OPH_CUDA_TRY(cudaMemsetAsync(a.bm, 0, sizeof(uint32_t) * (size_t)a.bm_words * g.g3, s));

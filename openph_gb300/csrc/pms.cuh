@@ -50,6 +50,10 @@ struct PmsArgs {
     // tier 3 merges)
     uint32_t *bm;
     int64_t bm_words;
+    // tier 4: columns wider than a CTA's shared window go to the cluster
+    // tier (a bitmap across a cluster's shared memory) instead of the
+    // global bitmap (0: tier 3 keeps them)
+    int cluster_tier;
     // per-instance bucket order (the server, whose instances are reduced on
     // D or on their anti-transpose; nullptr: `ascending` above for all):
     // iasc[b] = 1 for an instance in ascending order, ibucket[b * MAXC + d]
@@ -70,6 +74,7 @@ struct SweepGrids {
     int v0;                 // tier-0 candidate in use
     int m, t;               // grid of the per-column passes, Phase I tiles
     int g0, g1, g2, g3;     // Phase II tier grids
+    int g4;                 //   the cluster tier's (a multiple of its cluster size; 0: none)
     int gs;                 //   and the scalar tier's
     size_t s0, s1, s2, ss;  // their dynamic shared memory
 };
