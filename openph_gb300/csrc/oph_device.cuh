@@ -115,6 +115,7 @@ __device__ __forceinline__ int4 ld_acquire_v4(const int4 *p) {
                  : "memory");
     return v;
 }
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 __device__ __forceinline__ int4 ld_relaxed_v4(const int4 *p) {
     int4 v;
     asm volatile("ld.relaxed.gpu.global.v4.s32 {%0, %1, %2, %3}, [%4];"

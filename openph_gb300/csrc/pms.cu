@@ -1648,62 +1648,18 @@ constexpr int CL_ROWS = 32 * CL_WORDS;  // rows per CTA
 constexpr size_t CL_BYTES = sizeof(uint32_t) * CL_WORDS;
 constexpr int CL_BLOCK = 1024;
 
-// The next low of T xor P where the column's rows below its low that are
-// listed (t[0..tc), descending; every row of T at or above tfloor below the
-// low is listed, and `tall` when T has no other rows at all) and the
-// pivot's rows below its top that its record holds decide it: an absolute
-// row, -1 for a zero sum, -2 when they do not decide it.
-__device__ __forceinline__ int predict_next(const int (&t)[4], int tc, int tfloor, bool tall, const int4 &e, int np) {
-    int pr[3];
-    int pc;
-    bool pmore;
-    if (np <= 4) {
-        pc = np - 1;
-        pr[0] = np >= 2 ? rec_entry(e, np - 2) : -1;
-        pr[1] = np >= 3 ? rec_entry(e, np - 3) : -1;
-        pr[2] = np >= 4 ? e.x : -1;
-        pmore = false;
-    } else {
-        pr[0] = e.z;
-        pr[1] = e.y;
-        pr[2] = e.x;
-        pc = 3;
-        pmore = true;
-    }
-    int i = 0, k = 0;
-#pragma unroll
-    for (int step = 0; step < 8; step++) {
-        const bool ht = i < tc, hp = k < pc;
-        const int ti = i == 0 ? t[0] : i == 1 ? t[1] : i == 2 ? t[2] : t[3];
-        const int pk = k == 0 ? pr[0] : k == 1 ? pr[1] : pr[2];
-        if (ht && hp) {
-            if (ti != pk) return max(ti, pk);
-            i++;
-            k++;
-            continue;
-        }
-        if (ht) return pmore ? -2 : ti;           // P's remaining rows are unknown (or none)
-        if (hp) return pk >= tfloor ? pk : -2;    // T has no unlisted row at or above tfloor
-        return (tall && !pmore) ? -1 : -2;
-    }
-    return -2;
-}
+// Named barrier among the first `count` threads of the CTA (id 1; 0 is
+// __syncthreads): the chain's warps meet without the prefetching warp.
+__device__ __forceinline__ void bar_named(int count) { asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory"); }
 
-// The highest set bits (up to five) of the cluster bitmap below window row
-// `pos`, descending, as window rows in b0..b4; returns how many.  A warp's
-// search from the top, 128 words a step through distributed shared memory;
-// it stops at five bits, or one step after the step that found the first.
-// *floor: every set bit in [*floor, pos) was returned (0: the search reached
-// the bottom).
-__device__ __forceinline__ int cl_scan5(const cg::cluster_group &cl, uint32_t *cbm, int pos, int &b0, int &b1,
-                                        int &b2, int &b3, int &b4, int *floor) {
+// The highest set bit of the cluster bitmap strictly below window row `pos`,
+// -1 when there is none: a warp's search from the top, 128 words a step
+// through distributed shared memory.
+__device__ __forceinline__ int cl_below(const cg::cluster_group &cl, uint32_t *cbm, int pos) {
     const int lane = threadIdx.x & 31;
-    int cnt = 0;
-    *floor = 0;
-    if (pos <= 0) return 0;
+    if (pos <= 0) return -1;
     const int wl = (pos - 1) >> 5;
     const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
-    bool last = false;
     for (int c0 = wl & ~3; c0 >= 0; c0 -= 128) {
         const int w = c0 - 4 * lane;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
@@ -1715,38 +1671,96 @@ __device__ __forceinline__ int cl_scan5(const cg::cluster_group &cl, uint32_t *c
         const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
         const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
         const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
-        unsigned nz = __ballot_sync(0xffffffffu, (q0 | q1 | q2 | q3) != 0u);
-        while (nz && cnt < 5) {
-            const int src = __ffs(nz) - 1;  // the lowest lane holds the highest words
-            nz &= nz - 1;
-            const int ws = __shfl_sync(0xffffffffu, w, src);
-#pragma unroll
-            for (int k = 3; k >= 0; k--) {
-                uint32_t x = __shfl_sync(0xffffffffu, k == 3 ? q3 : k == 2 ? q2 : k == 1 ? q1 : q0, src);
-                while (x && cnt < 5) {
-                    const int hb = 31 - __clz(x);
-                    const int r = (ws + k) * 32 + hb;
-                    x &= ~(1u << hb);
-                    if (cnt == 0) b0 = r;
-                    else if (cnt == 1) b1 = r;
-                    else if (cnt == 2) b2 = r;
-                    else if (cnt == 3) b3 = r;
-                    else b4 = r;
-                    cnt++;
-                }
+        const int hi = q3 ? (w + 3) * 32 + 31 - __clz(q3)
+                     : q2 ? (w + 2) * 32 + 31 - __clz(q2)
+                     : q1 ? (w + 1) * 32 + 31 - __clz(q1)
+                     : q0 ? w * 32 + 31 - __clz(q0) : -1;
+        const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
+        if (nz) return __shfl_sync(0xffffffffu, hi, __ffs(nz) - 1);  // the lowest lane holds the highest words
+    }
+    return -1;
+}
+
+// The prefetching warp of a cluster chain.  In a large matrix the pivot
+// records and pivot rows a chain visits sit in HBM, not L2, and each
+// addition waits on the record of its low and then on the pivot's rows.
+// Most next lows of a long column are among its highest set bits below the
+// current low (84% on the anti-transpose of a Rips torus, 75% within the
+// highest 16), so this warp, outside the chain's barriers, follows the low
+// the chain publishes (`cur`): it takes the 32 highest set bits below it
+// (lane k the k-th, from a racy view of the bitmap: only what is prefetched
+// depends on it), prefetches their records into L2, and for the candidates
+// of its previous round (whose records have had that long to arrive) reads
+// the record and prefetches the pivot's rows.  It stops when `done` is set,
+// or after a bounded number of rounds.
+__device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uint32_t *cbm, int w0,
+                              const volatile int *cur, const volatile int *done, int *cand, int *tmp) {
+    const int lane = threadIdx.x & 31;
+    for (int k = lane; k < 64; k += 32) cand[k] = -1;
+    __syncwarp();
+    int last = -2, par = 0;
+    for (int round = 0; round < (1 << 20); round++) {
+        const int d = __shfl_sync(0xffffffffu, *done, 0);
+        if (d) break;
+        const int lj = __shfl_sync(0xffffffffu, *cur, 0);
+        if (lj == last || lj < 0) {
+            __nanosleep(100);
+            continue;
+        }
+        last = lj;
+        // the pivots of the previous round's candidates
+        const int cp = cand[(par ^ 1) * 32 + lane];
+        if (cp >= 0) {
+            const int4 hc = __ldcg(reinterpret_cast<const int4 *>(&a.rec[cp]));
+            if (hc.x >= 0 && hc.y > 4 && (unsigned)hc.w != SEG4_NONE) {
+                const int *P = a.pool + 4ll * (unsigned)hc.w + SEG_HDR;
+                const int lines = min((4 * hc.y + 127) >> 7, 16);
+                for (int q = 0; q < lines; q++) prefetch_l2(P + 32 * q);
             }
         }
-        if (cnt >= 5) {
-            *floor = b4;
-            return cnt;
+        // this round's candidates: the 32 highest set bits below the low, at
+        // most four steps of 128 words down
+        tmp[lane] = -1;
+        __syncwarp();
+        const int pos = lj - w0;
+        const int wl = (pos - 1) >> 5;
+        const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
+        int got = 0;
+        for (int c0 = wl & ~3, st = 0; pos > 0 && c0 >= 0 && st < 4 && got < 32; c0 -= 128, st++) {
+            const int w = c0 - 4 * lane;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (w >= 0) {
+                const int q = w / CL_WORDS;
+                v = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(cbm, q) + (w - q * CL_WORDS));
+            }
+            const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
+            const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
+            const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
+            const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
+            const int c = __popc(q0) + __popc(q1) + __popc(q2) + __popc(q3);
+            int incl = c;  // lane 0 holds the highest words: ranks run up the lanes
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            int r = got + incl - c;
+            const uint32_t qs[4] = {q3, q2, q1, q0};
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                for (uint32_t x = qs[k]; x && r < 32; r++) {
+                    const int hb = 31 - __clz(x);
+                    x &= ~(1u << hb);
+                    tmp[r] = (w + 3 - k) * 32 + hb;
+                }
+            got += __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
         }
-        if (last) {
-            *floor = c0 >= 124 ? (c0 - 124) * 32 : 0;
-            return cnt;
-        }
-        if (cnt > 0) last = true;
+        const int my = tmp[lane];
+        __syncwarp();
+        if (my >= 0) prefetch_l2(&a.rec[w0 + my]);
+        cand[par * 32 + lane] = my >= 0 ? w0 + my : -1;
+        par ^= 1;
     }
-    return cnt;
 }
 
 struct ClState {  // the leader's decision on the next queued column, copied into every CTA
@@ -1773,8 +1787,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
     __shared__ int s_cnt[2][CL];     // (leader) set bits per slice
     __shared__ int s_red[32], s_fb[32];
     __shared__ int s_small[4];
-    __shared__ int s_tl[6];
     __shared__ int s_lo;
+    __shared__ volatile int s_cur, s_done;   // the chain's low and its end, for the prefetching warp
+    __shared__ int s_cand[64], s_ctmp[32];  // the prefetching warp's candidates
     __shared__ __align__(16) int4 s_rec[2][2];
     __shared__ long long s_off;
     __shared__ int scratch[2 * (CL_BLOCK / 32)];
@@ -1831,63 +1846,53 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
         cl.sync();
         if (rank == 0) {
             // the chain, on this CTA: warps 0 .. nw-2 toggle the pivot's bits
-            // in whichever slice holds them, warp nw-1 fetches the record of
-            // the predicted next low meanwhile, warp 0 counts and searches;
-            // two CTA barriers per addition
+            // in whichever slice holds them (each thread one row), warp 0
+            // counts, searches for the next low and reads its record; two
+            // barriers of those warps per addition.  Warp nw-1 prefetches
+            // ahead of them (cl_prefetcher), outside their barriers.
             int lj = c.lj, n = c.n;
             int4 h, e;
             if (tid == 0) {
                 rec_load_acq(&a.rec[lj], h, e);
                 s_rec[1][0] = h;
                 s_rec[1][1] = e;
+                s_lo = c.lo;
+                s_cur = lj;
+                s_done = 0;
             }
             __syncthreads();  // s_rec[1] is next written by the second addition
             h = s_rec[1][0];
             e = s_rec[1][1];
-            int t[4] = {-1, -1, -1, -1};
-            int tc = min(4, max(n - 1, 0));
-            for (int q = 0; q < tc; q++) t[q] = T[n - 2 - q];
-            int tfloor = n - 1 > 4 ? t[3] : 0;
-            bool tall = n - 1 <= 4;
             bool made = false, fell = false;
-            if (tid == 0) s_lo = c.lo;
             const int ntg = CL_BLOCK - 32;
-            if (h.x >= 0 && h.x < j) {
+            if (wid == nw - 1) {
+                cl_prefetcher(a, cl, cbm, w0, &s_cur, &s_done, s_cand, s_ctmp);
+            } else if (h.x >= 0 && h.x < j) {
                 for (int par = 0;; par ^= 1) {
                     const int np = h.y;
                     const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
-                    const int pn = predict_next(t, tc, tfloor, tall, e, np);
-                    if (wid == nw - 1) {
-                        if (lane == 0 && pn >= 0) {
-                            int4 hh, ee;
-                            rec_load_acq(&a.rec[pn], hh, ee);
-                            s_rec[par][0] = hh;
-                            s_rec[par][1] = ee;
+                    int d = 0;
+                    bool below = false;
+                    for (int k = tid; k < np; k += ntg) {
+                        const int row = P ? __ldcg(P + k) : rec_entry(e, k);
+                        const int r = row - w0;
+                        if (r < 0) {
+                            below = true;
+                            continue;
                         }
-                    } else {
-                        int d = 0;
-                        bool below = false;
-                        for (int k = tid; k < np; k += ntg) {
-                            const int row = P ? __ldcg(P + k) : rec_entry(e, k);
-                            const int r = row - w0;
-                            if (r < 0) {
-                                below = true;
-                                continue;
-                            }
-                            if (k == 0) s_lo = min(s_lo, row);  // only thread 0 writes it
-                            const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
-                            uint32_t *wp = cl.map_shared_rank(cbm, q) + (lr >> 5);
-                            const uint32_t bit = 1u << (lr & 31);
-                            d += (atomicXor(wp, bit) & bit) ? -1 : 1;
-                        }
-                        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-                        const unsigned fb = __ballot_sync(0xffffffffu, below);
-                        if (lane == 0) {
-                            s_red[wid] = d;
-                            s_fb[wid] = fb != 0u;
-                        }
+                        if (k == 0) s_lo = min(s_lo, row);  // only thread 0 writes it
+                        const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
+                        uint32_t *wp = cl.map_shared_rank(cbm, q) + (lr >> 5);
+                        const uint32_t bit = 1u << (lr & 31);
+                        d += (atomicXor(wp, bit) & bit) ? -1 : 1;
                     }
-                    __syncthreads();
+                    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                    const unsigned fb = __ballot_sync(0xffffffffu, below);
+                    if (lane == 0) {
+                        s_red[wid] = d;
+                        s_fb[wid] = fb != 0u;
+                    }
+                    bar_named(ntg);
                     if (wid == 0) {
                         int tt = lane < nw - 1 ? s_red[lane] : 0;
                         int f = lane < nw - 1 ? s_fb[lane] : 0;
@@ -1896,11 +1901,11 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                             f |= __shfl_xor_sync(0xffffffffu, f, o);
                         }
                         const int nn = n + tt;
-                        int b0 = -1, b1 = -1, b2 = -1, b3 = -1, b4 = -1, fl = 0, cnt = 0;
-                        if (!f && nn > 0) cnt = cl_scan5(cl, cbm, lj - w0, b0, b1, b2, b3, b4, &fl);
-                        const int next = cnt > 0 ? w0 + b0 : -1;
+                        const int b = (!f && nn > 0) ? cl_below(cl, cbm, lj - w0) : -1;
+                        const int next = b >= 0 ? w0 + b : -1;
                         if (lane == 0) {
-                            if (!f && next >= 0 && next != pn) {
+                            if (next >= 0) {
+                                s_cur = next;  // for the prefetching warp
                                 int4 hh, ee;
                                 rec_load_acq(&a.rec[next], hh, ee);
                                 s_rec[par][0] = hh;
@@ -1909,28 +1914,19 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                             s_small[0] = nn;
                             s_small[1] = next;  // -1: zero column
                             s_small[2] = f;     // a pivot row below the window
-                            s_small[3] = cnt;
-                            s_tl[0] = b1 >= 0 ? w0 + b1 : -1;
-                            s_tl[1] = b2 >= 0 ? w0 + b2 : -1;
-                            s_tl[2] = b3 >= 0 ? w0 + b3 : -1;
-                            s_tl[3] = b4 >= 0 ? w0 + b4 : -1;
-                            s_tl[4] = w0 + fl;  // every row at or above it below the next low is listed
-                            s_tl[5] = fl == 0 && cnt < 5;  // the search reached the bottom: all rows listed
                         }
                     }
-                    __syncthreads();
-                    const int nn = s_small[0], next = s_small[1], cnt = s_small[3];
+                    bar_named(ntg);
+                    const int nn = s_small[0], next = s_small[1];
                     if (s_small[2]) {
                         // undo the toggles: the column is as before this
                         // addition; the merge path takes over after the write-back
-                        if (wid < nw - 1)
-                            for (int k = tid; k < np; k += ntg) {
-                                const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
-                                if (r < 0) continue;
-                                const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
-                                atomicXor(cl.map_shared_rank(cbm, q) + (lr >> 5), 1u << (lr & 31));
-                            }
-                        __syncthreads();
+                        for (int k = tid; k < np; k += ntg) {
+                            const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
+                            if (r < 0) continue;
+                            const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
+                            atomicXor(cl.map_shared_rank(cbm, q) + (lr >> 5), 1u << (lr & 31));
+                        }
                         fell = true;
                         break;
                     }
@@ -1943,13 +1939,6 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                         break;
                     }
                     lj = next;
-                    tc = max(cnt - 1, 0);
-                    t[0] = s_tl[0];
-                    t[1] = s_tl[1];
-                    t[2] = s_tl[2];
-                    t[3] = s_tl[3];
-                    tfloor = s_tl[4];
-                    tall = s_tl[5] != 0;
                     h = s_rec[par][0];
                     e = s_rec[par][1];
                     mark_clear<false>(a, lj, tid == 0);
@@ -1960,6 +1949,8 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                     if (h.x < 0 || h.x >= j) break;
                 }
             }
+            if (tid == 0) s_done = 1;
+            __syncthreads();  // every warp, the prefetcher included, past the chain (and any undo)
             // the result, and the column's new segment when it outgrew its own
             if (tid == 0) {
                 ClResult r{};
