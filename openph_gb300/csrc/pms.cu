@@ -1485,21 +1485,17 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
                 const uint32_t bit = 1u << (r & 31);
                 d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
             }
-            for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-            const unsigned fb = __ballot_sync(0xffffffffu, below);
+            d = __reduce_add_sync(0xffffffffu, d);
+            const bool fb = __any_sync(0xffffffffu, below);
             if (lane == 0) {
                 s_red[wid] = d;
-                s_fb[wid] = fb != 0u;
+                s_fb[wid] = fb;
             }
         }
         __syncthreads();
         if (wid == 0) {
-            int t = lane < nw - 1 ? s_red[lane] : 0;
-            int f = lane < nw - 1 ? s_fb[lane] : 0;
-            for (int o = 16; o > 0; o >>= 1) {
-                t += __shfl_xor_sync(0xffffffffu, t, o);
-                f |= __shfl_xor_sync(0xffffffffu, f, o);
-            }
+            const int t = __reduce_add_sync(0xffffffffu, lane < nw - 1 ? s_red[lane] : 0);
+            const int f = __any_sync(0xffffffffu, lane < nw - 1 && s_fb[lane]);
             const int nn = n + t;
             int next = -1, nb = -1;
             if (!f && nn > 0) {
@@ -1652,10 +1648,17 @@ constexpr int CL_BLOCK = 1024;
 // __syncthreads): the chain's warps meet without the prefetching warp.
 __device__ __forceinline__ void bar_named(int count) { asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory"); }
 
+// Word w of the cluster bitmap (slice w / CL_WORDS), through the CTA's own
+// shared memory when it holds that slice.
+__device__ __forceinline__ uint32_t *cl_word(const cg::cluster_group &cl, uint32_t *cbm, int w, int rank) {
+    const int q = w / CL_WORDS;
+    return (q == rank ? cbm : cl.map_shared_rank(cbm, q)) + (w - q * CL_WORDS);
+}
+
 // The highest set bit of the cluster bitmap strictly below window row `pos`,
 // -1 when there is none: a warp's search from the top, 128 words a step
 // through distributed shared memory.
-__device__ __forceinline__ int cl_below(const cg::cluster_group &cl, uint32_t *cbm, int pos) {
+__device__ __forceinline__ int cl_below(const cg::cluster_group &cl, uint32_t *cbm, int pos, int rank) {
     const int lane = threadIdx.x & 31;
     if (pos <= 0) return -1;
     const int wl = (pos - 1) >> 5;
@@ -1663,10 +1666,7 @@ __device__ __forceinline__ int cl_below(const cg::cluster_group &cl, uint32_t *c
     for (int c0 = wl & ~3; c0 >= 0; c0 -= 128) {
         const int w = c0 - 4 * lane;
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (w >= 0) {
-            const int q = w / CL_WORDS;
-            v = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(cbm, q) + (w - q * CL_WORDS));
-        }
+        if (w >= 0) v = *reinterpret_cast<const uint4 *>(cl_word(cl, cbm, w, rank));
         const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
         const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
         const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
@@ -1687,18 +1687,15 @@ __device__ __forceinline__ int cl_below(const cg::cluster_group &cl, uint32_t *c
 // Most next lows of a long column are among its highest set bits below the
 // current low (84% on the anti-transpose of a Rips torus, 75% within the
 // highest 16), so this warp, outside the chain's barriers, follows the low
-// the chain publishes (`cur`): it takes the 32 highest set bits below it
-// (lane k the k-th, from a racy view of the bitmap: only what is prefetched
-// depends on it), prefetches their records into L2, and for the candidates
-// of its previous round (whose records have had that long to arrive) reads
-// the record and prefetches the pivot's rows.  It stops when `done` is set,
-// or after a bounded number of rounds.
-__device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uint32_t *cbm, int w0,
-                              const volatile int *cur, const volatile int *done, int *cand, int *tmp) {
+// the chain publishes (`cur`): each round it takes the 32 highest set bits
+// below it (lane k the k-th, from a racy view of the bitmap: only what is
+// prefetched depends on it), reads their records (bringing them into L2)
+// and prefetches the rows of their pivots.  It stops when `done` is set, or
+// after a bounded number of rounds.
+__device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uint32_t *cbm, int w0, int rank,
+                              const volatile int *cur, const volatile int *done, int *tmp) {
     const int lane = threadIdx.x & 31;
-    for (int k = lane; k < 64; k += 32) cand[k] = -1;
-    __syncwarp();
-    int last = -2, par = 0;
+    int last = -2;
     for (int round = 0; round < (1 << 20); round++) {
         const int d = __shfl_sync(0xffffffffu, *done, 0);
         if (d) break;
@@ -1708,18 +1705,8 @@ __device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uin
             continue;
         }
         last = lj;
-        // the pivots of the previous round's candidates
-        const int cp = cand[(par ^ 1) * 32 + lane];
-        if (cp >= 0) {
-            const int4 hc = __ldcg(reinterpret_cast<const int4 *>(&a.rec[cp]));
-            if (hc.x >= 0 && hc.y > 4 && (unsigned)hc.w != SEG4_NONE) {
-                const int *P = a.pool + 4ll * (unsigned)hc.w + SEG_HDR;
-                const int lines = min((4 * hc.y + 127) >> 7, 16);
-                for (int q = 0; q < lines; q++) prefetch_l2(P + 32 * q);
-            }
-        }
-        // this round's candidates: the 32 highest set bits below the low, at
-        // most four steps of 128 words down
+        // the 32 highest set bits below the low, at most four steps of 128
+        // words down
         tmp[lane] = -1;
         __syncwarp();
         const int pos = lj - w0;
@@ -1729,10 +1716,7 @@ __device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uin
         for (int c0 = wl & ~3, st = 0; pos > 0 && c0 >= 0 && st < 4 && got < 32; c0 -= 128, st++) {
             const int w = c0 - 4 * lane;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (w >= 0) {
-                const int q = w / CL_WORDS;
-                v = *reinterpret_cast<const uint4 *>(cl.map_shared_rank(cbm, q) + (w - q * CL_WORDS));
-            }
+            if (w >= 0) v = *reinterpret_cast<const uint4 *>(cl_word(cl, cbm, w, rank));
             const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
             const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
             const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
@@ -1757,9 +1741,14 @@ __device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uin
         }
         const int my = tmp[lane];
         __syncwarp();
-        if (my >= 0) prefetch_l2(&a.rec[w0 + my]);
-        cand[par * 32 + lane] = my >= 0 ? w0 + my : -1;
-        par ^= 1;
+        if (my >= 0) {
+            const int4 hc = __ldcg(reinterpret_cast<const int4 *>(&a.rec[w0 + my]));
+            if (hc.x >= 0 && hc.y > 4 && (unsigned)hc.w != SEG4_NONE) {
+                const int *P = a.pool + 4ll * (unsigned)hc.w + SEG_HDR;
+                const int lines = min((4 * hc.y + 127) >> 7, 16);
+                for (int q = 0; q < lines; q++) prefetch_l2(P + 32 * q);
+            }
+        }
     }
 }
 
@@ -1767,6 +1756,7 @@ struct ClState {  // the leader's decision on the next queued column, copied int
     int idx;      // queue position (>= the queue's count: no work left)
     int go;       // 0: nothing to do, 1: the cluster bitmap, 2: the merge path (rows below the window)
     int j, lj, n, w0, lo;
+    int chain;    // the CTA that runs the chain: the one holding the low's slice
 };
 struct ClResult {  // the leader's chain, copied into every CTA
     int n, lj, lo, made, fell, stored, dcap, pad;
@@ -1789,7 +1779,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
     __shared__ int s_small[4];
     __shared__ int s_lo;
     __shared__ volatile int s_cur, s_done;   // the chain's low and its end, for the prefetching warp
-    __shared__ int s_cand[64], s_ctmp[32];  // the prefetching warp's candidates
+    __shared__ int s_ctmp[32];  // the prefetching warp's candidates
     __shared__ __align__(16) int4 s_rec[2][2];
     __shared__ long long s_off;
     __shared__ int scratch[2 * (CL_BLOCK / 32)];
@@ -1817,6 +1807,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                         c.w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 127) & ~127ll) : 0;
                         c.lo = c.n > 0 ? a.pool[sj + SEG_HDR] : lj;
                         c.go = c.lo < c.w0 ? 2 : 1;
+                        c.chain = min((lj - c.w0) / CL_ROWS, CL - 1);
                     }
                 }
             }
@@ -1844,10 +1835,12 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
             }
         }
         cl.sync();
-        if (rank == 0) {
-            // the chain, on this CTA: warps 0 .. nw-2 toggle the pivot's bits
-            // in whichever slice holds them (each thread one row), warp 0
-            // counts, searches for the next low and reads its record; two
+        if (rank == c.chain) {
+            // the chain, on the CTA that holds the low's slice (where its
+            // searches and most of its toggles fall: the low of a long chain
+            // stays within one slice): warps 0 .. nw-2 toggle the pivot's
+            // bits in whichever slice holds them (each thread one row), warp
+            // 0 counts, searches for the next low and reads its record; two
             // barriers of those warps per addition.  Warp nw-1 prefetches
             // ahead of them (cl_prefetcher), outside their barriers.
             int lj = c.lj, n = c.n;
@@ -1866,7 +1859,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
             bool made = false, fell = false;
             const int ntg = CL_BLOCK - 32;
             if (wid == nw - 1) {
-                cl_prefetcher(a, cl, cbm, w0, &s_cur, &s_done, s_cand, s_ctmp);
+                cl_prefetcher(a, cl, cbm, w0, rank, &s_cur, &s_done, s_ctmp);
             } else if (h.x >= 0 && h.x < j) {
                 for (int par = 0;; par ^= 1) {
                     const int np = h.y;
@@ -1881,27 +1874,21 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                             continue;
                         }
                         if (k == 0) s_lo = min(s_lo, row);  // only thread 0 writes it
-                        const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
-                        uint32_t *wp = cl.map_shared_rank(cbm, q) + (lr >> 5);
-                        const uint32_t bit = 1u << (lr & 31);
-                        d += (atomicXor(wp, bit) & bit) ? -1 : 1;
+                        const uint32_t bit = 1u << (r & 31);
+                        d += (atomicXor(cl_word(cl, cbm, r >> 5, rank), bit) & bit) ? -1 : 1;
                     }
-                    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-                    const unsigned fb = __ballot_sync(0xffffffffu, below);
+                    d = __reduce_add_sync(0xffffffffu, d);
+                    const bool fb = __any_sync(0xffffffffu, below);
                     if (lane == 0) {
                         s_red[wid] = d;
-                        s_fb[wid] = fb != 0u;
+                        s_fb[wid] = fb;
                     }
                     bar_named(ntg);
                     if (wid == 0) {
-                        int tt = lane < nw - 1 ? s_red[lane] : 0;
-                        int f = lane < nw - 1 ? s_fb[lane] : 0;
-                        for (int o = 16; o > 0; o >>= 1) {
-                            tt += __shfl_xor_sync(0xffffffffu, tt, o);
-                            f |= __shfl_xor_sync(0xffffffffu, f, o);
-                        }
+                        const int tt = __reduce_add_sync(0xffffffffu, lane < nw - 1 ? s_red[lane] : 0);
+                        const int f = __any_sync(0xffffffffu, lane < nw - 1 && s_fb[lane]);
                         const int nn = n + tt;
-                        const int b = (!f && nn > 0) ? cl_below(cl, cbm, lj - w0) : -1;
+                        const int b = (!f && nn > 0) ? cl_below(cl, cbm, lj - w0, rank) : -1;
                         const int next = b >= 0 ? w0 + b : -1;
                         if (lane == 0) {
                             if (next >= 0) {
@@ -1924,8 +1911,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
                         for (int k = tid; k < np; k += ntg) {
                             const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
                             if (r < 0) continue;
-                            const int q = r / CL_ROWS, lr = r - q * CL_ROWS;
-                            atomicXor(cl.map_shared_rank(cbm, q) + (lr >> 5), 1u << (lr & 31));
+                            atomicXor(cl_word(cl, cbm, r >> 5, rank), 1u << (r & 31));
                         }
                         fell = true;
                         break;
@@ -2000,9 +1986,9 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
         }
         bitmap_extract<true>(cbm, a_w, b_w, w0 + rank * CL_ROWS, r.stored ? a.pool + r.dst + SEG_HDR + off : nullptr,
                              s_red);
-        __threadfence();  // this slice's rows visible before the leader publishes the column
+        __threadfence();  // this slice's rows visible before the chain's CTA publishes the column
         cl.sync();
-        if (rank == 0) {
+        if (rank == c.chain) {
             if (r.stored) {
                 if (tid == 0) {
                     a.pool[r.dst] = r.n;
@@ -2023,7 +2009,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
             __syncthreads();
         }
     }
-    if (rank == 0 && tid == 0) tier_stats(a, 3, adds, slots);  // counted with the bitmap tier
+    if (tid == 0) tier_stats(a, 3, adds, slots);  // counted with the bitmap tier
     cl.sync();  // no CTA leaves while another may still reach its shared memory
 }
 
