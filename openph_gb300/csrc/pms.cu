@@ -77,6 +77,10 @@ __device__ __forceinline__ int64_t p1_count(const PmsArgs &a) { return a.ulist ?
 __device__ __forceinline__ int64_t p1_col(const PmsArgs &a, int64_t idx) {
     return a.ulist ? (int64_t)a.ulist[idx] : idx;
 }
+// A compacted list that fits one tile: Phase I runs as one block
+// (k_p1_small) and the grid-wide Phase I kernels return at once.
+__device__ __forceinline__ bool p1_small(const PmsArgs &a) { return a.ulist && *a.ucur <= P1_TILE; }
+
 // Another column to the left holds the same low: a published pivot, or an
 // earlier column recorded in first[].
 __device__ __forceinline__ bool is_repeat(const PmsArgs &a, int64_t j, int lj) {
@@ -86,19 +90,17 @@ __device__ __forceinline__ bool is_repeat(const PmsArgs &a, int64_t j, int lj) {
 
 // (a) apply pending clears (clear_positives, pms_functions.cu:131-140) and
 //     record the first column of every low.
-__global__ void k_p1_first(PmsArgs a) {
-    if (a.st->converged) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.st->reps = 0;
-        a.st->wl_count = 0;
-        for (int t = 0; t < 5; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
-        a.st->s_cursor = 0;
-        a.st->s_out = 0;
-        if (OPH_COUNTS) a.st->diag[5] = 0;  // the eager tier's longest chain, per sweep
-    }
+__device__ __forceinline__ void p1_reset(const PmsArgs &a) {
+    a.st->reps = 0;
+    a.st->wl_count = 0;
+    for (int t = 0; t < 5; t++) { a.st->t_count[t] = 0; a.st->t_cursor[t] = 0; }
+    a.st->s_cursor = 0;
+    a.st->s_out = 0;
+    if (OPH_COUNTS) a.st->diag[5] = 0;  // the eager tier's longest chain, per sweep
+}
+__device__ __forceinline__ void p1_first_range(const PmsArgs &a, int64_t i0, int64_t stride) {
     const int64_t n = p1_count(a);
-    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n;
-         idx += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t idx = i0; idx < n; idx += stride) {
         const int64_t j = p1_col(a, idx);
         int lj = a.low[j];
         if (a.clear[j]) {
@@ -118,6 +120,11 @@ __global__ void k_p1_first(PmsArgs a) {
                 atomicMin(&a.first[lj], (int)j);
         }
     }
+}
+__global__ void k_p1_first(PmsArgs a) {
+    if (a.st->converged || p1_small(a)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) p1_reset(a);
+    p1_first_range(a, blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 __device__ __forceinline__ int warp_max(int v) {
@@ -182,7 +189,7 @@ __device__ __forceinline__ void k_p1_tiles_tile(PmsArgs a, const int64_t n, cons
 // for the machine, not for the matrix (a grid of one block per tile of
 // the full matrix costs ~0.3 ms of empty blocks per sweep at 3.5e8 columns).
 __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
-    if (a.st->converged) return;
+    if (a.st->converged || p1_small(a)) return;
     const int64_t n = p1_count(a);
     for (int64_t tile = blockIdx.x; tile * P1_TILE < n; tile += gridDim.x) {
         k_p1_tiles_tile(a, n, tile);
@@ -193,7 +200,7 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_tiles(PmsArgs a) {
 // (c) exclusive prefix max of the tile maxima, one warp per bucket; decides
 //     convergence (no repeated low anywhere).
 __global__ void k_p1_scan(PmsArgs a) {
-    if (a.st->converged) return;
+    if (a.st->converged || p1_small(a)) return;
     if (a.st->reps == 0) {
         if (threadIdx.x == 0) a.st->converged = 1;
         return;
@@ -347,7 +354,7 @@ __device__ __forceinline__ void k_p1_mark_tile(PmsArgs a, const int64_t n, const
 // for the machine, not for the matrix (a grid of one block per tile of
 // the full matrix costs ~0.3 ms of empty blocks per sweep at 3.5e8 columns).
 __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
-    if (a.st->converged) return;
+    if (a.st->converged || p1_small(a)) return;
     const int64_t n = p1_count(a);
     for (int64_t tile = blockIdx.x; tile * P1_TILE < n; tile += gridDim.x) {
         k_p1_mark_tile(a, n, tile);
@@ -355,9 +362,36 @@ __global__ void __launch_bounds__(P1_THREADS) k_p1_mark(PmsArgs a) {
     }
 }
 
+// The end of (e): the next list's length, and the bucket each instance (or
+// the matrix) opens to Phase II: the lowest with unresolved columns (counts
+// of this sweep's k_p1_mark, cleared for the next one).  One block.
+__device__ __forceinline__ void p1_kscan_tail(const PmsArgs &a, int total) {
+    if (threadIdx.x == 0) {
+        *a.unext = total;
+        if (a.ascending) {
+            int open = MAXC;
+            for (int d = MAXC - 1; d >= 0; d--) {
+                if (a.st->bucket_unres[d] > 0) open = d;
+                a.st->bucket_unres[d] = 0;
+            }
+            a.st->bucket_open = open;
+        }
+    }
+    if (a.iopen) {
+        for (int b = threadIdx.x; b < a.nslots; b += blockDim.x) {
+            int open = MAXC;
+            for (int d = MAXC - 1; d >= 0; d--) {
+                if (a.ibucket[b * MAXC + d] > 0) open = d;
+                a.ibucket[b * MAXC + d] = 0;
+            }
+            a.iopen[b] = a.iasc[b] ? open : MAXC;
+        }
+    }
+}
+
 // (e) compacted list: exclusive scan of the per-tile counts (one block).
 __global__ void k_p1_kscan(PmsArgs a) {
-    if (a.st->converged) return;
+    if (a.st->converged || p1_small(a)) return;
     __shared__ int wsum[32];
     const int64_t n = (p1_count(a) + P1_TILE - 1) / P1_TILE;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -382,31 +416,7 @@ __global__ void k_p1_kscan(PmsArgs a) {
         carry += total;
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        *a.unext = carry;
-        if (a.ascending) {
-            // the lowest bucket with unresolved columns opens (counts of
-            // this sweep's k_p1_mark, cleared for the next one)
-            int open = MAXC;
-            for (int d = MAXC - 1; d >= 0; d--) {
-                if (a.st->bucket_unres[d] > 0) open = d;
-                a.st->bucket_unres[d] = 0;
-            }
-            a.st->bucket_open = open;
-        }
-    }
-    if (a.iopen) {
-        // per instance: the lowest bucket with unresolved columns opens
-        // (counts of this sweep's k_p1_mark, cleared for the next one)
-        for (int b = threadIdx.x; b < a.nslots; b += blockDim.x) {
-            int open = MAXC;
-            for (int d = MAXC - 1; d >= 0; d--) {
-                if (a.ibucket[b * MAXC + d] > 0) open = d;
-                a.ibucket[b * MAXC + d] = 0;
-            }
-            a.iopen[b] = a.iasc[b] ? open : MAXC;
-        }
-    }
+    p1_kscan_tail(a, carry);
 }
 
 // (f) compacted list: the columns that stay unresolved, in order, into the
@@ -486,12 +496,45 @@ __device__ __forceinline__ void k_p1_scatter_tile(PmsArgs a, const int64_t n, co
 // for the machine, not for the matrix (a grid of one block per tile of
 // the full matrix costs ~0.3 ms of empty blocks per sweep at 3.5e8 columns).
 __global__ void __launch_bounds__(P1_THREADS) k_p1_scatter(PmsArgs a) {
-    if (a.st->converged) return;
+    if (a.st->converged || p1_small(a)) return;
     const int64_t n = p1_count(a);
     for (int64_t tile = blockIdx.x; tile * P1_TILE < n; tile += gridDim.x) {
         k_p1_scatter_tile(a, n, tile);
         __syncthreads();  // the next tile reuses the shared arrays
     }
+}
+
+// Phase I of a compacted list that fits one tile, as one block: (a)-(f) in
+// order with block barriers between them, the tile's scan prefix being the
+// empty one.  Six grid launches of mostly idle blocks become one.
+__global__ void __launch_bounds__(P1_THREADS) k_p1_small(PmsArgs a) {
+    if (a.st->converged || !p1_small(a)) return;
+    const int64_t n = p1_count(a);
+    if (threadIdx.x == 0) p1_reset(a);
+    __syncthreads();
+    p1_first_range(a, threadIdx.x, blockDim.x);
+    __syncthreads();
+    __shared__ int s_reps;
+    k_p1_tiles_tile(a, n, 0);
+    __syncthreads();
+    if (threadIdx.x == 0) s_reps = atomicAdd(&a.st->reps, 0);  // thread 0 added the tile's count
+    __syncthreads();
+    if (s_reps == 0) {  // no repeated low: converged
+        if (threadIdx.x == 0) a.st->converged = 1;
+        return;
+    }
+    if (threadIdx.x < MAXC) a.agg[threadIdx.x] = -1;  // nothing before the first tile
+    __syncthreads();
+    k_p1_mark_tile(a, n, 0);
+    __syncthreads();
+    int keep = 0;
+    if (threadIdx.x == 0) {  // the tile's count, written by thread 0; its offset is 0
+        keep = a.kagg[0];
+        a.kagg[0] = 0;
+    }
+    p1_kscan_tail(a, keep);  // reads `keep` on thread 0 only
+    __syncthreads();
+    k_p1_scatter_tile(a, n, 0);
 }
 
 // (e') without a compacted list: reset first[], apply the clears of this
@@ -2235,6 +2278,7 @@ static void launch_sweep_ev(const PmsArgs &a0, const SweepGrids &g, cudaStream_t
         a.t0_count = &a0.st->t_count[0];
     }
     if (ev) cudaEventRecord(ev[0], s);
+    if (a.ulist) k_p1_small<<<1, P1_THREADS, 0, s>>>(a);
     k_p1_first<<<g.m, 256, 0, s>>>(a);
     k_p1_tiles<<<g.t, P1_THREADS, 0, s>>>(a);
     k_p1_scan<<<1, 32 * MAXC, 0, s>>>(a);
@@ -2274,11 +2318,11 @@ void launch_sweep(const PmsArgs &a, const SweepGrids &g, cudaStream_t s, int par
     launch_sweep_ev(a, g, s, ev, parity);
 }
 
-// Kernels one sweep launches (launch_sweep_ev): Phase I (six with the
-// compacted list, else five), the scalar tier, tiers 0-3, the cluster tier
+// Kernels one sweep launches (launch_sweep_ev): Phase I (the one-block
+// kernel and six grid kernels with the compacted list, else five), the scalar tier, tiers 0-3, the cluster tier
 // when it runs, the counter.
 static int kernels_per_sweep(const PmsArgs &a) {
-    return (a.ulist ? 6 : 5) + (a.slist ? 1 : 0) + 4 + (a.cluster_tier ? 1 : 0) + 1;
+    return (a.ulist ? 7 : 5) + (a.slist ? 1 : 0) + 4 + (a.cluster_tier ? 1 : 0) + 1;
 }
 
 // Sweeps replayed from a captured CUDA graph (0: launched one by one).
