@@ -462,8 +462,8 @@ __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_warp(const int64
 }
 
 // the same for the queued columns of MID_COL < n <= LONG_COL rows: eight
-// values a lane up to WIDE_COL rows, else a bitonic network over the warp's
-// slice of shared memory
+// values a lane up to WIDE_COL rows, sixteen up to twice that, else a
+// bitonic network over the warp's slice of shared memory
 __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_wide(const int64_t *__restrict__ dcolptr,
                                                                      int *__restrict__ pool,
                                                                      int32_t *__restrict__ low,
@@ -481,6 +481,11 @@ __global__ void __launch_bounds__(FIN_WARPS * 32) k_dual_finish_wide(const int64
         int *R = pool + seg_start(c, a) + SEG_HDR;
         if (n <= WIDE_COL) {
             const int top = warp_sort_column<8>(R, n);
+            if (lane == 0) low[c] = top;
+            continue;
+        }
+        if (n <= 2 * WIDE_COL) {  // sixteen values a lane: in registers, no warp barriers
+            const int top = warp_sort_column<16>(R, n);
             if (lane == 0) low[c] = top;
             continue;
         }
