@@ -350,8 +350,9 @@ def run_reference(args, ws, rank):
 # --------------------------------------------------------------- torus
 # What bounds each Phase II kernel, from its ncu captures (profiles/).
 ROOFLINE_NOTES = {
-    "tier3": "latency-bound: chains of dependent additions on a few long columns of the anti-transpose; "
-             "the merge-equivalent bytes are what a merge would move, far above the kernel's DRAM traffic",
+    "tier3": "latency-bound: chains of dependent additions on a few long columns of the anti-transpose "
+             "(each addition waits on its low's pivot record, then the pivot's rows, from L2 or HBM); the "
+             "merge-equivalent bytes are what a merge would move, far above the kernels' DRAM traffic",
     "narrow": "instruction-issue-bound (ncu: 60-89% issue active, DRAM 1-2%); T stays on chip per chain",
 }
 
@@ -517,7 +518,9 @@ def run_torus(args, ws, rank, local, bm, dist):
                         "k_p2_scalar + k_p2_tier<8,128,256> (scalar tier and tier 0, a pair per sweep)"),
              "tier1": (tier_ms[0], slot_prof["tier_slots"][1], "k_p2_tier1<32,512,256> (tier 1)"),
              "tier2": (tier_ms[1], slot_prof["tier_slots"][2], "k_p2_block<8192,256> (tier 2)"),
-             "tier3": (tier_ms[2], slot_prof["tier_slots"][3], "k_p2_bitmap<1024> (tier 3, bitmap columns)")}
+             "tier3": (tier_ms[2], slot_prof["tier_slots"][3],
+                       "k_p2_bitmap<1024> + k_p2_cluster<8> (tier 3: bitmap columns in one CTA's shared window, "
+                       "wider ones across a cluster's shared memory; one launch of each per sweep)")}
     dom = max(comps, key=lambda k: comps[k][0])
     dom_ms, dom_slots, dom_name = comps[dom]
     per_red_dom_s = dom_ms / 1e3 / args.steps

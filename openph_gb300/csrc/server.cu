@@ -714,6 +714,8 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
         cudaGetLastError();
     }
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
+    // columns wider than a CTA's shared window go to the cluster tier
+    a.cluster_tier = ok && sv->g.g4 > 0;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->sub_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->adm_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (ok) ok = cudaEventCreateWithFlags(&sv->adm_done, cudaEventDisableTiming) == cudaSuccess;
