@@ -1456,6 +1456,250 @@ __device__ __forceinline__ int bm_below(const uint32_t *bm, int pos) {
     return -1;
 }
 
+// Named barrier among the first `count` threads of the CTA (id 1; 0 is
+// __syncthreads): a chain's warps meet without its prefetching warp.
+__device__ __forceinline__ void bar_named(int count) { asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory"); }
+
+// A bitmap window seen through `word(w)`: a pointer to its word w, in the
+// CTA's own shared memory (tier 3) or in the slice of a cluster that holds it
+// (tier 4, distributed shared memory).
+
+// The highest set bit strictly below window row `pos`, -1 when there is
+// none: a warp's search from the top, 128 words a step.
+template <class W>
+__device__ __forceinline__ int bits_below(W word, int pos) {
+    const int lane = threadIdx.x & 31;
+    if (pos <= 0) return -1;
+    const int wl = (pos - 1) >> 5;
+    const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
+    for (int c0 = wl & ~3; c0 >= 0; c0 -= 128) {
+        const int w = c0 - 4 * lane;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (w >= 0) v = *reinterpret_cast<const uint4 *>(word(w));
+        const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
+        const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
+        const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
+        const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
+        const int hi = q3 ? (w + 3) * 32 + 31 - __clz(q3)
+                     : q2 ? (w + 2) * 32 + 31 - __clz(q2)
+                     : q1 ? (w + 1) * 32 + 31 - __clz(q1)
+                     : q0 ? w * 32 + 31 - __clz(q0) : -1;
+        const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
+        if (nz) return __shfl_sync(0xffffffffu, hi, __ffs(nz) - 1);  // the lowest lane holds the highest words
+    }
+    return -1;
+}
+
+// The prefetching warp of a chain.  In a large matrix the pivot records and
+// pivot rows a chain visits sit in HBM, not L2, and each addition waits on
+// the record of its low and then on the pivot's rows.  Most next lows of a
+// long column are among its highest set bits below the current low (84% on
+// the anti-transpose of a Rips torus, 75% within the highest 16), so this
+// warp, outside the chain's barriers, follows the low the chain publishes
+// (`cur`): each round it takes the 32 highest set bits below it (lane k the
+// k-th, from a racy view of the bitmap: only what is prefetched depends on
+// it), reads their records (bringing them into L2) and prefetches the rows of
+// their pivots.  It stops when `done` is set, or after a bounded number of
+// rounds.
+template <class W>
+__device__ void chain_prefetcher(const PmsArgs &a, W word, int w0, const volatile int *cur, const volatile int *done,
+                                 int *tmp) {
+    const int lane = threadIdx.x & 31;
+    int last = -2;
+    for (int round = 0; round < (1 << 20); round++) {
+        const int d = __shfl_sync(0xffffffffu, *done, 0);
+        if (d) break;
+        const int lj = __shfl_sync(0xffffffffu, *cur, 0);
+        if (lj == last || lj < 0) {
+            __nanosleep(100);
+            continue;
+        }
+        last = lj;
+        // the 32 highest set bits below the low, at most four steps of 128
+        // words down
+        tmp[lane] = -1;
+        __syncwarp();
+        const int pos = lj - w0;
+        const int wl = (pos - 1) >> 5;
+        const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
+        int got = 0;
+        for (int c0 = wl & ~3, st = 0; pos > 0 && c0 >= 0 && st < 4 && got < 32; c0 -= 128, st++) {
+            const int w = c0 - 4 * lane;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (w >= 0) v = *reinterpret_cast<const uint4 *>(word(w));
+            const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
+            const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
+            const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
+            const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
+            const int c = __popc(q0) + __popc(q1) + __popc(q2) + __popc(q3);
+            int incl = c;  // lane 0 holds the highest words: ranks run up the lanes
+            for (int o = 1; o < 32; o <<= 1) {
+                const int u = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += u;
+            }
+            int r = got + incl - c;
+            const uint32_t qs[4] = {q3, q2, q1, q0};
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                for (uint32_t x = qs[k]; x && r < 32; r++) {
+                    const int hb = 31 - __clz(x);
+                    x &= ~(1u << hb);
+                    tmp[r] = (w + 3 - k) * 32 + hb;
+                }
+            got += __shfl_sync(0xffffffffu, incl, 31);
+            __syncwarp();
+        }
+        const int my = tmp[lane];
+        __syncwarp();
+        if (my >= 0) {
+            const int4 hc = __ldcg(reinterpret_cast<const int4 *>(&a.rec[w0 + my]));
+            if (hc.x >= 0 && hc.y > 4 && (unsigned)hc.w != SEG4_NONE) {
+                const int *P = a.pool + 4ll * (unsigned)hc.w + SEG_HDR;
+                const int lines = min((4 * hc.y + 127) >> 7, 16);
+                for (int q = 0; q < lines; q++) prefetch_l2(P + 32 * q);
+            }
+        }
+    }
+}
+
+struct ChainResult {
+    int n, lj, lo;     // the column's length and low after the chain, its lowest row ever set
+    bool made, fell;   // it became the pivot of its low / a pivot row lay below the window
+};
+
+// The chain of additions into bitmap column j (tiers 3 and 4), run by the
+// whole CTA (1024 threads) once the column's rows are set in the window
+// [w0, ...) that `word` reaches: warps 0 .. 30 toggle the pivot's rows (one
+// each), warp 0 then counts the column, finds the next low (bits_below) and
+// reads that row's pivot record; two barriers of those 31 warps per
+// addition.  Warp 31 prefetches ahead of them (chain_prefetcher).  A pivot
+// row below the window undoes that addition's toggles and ends the chain
+// (`fell`): the caller hands the column to the merge path.  n, lj: the
+// column's length and low; lo: its lowest row.
+template <class W>
+__device__ ChainResult bitmap_chain(const PmsArgs &a, int j, int lj, int n, int lo, int w0, W word,
+                                    long long &adds, long long &slots) {
+    __shared__ int s_red[32], s_fb[32];
+    __shared__ int s_small[4];
+    __shared__ int s_lo;
+    __shared__ volatile int s_cur, s_done;  // the chain's low and its end, for the prefetching warp
+    __shared__ int s_ctmp[32];              // the prefetching warp's candidates
+    __shared__ __align__(16) int4 s_rec[2][2];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+    const int ntg = blockDim.x - 32;
+    int4 h, e;
+    if (tid == 0) {
+        rec_load_acq(&a.rec[lj], h, e);
+        s_rec[1][0] = h;
+        s_rec[1][1] = e;
+        s_lo = lo;
+        s_cur = lj;
+        s_done = 0;
+    }
+    __syncthreads();  // s_rec[1] is next written by the second addition
+    h = s_rec[1][0];
+    e = s_rec[1][1];
+    bool made = false, fell = false;
+    if (wid == nw - 1) {
+        chain_prefetcher(a, word, w0, &s_cur, &s_done, s_ctmp);
+    } else if (h.x >= 0 && h.x < j) {
+        for (int par = 0;; par ^= 1) {
+            const int np = h.y;
+            const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
+            int d = 0;
+            bool below = false;
+            for (int k = tid; k < np; k += ntg) {
+                const int row = P ? __ldcg(P + k) : rec_entry(e, k);
+                const int r = row - w0;
+                if (r < 0) {
+                    below = true;
+                    continue;
+                }
+                if (k == 0) s_lo = min(s_lo, row);  // only thread 0 writes it
+                const uint32_t bit = 1u << (r & 31);
+                d += (atomicXor(word(r >> 5), bit) & bit) ? -1 : 1;
+            }
+            d = __reduce_add_sync(0xffffffffu, d);
+            const bool fb = __any_sync(0xffffffffu, below);
+            if (lane == 0) {
+                s_red[wid] = d;
+                s_fb[wid] = fb;
+            }
+            bar_named(ntg);
+            if (wid == 0) {
+                const int tt = __reduce_add_sync(0xffffffffu, lane < nw - 1 ? s_red[lane] : 0);
+                const int f = __any_sync(0xffffffffu, lane < nw - 1 && s_fb[lane]);
+                const int nn = n + tt;
+                const int b = (!f && nn > 0) ? bits_below(word, lj - w0) : -1;
+                const int next = b >= 0 ? w0 + b : -1;
+                if (lane == 0) {
+                    if (next >= 0) {
+                        s_cur = next;  // for the prefetching warp
+                        int4 hh, ee;
+                        rec_load_acq(&a.rec[next], hh, ee);
+                        s_rec[par][0] = hh;
+                        s_rec[par][1] = ee;
+                    }
+                    s_small[0] = nn;
+                    s_small[1] = next;  // -1: zero column
+                    s_small[2] = f;     // a pivot row below the window
+                }
+            }
+            bar_named(ntg);
+            const int nn = s_small[0], next = s_small[1];
+            if (s_small[2]) {
+                // undo the toggles: the column is as before this addition
+                for (int k = tid; k < np; k += ntg) {
+                    const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
+                    if (r >= 0) atomicXor(word(r >> 5), 1u << (r & 31));
+                }
+                fell = true;
+                break;
+            }
+            slots += n + np + nn;
+            adds++;
+            n = nn;
+            if (next < 0) {
+                n = 0;
+                lj = -1;
+                break;
+            }
+            lj = next;
+            h = s_rec[par][0];
+            e = s_rec[par][1];
+            mark_clear<false>(a, lj, tid == 0);
+            if (h.z == j) {  // the beta check: row lj first appears in j
+                made = true;
+                break;
+            }
+            if (h.x < 0 || h.x >= j) break;
+        }
+    }
+    if (tid == 0) s_done = 1;
+    __syncthreads();  // every warp, the prefetcher included, past the chain (and any undo)
+    ChainResult res;
+    res.n = n;
+    res.lj = lj;
+    res.lo = s_lo;
+    res.made = made;
+    res.fell = fell;
+    // every thread took the chain warps' values: warp 31 ran no additions,
+    // so its n and lj come from the shared result below
+    __shared__ int s_out[2];
+    if (tid == 0) {
+        s_out[0] = n;
+        s_out[1] = (made ? 1 : 0) | (fell ? 2 : 0);
+        s_small[3] = lj;
+    }
+    __syncthreads();
+    res.n = s_out[0];
+    res.lj = s_small[3];
+    res.made = (s_out[1] & 1) != 0;
+    res.fell = (s_out[1] & 2) != 0;
+    __syncthreads();  // s_out and s_small are rewritten by the next column's chain
+    return res;
+}
+
 // Returns true when the column needs the merge path (its state written back
 // first).
 //
@@ -1493,101 +1737,114 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
     const int w0 = (long long)lj + 1 > nbits ? (int)(((long long)lj + 1 - nbits + 31) & ~31ll) : 0;
     if (n > 0 && T[0] < w0) return true;
     int t1 = n >= 2 ? T[n - 2] : -1;  // the set bit below the low
-    if (tid == 0) s_lo = n > 0 ? T[0] : lj;  // no set bit below it
+    const int lo0 = n > 0 ? T[0] : lj;  // no set bit below it
+    if (tid == 0) s_lo = lo0;
     for (int k = tid; k < n; k += blockDim.x) {
         const int r = T[k] - w0;
         atomicOr(bm + (r >> 5), 1u << (r & 31));
     }
     __syncthreads();
     bool made_pivot = false, fell_back = false;
-    const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-    const int ntg = blockDim.x - 32;  // toggling threads: every warp but the last
-    for (int par = 0;; par ^= 1) {
-        const int np = h.y;
-        const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
-        const int p2 = np >= 2 ? (P ? e.z : rec_entry(e, np - 2)) : -1;
-        const bool known = t1 != p2 || t1 < 0;
-        const int pnext = known ? max(t1, p2) : -1;  // -1 when known: T = P, the sum is zero
-        if (wid == nw - 1) {
-            if (lane == 0 && pnext >= 0) {
-                int4 hh, ee;
-                rec_load_acq(&a.rec[pnext], hh, ee);
-                s_rec[par][0] = hh;
-                s_rec[par][1] = ee;
-            }
-        } else {
-            int d = 0;
-            bool below = false;
-            for (int k = tid; k < np; k += ntg) {
-                const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
-                if (r < 0) {
-                    below = true;
-                    continue;
-                }
-                if (k == 0) s_lo = min(s_lo, r + w0);  // only thread 0 writes it
-                const uint32_t bit = 1u << (r & 31);
-                d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
-            }
-            d = __reduce_add_sync(0xffffffffu, d);
-            const bool fb = __any_sync(0xffffffffu, below);
-            if (lane == 0) {
-                s_red[wid] = d;
-                s_fb[wid] = fb;
-            }
-        }
+    if constexpr (SM) {
+        // the shared window: the chain with its prefetching warp
+        (void)t1;
+        const ChainResult ch = bitmap_chain(a, j, lj, n, lo0, w0, [&](int w) { return bm + w; }, adds, slots);
+        n = ch.n;
+        lj = ch.lj;
+        made_pivot = ch.made;
+        fell_back = ch.fell;
+        if (tid == 0) s_lo = ch.lo;
         __syncthreads();
-        if (wid == 0) {
-            const int t = __reduce_add_sync(0xffffffffu, lane < nw - 1 ? s_red[lane] : 0);
-            const int f = __any_sync(0xffffffffu, lane < nw - 1 && s_fb[lane]);
-            const int nn = n + t;
-            int next = -1, nb = -1;
-            if (!f && nn > 0) {
-                // lj's bit went with the pivot's top: the next low lies below it
-                next = known ? (pnext >= 0 ? pnext - w0 : -1) : bm_below<SM>(bm, lj - w0);
-                if (nn > 1 && next >= 0) nb = bm_below<SM>(bm, next);
-            }
-            if (lane == 0) {
-                if (!f && next >= 0 && !(known && w0 + next == pnext)) {
+    } else {
+        const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+        const int ntg = blockDim.x - 32;  // toggling threads: every warp but the last
+        for (int par = 0;; par ^= 1) {
+            const int np = h.y;
+            const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
+            const int p2 = np >= 2 ? (P ? e.z : rec_entry(e, np - 2)) : -1;
+            const bool known = t1 != p2 || t1 < 0;
+            const int pnext = known ? max(t1, p2) : -1;  // -1 when known: T = P, the sum is zero
+            if (wid == nw - 1) {
+                if (lane == 0 && pnext >= 0) {
                     int4 hh, ee;
-                    rec_load_acq(&a.rec[w0 + next], hh, ee);
+                    rec_load_acq(&a.rec[pnext], hh, ee);
                     s_rec[par][0] = hh;
                     s_rec[par][1] = ee;
                 }
-                s_small[0] = nn;
-                s_small[1] = next;  // -1: zero column (or, never, no bit left)
-                s_small[2] = nb;    // the set bit below it
-                s_small[3] = f;     // the pivot reaches below the window
-            }
-        }
-        __syncthreads();
-        const int nn = s_small[0], next = s_small[1], nb = s_small[2];
-        if (s_small[3]) {
-            // undo the toggles: the column is back to its state before this
-            // addition, which the merge path takes over
-            if (wid < nw - 1)
+            } else {
+                int d = 0;
+                bool below = false;
                 for (int k = tid; k < np; k += ntg) {
                     const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
-                    if (r >= 0) atomicXor(bm + (r >> 5), 1u << (r & 31));
+                    if (r < 0) {
+                        below = true;
+                        continue;
+                    }
+                    if (k == 0) s_lo = min(s_lo, r + w0);  // only thread 0 writes it
+                    const uint32_t bit = 1u << (r & 31);
+                    d += (atomicXor(bm + (r >> 5), bit) & bit) ? -1 : 1;
                 }
+                d = __reduce_add_sync(0xffffffffu, d);
+                const bool fb = __any_sync(0xffffffffu, below);
+                if (lane == 0) {
+                    s_red[wid] = d;
+                    s_fb[wid] = fb;
+                }
+            }
             __syncthreads();
-            fell_back = true;
-            break;
+            if (wid == 0) {
+                const int t = __reduce_add_sync(0xffffffffu, lane < nw - 1 ? s_red[lane] : 0);
+                const int f = __any_sync(0xffffffffu, lane < nw - 1 && s_fb[lane]);
+                const int nn = n + t;
+                int next = -1, nb = -1;
+                if (!f && nn > 0) {
+                    // lj's bit went with the pivot's top: the next low lies below it
+                    next = known ? (pnext >= 0 ? pnext - w0 : -1) : bm_below<SM>(bm, lj - w0);
+                    if (nn > 1 && next >= 0) nb = bm_below<SM>(bm, next);
+                }
+                if (lane == 0) {
+                    if (!f && next >= 0 && !(known && w0 + next == pnext)) {
+                        int4 hh, ee;
+                        rec_load_acq(&a.rec[w0 + next], hh, ee);
+                        s_rec[par][0] = hh;
+                        s_rec[par][1] = ee;
+                    }
+                    s_small[0] = nn;
+                    s_small[1] = next;  // -1: zero column (or, never, no bit left)
+                    s_small[2] = nb;    // the set bit below it
+                    s_small[3] = f;     // the pivot reaches below the window
+                }
+            }
+            __syncthreads();
+            const int nn = s_small[0], next = s_small[1], nb = s_small[2];
+            if (s_small[3]) {
+                // undo the toggles: the column is back to its state before this
+                // addition, which the merge path takes over
+                if (wid < nw - 1)
+                    for (int k = tid; k < np; k += ntg) {
+                        const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
+                        if (r >= 0) atomicXor(bm + (r >> 5), 1u << (r & 31));
+                    }
+                __syncthreads();
+                fell_back = true;
+                break;
+            }
+            slots += n + np + nn;
+            adds++;
+            n = nn;
+            if (next < 0) {
+                n = 0;
+                lj = -1;
+                break;
+            }
+            lj = w0 + next;
+            t1 = nb >= 0 ? w0 + nb : -1;
+            h = s_rec[par][0];
+            e = s_rec[par][1];
+            mark_clear<false>(a, lj, tid == 0);
+            if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
+            if (h.x < 0 || h.x >= j) break;
         }
-        slots += n + np + nn;
-        adds++;
-        n = nn;
-        if (next < 0) {
-            n = 0;
-            lj = -1;
-            break;
-        }
-        lj = w0 + next;
-        t1 = nb >= 0 ? w0 + nb : -1;
-        h = s_rec[par][0];
-        e = s_rec[par][1];
-        mark_clear<false>(a, lj, tid == 0);
-        if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
-        if (h.x < 0 || h.x >= j) break;
     }
     const int lo_row = s_lo;
     long long dst = sj;
@@ -1687,112 +1944,11 @@ constexpr int CL_ROWS = 32 * CL_WORDS;  // rows per CTA
 constexpr size_t CL_BYTES = sizeof(uint32_t) * CL_WORDS;
 constexpr int CL_BLOCK = 1024;
 
-// Named barrier among the first `count` threads of the CTA (id 1; 0 is
-// __syncthreads): the chain's warps meet without the prefetching warp.
-__device__ __forceinline__ void bar_named(int count) { asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory"); }
-
 // Word w of the cluster bitmap (slice w / CL_WORDS), through the CTA's own
 // shared memory when it holds that slice.
 __device__ __forceinline__ uint32_t *cl_word(const cg::cluster_group &cl, uint32_t *cbm, int w, int rank) {
     const int q = w / CL_WORDS;
     return (q == rank ? cbm : cl.map_shared_rank(cbm, q)) + (w - q * CL_WORDS);
-}
-
-// The highest set bit of the cluster bitmap strictly below window row `pos`,
-// -1 when there is none: a warp's search from the top, 128 words a step
-// through distributed shared memory.
-__device__ __forceinline__ int cl_below(const cg::cluster_group &cl, uint32_t *cbm, int pos, int rank) {
-    const int lane = threadIdx.x & 31;
-    if (pos <= 0) return -1;
-    const int wl = (pos - 1) >> 5;
-    const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
-    for (int c0 = wl & ~3; c0 >= 0; c0 -= 128) {
-        const int w = c0 - 4 * lane;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (w >= 0) v = *reinterpret_cast<const uint4 *>(cl_word(cl, cbm, w, rank));
-        const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
-        const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
-        const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
-        const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
-        const int hi = q3 ? (w + 3) * 32 + 31 - __clz(q3)
-                     : q2 ? (w + 2) * 32 + 31 - __clz(q2)
-                     : q1 ? (w + 1) * 32 + 31 - __clz(q1)
-                     : q0 ? w * 32 + 31 - __clz(q0) : -1;
-        const unsigned nz = __ballot_sync(0xffffffffu, hi >= 0);
-        if (nz) return __shfl_sync(0xffffffffu, hi, __ffs(nz) - 1);  // the lowest lane holds the highest words
-    }
-    return -1;
-}
-
-// The prefetching warp of a cluster chain.  In a large matrix the pivot
-// records and pivot rows a chain visits sit in HBM, not L2, and each
-// addition waits on the record of its low and then on the pivot's rows.
-// Most next lows of a long column are among its highest set bits below the
-// current low (84% on the anti-transpose of a Rips torus, 75% within the
-// highest 16), so this warp, outside the chain's barriers, follows the low
-// the chain publishes (`cur`): each round it takes the 32 highest set bits
-// below it (lane k the k-th, from a racy view of the bitmap: only what is
-// prefetched depends on it), reads their records (bringing them into L2)
-// and prefetches the rows of their pivots.  It stops when `done` is set, or
-// after a bounded number of rounds.
-__device__ void cl_prefetcher(const PmsArgs &a, const cg::cluster_group &cl, uint32_t *cbm, int w0, int rank,
-                              const volatile int *cur, const volatile int *done, int *tmp) {
-    const int lane = threadIdx.x & 31;
-    int last = -2;
-    for (int round = 0; round < (1 << 20); round++) {
-        const int d = __shfl_sync(0xffffffffu, *done, 0);
-        if (d) break;
-        const int lj = __shfl_sync(0xffffffffu, *cur, 0);
-        if (lj == last || lj < 0) {
-            __nanosleep(100);
-            continue;
-        }
-        last = lj;
-        // the 32 highest set bits below the low, at most four steps of 128
-        // words down
-        tmp[lane] = -1;
-        __syncwarp();
-        const int pos = lj - w0;
-        const int wl = (pos - 1) >> 5;
-        const uint32_t ml = 0xffffffffu >> (31 - ((pos - 1) & 31));
-        int got = 0;
-        for (int c0 = wl & ~3, st = 0; pos > 0 && c0 >= 0 && st < 4 && got < 32; c0 -= 128, st++) {
-            const int w = c0 - 4 * lane;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (w >= 0) v = *reinterpret_cast<const uint4 *>(cl_word(cl, cbm, w, rank));
-            const uint32_t q0 = w > wl ? 0u : w == wl ? v.x & ml : v.x;
-            const uint32_t q1 = w + 1 > wl ? 0u : w + 1 == wl ? v.y & ml : v.y;
-            const uint32_t q2 = w + 2 > wl ? 0u : w + 2 == wl ? v.z & ml : v.z;
-            const uint32_t q3 = w + 3 > wl ? 0u : w + 3 == wl ? v.w & ml : v.w;
-            const int c = __popc(q0) + __popc(q1) + __popc(q2) + __popc(q3);
-            int incl = c;  // lane 0 holds the highest words: ranks run up the lanes
-            for (int o = 1; o < 32; o <<= 1) {
-                const int u = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += u;
-            }
-            int r = got + incl - c;
-            const uint32_t qs[4] = {q3, q2, q1, q0};
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                for (uint32_t x = qs[k]; x && r < 32; r++) {
-                    const int hb = 31 - __clz(x);
-                    x &= ~(1u << hb);
-                    tmp[r] = (w + 3 - k) * 32 + hb;
-                }
-            got += __shfl_sync(0xffffffffu, incl, 31);
-            __syncwarp();
-        }
-        const int my = tmp[lane];
-        __syncwarp();
-        if (my >= 0) {
-            const int4 hc = __ldcg(reinterpret_cast<const int4 *>(&a.rec[w0 + my]));
-            if (hc.x >= 0 && hc.y > 4 && (unsigned)hc.w != SEG4_NONE) {
-                const int *P = a.pool + 4ll * (unsigned)hc.w + SEG_HDR;
-                const int lines = min((4 * hc.y + 127) >> 7, 16);
-                for (int q = 0; q < lines; q++) prefetch_l2(P + 32 * q);
-            }
-        }
-    }
 }
 
 struct ClState {  // the leader's decision on the next queued column, copied into every CTA
@@ -1818,13 +1974,7 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
     __shared__ ClState s_cs[2];      // per parity of the loop: written by the leader into every CTA
     __shared__ ClResult s_res[2];
     __shared__ int s_cnt[2][CL];     // (leader) set bits per slice
-    __shared__ int s_red[32], s_fb[32];
-    __shared__ int s_small[4];
-    __shared__ int s_lo;
-    __shared__ volatile int s_cur, s_done;   // the chain's low and its end, for the prefetching warp
-    __shared__ int s_ctmp[32];  // the prefetching warp's candidates
-    __shared__ __align__(16) int4 s_rec[2][2];
-    __shared__ long long s_off;
+    __shared__ int s_red[32];
     __shared__ int scratch[2 * (CL_BLOCK / 32)];
     const int32_t *in_list = (tier & 1) ? a.widelist : a.worklist;
     for (int q = 4 * tid; q < CL_WORDS; q += 4 * CL_BLOCK)
@@ -1879,113 +2029,20 @@ __global__ void __cluster_dims__(CL, 1, 1) __launch_bounds__(CL_BLOCK) k_p2_clus
         }
         cl.sync();
         if (rank == c.chain) {
-            // the chain, on the CTA that holds the low's slice (where its
-            // searches and most of its toggles fall: the low of a long chain
-            // stays within one slice): warps 0 .. nw-2 toggle the pivot's
-            // bits in whichever slice holds them (each thread one row), warp
-            // 0 counts, searches for the next low and reads its record; two
-            // barriers of those warps per addition.  Warp nw-1 prefetches
-            // ahead of them (cl_prefetcher), outside their barriers.
-            int lj = c.lj, n = c.n;
-            int4 h, e;
-            if (tid == 0) {
-                rec_load_acq(&a.rec[lj], h, e);
-                s_rec[1][0] = h;
-                s_rec[1][1] = e;
-                s_lo = c.lo;
-                s_cur = lj;
-                s_done = 0;
-            }
-            __syncthreads();  // s_rec[1] is next written by the second addition
-            h = s_rec[1][0];
-            e = s_rec[1][1];
-            bool made = false, fell = false;
-            const int ntg = CL_BLOCK - 32;
-            if (wid == nw - 1) {
-                cl_prefetcher(a, cl, cbm, w0, rank, &s_cur, &s_done, s_ctmp);
-            } else if (h.x >= 0 && h.x < j) {
-                for (int par = 0;; par ^= 1) {
-                    const int np = h.y;
-                    const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
-                    int d = 0;
-                    bool below = false;
-                    for (int k = tid; k < np; k += ntg) {
-                        const int row = P ? __ldcg(P + k) : rec_entry(e, k);
-                        const int r = row - w0;
-                        if (r < 0) {
-                            below = true;
-                            continue;
-                        }
-                        if (k == 0) s_lo = min(s_lo, row);  // only thread 0 writes it
-                        const uint32_t bit = 1u << (r & 31);
-                        d += (atomicXor(cl_word(cl, cbm, r >> 5, rank), bit) & bit) ? -1 : 1;
-                    }
-                    d = __reduce_add_sync(0xffffffffu, d);
-                    const bool fb = __any_sync(0xffffffffu, below);
-                    if (lane == 0) {
-                        s_red[wid] = d;
-                        s_fb[wid] = fb;
-                    }
-                    bar_named(ntg);
-                    if (wid == 0) {
-                        const int tt = __reduce_add_sync(0xffffffffu, lane < nw - 1 ? s_red[lane] : 0);
-                        const int f = __any_sync(0xffffffffu, lane < nw - 1 && s_fb[lane]);
-                        const int nn = n + tt;
-                        const int b = (!f && nn > 0) ? cl_below(cl, cbm, lj - w0, rank) : -1;
-                        const int next = b >= 0 ? w0 + b : -1;
-                        if (lane == 0) {
-                            if (next >= 0) {
-                                s_cur = next;  // for the prefetching warp
-                                int4 hh, ee;
-                                rec_load_acq(&a.rec[next], hh, ee);
-                                s_rec[par][0] = hh;
-                                s_rec[par][1] = ee;
-                            }
-                            s_small[0] = nn;
-                            s_small[1] = next;  // -1: zero column
-                            s_small[2] = f;     // a pivot row below the window
-                        }
-                    }
-                    bar_named(ntg);
-                    const int nn = s_small[0], next = s_small[1];
-                    if (s_small[2]) {
-                        // undo the toggles: the column is as before this
-                        // addition; the merge path takes over after the write-back
-                        for (int k = tid; k < np; k += ntg) {
-                            const int r = (P ? __ldcg(P + k) : rec_entry(e, k)) - w0;
-                            if (r < 0) continue;
-                            atomicXor(cl_word(cl, cbm, r >> 5, rank), 1u << (r & 31));
-                        }
-                        fell = true;
-                        break;
-                    }
-                    slots += n + np + nn;
-                    adds++;
-                    n = nn;
-                    if (next < 0) {
-                        n = 0;
-                        lj = -1;
-                        break;
-                    }
-                    lj = next;
-                    h = s_rec[par][0];
-                    e = s_rec[par][1];
-                    mark_clear<false>(a, lj, tid == 0);
-                    if (h.z == j) {  // the beta check: row lj first appears in j
-                        made = true;
-                        break;
-                    }
-                    if (h.x < 0 || h.x >= j) break;
-                }
-            }
-            if (tid == 0) s_done = 1;
-            __syncthreads();  // every warp, the prefetcher included, past the chain (and any undo)
+            // the chain, on the CTA that holds the low's slice: its searches
+            // and most of its toggles fall there (the low of a long chain
+            // stays within one slice); the pivot rows elsewhere are toggled
+            // through distributed shared memory
+            const ChainResult ch = bitmap_chain(
+                a, j, c.lj, c.n, c.lo, w0, [&](int w) { return cl_word(cl, cbm, w, rank); }, adds, slots);
+            const int n = ch.n, lj = ch.lj;
+            const bool made = ch.made, fell = ch.fell;
             // the result, and the column's new segment when it outgrew its own
             if (tid == 0) {
                 ClResult r{};
                 r.n = n;
                 r.lj = lj;
-                r.lo = s_lo;
+                r.lo = ch.lo;
                 r.made = made;
                 r.fell = fell;
                 r.stored = 1;
