@@ -519,6 +519,104 @@ static oph_context *default_context(int device, int *rc) {
     return g_ctx[device];
 }
 
+}  // extern "C"
+
+// The reference's per-iteration trackers of a standard or twist reduction
+// (track_host, tracker.cu:136-172, after every column: standard.cu:44-49,
+// twist.cu:68-71; track on the device for the parallel forms,
+// standard_parallel.cu:40-43, twist_parallel.cu:75-78), replayed on the
+// host from the walk: the state after iteration k is every visited column at
+// its final low, twist's cleared rows at -1, every other column at its
+// initial low.  classes and ess follow each form's own updates: the CPU
+// forms classify the visited column (a zero column as 1) and clear ess at
+// the pair (ess_hat of the intermediate lows clears rows that are already
+// some earlier pivot's low); the parallel forms re-apply update_classes
+// (pivot pairs only) and ess_hat (every current low, and the pairs) after
+// each column, kernels.cu:93-124.  Out: 4 sums per entry, as Tracking::acc.
+static void replay_seq_trackers(const SeqTracking &tk, int algo, const std::vector<int32_t> &low_fin,
+                                const std::vector<int32_t> &low_true, const std::vector<int32_t> &ess_true,
+                                std::vector<double> &out) {
+    const int64_t m = (int64_t)low_fin.size();
+    const bool twist = algo == OPH_ALGO_TWIST || algo == OPH_ALGO_TWIST_PARALLEL;
+    const bool par = algo == OPH_ALGO_STANDARD_PARALLEL || algo == OPH_ALGO_TWIST_PARALLEL;
+    std::vector<int32_t> low(tk.low0);
+    std::vector<int8_t> cls(m, 0), ess(m, 1);
+    std::vector<int64_t> hist(m + 2, 0);  // counts of |low - low_true| (both in [-1, m))
+    double l1 = 0;
+    int64_t mx = 0, uncl = m, esum = m;
+    auto diff = [&](int64_t c) { return (int64_t)std::llabs((long long)low[c] - (long long)low_true[c]); };
+    for (int64_t c = 0; c < m; c++) {
+        const int64_t d = diff(c);
+        hist[d]++;
+        l1 += (double)d;
+        mx = std::max(mx, d);
+    }
+    auto set_low = [&](int64_t c, int32_t v) {
+        const int64_t d0 = diff(c);
+        hist[d0]--;
+        l1 -= (double)d0;
+        low[c] = v;
+        const int64_t d1 = diff(c);
+        hist[d1]++;
+        l1 += (double)d1;
+        if (d1 > mx) mx = d1;
+        while (mx > 0 && hist[mx] == 0) mx--;
+    };
+    auto set_cls = [&](int64_t c, int8_t v) {
+        if (cls[c] == 0 && v != 0) uncl--;
+        cls[c] = v;
+    };
+    auto clear_ess = [&](int64_t c) {
+        if (ess[c]) {
+            ess[c] = 0;
+            esum--;
+        }
+    };
+    auto entry = [&](int64_t k) {
+        out[4 * k] = l1;
+        out[4 * k + 1] = (double)mx;
+        out[4 * k + 2] = (double)uncl;
+        out[4 * k + 3] = (double)esum;
+    };
+    out.assign(4 * (size_t)tk.iters, 0.0);
+    entry(0);
+    int64_t k = 1;
+    auto visit = [&](int64_t j) {
+        const int32_t l = low_fin[j];
+        if (low[j] != l) set_low(j, l);
+        if (twist && l >= 0 && low[l] != -1) set_low(l, -1);
+        if (l >= 0) {
+            set_cls(j, -1);
+            set_cls(l, 1);
+            clear_ess(j);
+            clear_ess(l);
+        } else if (!par) {
+            set_cls(j, 1);
+        }
+        if (par) {
+            if (k == 1) {
+                for (int64_t c = 0; c < m; c++)
+                    if (low[c] >= 0) clear_ess(low[c]);
+            } else if (l >= 0) {
+                clear_ess(l);
+            }
+        }
+        if (k < tk.iters) entry(k);
+        k++;
+    };
+    if (twist) {
+        int maxd = -1;
+        for (int64_t c = 0; c < m; c++) maxd = std::max(maxd, (int)tk.dim[c]);
+        for (int d = maxd; d >= 1; d--)
+            for (int64_t j = 0; j < m; j++)
+                if (tk.dim[j] == d) visit(j);
+    } else {
+        for (int64_t j = 0; j < m; j++) visit(j);
+    }
+}
+
+extern "C" {
+
 __attribute__((visibility("default"))) int oph_openph(const char *algstr, const int *h_rows_in, const int *h_cols_in,
                                                       int m, int col_width, const int *h_low_true, int nnz, int *h_low,
                                                       int *h_ess, float *err_linf, float *err_lone, float *err_redu,
@@ -577,8 +675,8 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
         k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 0);
         k_ess_true<<<grid_for(ctx, m), 256, 0, s>>>(lt0, m, esst, 1);
     }
-    // pms records an entry per sweep (pms.cu:16,106); the other algorithms
-    // record the initial and the final state
+    // pms records an entry per sweep (pms.cu:16,106); standard and twist an
+    // entry per column (below); the row forms the initial and final state
     Tracking tr;
     const bool per_sweep = track && m > 0 && algo == OPH_ALGO_PMS;
     if (per_sweep) {
@@ -594,6 +692,13 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
         d_acc = (double *)ctx_alloc(ctx, S_TRACK, sizeof(double) * (16 + 4 * 2));
         if (!d_acc) return OPH_ERR_OOM;
     }
+    // standard and twist (both forms) record an entry per column, replayed
+    // on the host after the walk; the row forms the initial and final state
+    SeqTracking stk;
+    const bool per_col = track && m > 0 &&
+                         (algo == OPH_ALGO_STANDARD || algo == OPH_ALGO_STANDARD_PARALLEL ||
+                          algo == OPH_ALGO_TWIST || algo == OPH_ALGO_TWIST_PARALLEL);
+    if (per_col) ctx->seq_track = &stk;
     Outputs o;
     o.low = d_out;
     o.one_based = 1;
@@ -601,6 +706,7 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
     oph_info info{};
     rc = reduce_core(ctx, algo, w, o, &info);
     ctx->track = nullptr;
+    ctx->seq_track = nullptr;
     if (rc) return rc;
     if (m > 0) {
         OPH_CUDA_TRY(cudaMemcpyAsync(h_low, d_out, sizeof(int) * m, cudaMemcpyDeviceToHost, s));
@@ -621,12 +727,25 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
                                          cudaMemcpyDeviceToHost, s));
         }
     }
+    std::vector<int32_t> h_low0, h_lt, h_et;
+    if (per_col && stk.iters > 0) {
+        h_low0.resize(m);
+        h_lt.resize(m);
+        h_et.resize(m);
+        OPH_CUDA_TRY(cudaMemcpyAsync(h_low0.data(), w.low, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+        OPH_CUDA_TRY(cudaMemcpyAsync(h_lt.data(), lt0, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+        OPH_CUDA_TRY(cudaMemcpyAsync(h_et.data(), esst, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+    }
     OPH_CUDA_TRY(cudaStreamSynchronize(s));
     if (num_iters) *num_iters = it;
     const int last = it - 1 < m ? it - 1 : m;
+    const bool replayed = per_col && stk.iters == it && (int64_t)stk.ns.size() == it;
+    if (replayed) replay_seq_trackers(stk, algo, h_low0, h_lt, h_et, entries);
     if (time_track && m >= 1) {
         time_track[0] = 0.0f;
-        if (per_sweep) {
+        if (replayed) {
+            for (int k = 1; k <= last; k++) time_track[k] = (float)((stk.ns[k] - stk.ns[k - 1]) * 1e-6);
+        } else if (per_sweep) {
             for (int k = 1; k < last && k - 1 < (int)tr.sweep_ms.size(); k++) time_track[k] = tr.sweep_ms[k - 1];
             time_track[last] = (int)tr.sweep_ms.size() >= last ? tr.sweep_ms[last - 1] : info.device_ms;
         } else {
@@ -643,11 +762,17 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
             if (err_redu) err_redu[k] = (float)(unclassified / (double)m);
             if (err_ess) err_ess[k] = ess_hat == esst_sum ? 1.0f : (float)(esst_sum / ess_hat);
         };
-        if (per_sweep)
-            for (int k = 0; k < last && k < tr.slots; k++)
+        if (replayed) {
+            // every entry, the last included, as the algorithm leaves it
+            for (int k = 0; k <= last; k++)
                 put(k, entries[4 * k], entries[4 * k + 1], entries[4 * k + 2], entries[4 * k + 3]);
-        // the last entry: the final lows, every column classified
-        put(last, acc[0], acc[1], 0.0, acc[2]);
+        } else {
+            if (per_sweep)
+                for (int k = 0; k < last && k < tr.slots; k++)
+                    put(k, entries[4 * k], entries[4 * k + 1], entries[4 * k + 2], entries[4 * k + 3]);
+            // the last entry: the final lows, every column classified
+            put(last, acc[0], acc[1], 0.0, acc[2]);
+        }
     }
     return OPH_OK;
 }

@@ -65,6 +65,7 @@ struct DevStatus {
     int reps;                      // repeated lows seen by the last Phase I
     int resume_dim;                // sequential walkers: where to resume after a regrow
     long long resume_pos;          //   (column or row index; -1 = finished)
+    long long resume_iter;         //   and the iteration count reached (trackers)
     int max_dim;                   // largest nnz(col) - 1 seen by the set-up
     int pad;
     int ucount[2];                     // compacted Phase I: list sizes (ping-pong)

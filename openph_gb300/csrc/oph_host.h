@@ -123,6 +123,20 @@ struct Tracking {
     std::vector<float> sweep_ms;        // device time of each sweep that ran
 };
 
+// Per-iteration progress of the standard and twist walks (the reference's
+// track_host after every column, standard.cu:44-49, twist.cu:68-71).  In
+// those algorithms a column is reduced completely at its one visit, so the
+// state after iteration k follows from the visit order, the initial lows and
+// the final lows (twist also clears the low of each new pivot's row); the
+// walker only stamps the end of every iteration (globaltimer, ns), and the
+// host replays the rest.
+struct SeqTracking {
+    std::vector<int32_t> low0;  // the lows before the walk
+    std::vector<int8_t> dim;    // nnz - 1 per column (twist's visit order)
+    std::vector<long long> ns;  // end of iteration k (k = 0: the walk's start)
+    long long iters = 0;        // entries: 1 + iterations
+};
+
 struct Context {
     int device = 0;
     int sm_count = 0;
@@ -143,6 +157,7 @@ struct Context {
     int tier0 = 0;                  // Phase II tier-0 candidate (autotuned)
     int dual = OPH_DUAL_AUTO;       // which matrix pms reduces
     Tracking *track = nullptr;      // per-sweep trackers for the current reduction
+    SeqTracking *seq_track = nullptr;  // per-iteration trackers of a standard / twist walk
     // two pms sweeps (the list ping-pong's two parities) captured as one CUDA
     // graph and replayed instead of 2 x 11 launches; sweep_key holds the
     // launch arguments it was captured with
@@ -160,7 +175,7 @@ struct Context {
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_IASC, S_IBUCKET, S_IOPEN, S_RANGES, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_IASC, S_IBUCKET, S_IOPEN, S_RANGES, S_SEQNS, S_NSLOTS
 };
 
 }  // namespace oph

@@ -44,7 +44,15 @@ struct SeqArgs {
     int max_dim;
     int twist;         // standard (0) or twist (1)
     int row_quirk;     // row: keep the reference CPU form's running ess estimate
+    long long *it_ns;  // standard / twist with trackers: end of every iteration (globaltimer), or nullptr
+    long long it_base; //   the iteration this launch starts at (1, or where an interrupted walk stopped)
 };
+
+__device__ __forceinline__ long long global_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Chain of additions into column j by one warp, `next(low)` giving the column
 // to add next (or -1 to stop).  The column stays in shared memory (sA/sB/sC,
@@ -140,6 +148,12 @@ __global__ void __launch_bounds__(32) k_seq_walk(SeqArgs a) {
     auto tile = cg::tiled_partition<32>(cg::this_thread_block());
     const int lane = tile.thread_rank();
     long long adds = 0, slots = 0;
+    // iterations (the reference's, one per visited column) and their end
+    // times, when trackers are kept: columns retired together in a window
+    // share its time evenly
+    long long it = a.it_base;
+    long long tprev = global_ns();
+    if (a.it_ns && it == 1 && lane == 0) a.it_ns[0] = tprev;
     const int d_end = a.twist ? 1 : a.start_dim;
     for (int d = a.start_dim; d >= d_end; d--) {
         long long j0 = (d == a.start_dim) ? a.start_pos : 0;
@@ -163,6 +177,16 @@ __global__ void __launch_bounds__(32) k_seq_walk(SeqArgs a) {
                 a.arglow[lj] = (int)j;
                 if (a.twist) a.low[lj] = -1;
             }
+            {
+                const unsigned retired = tile.ballot(in) & (fs == 32 ? 0xffffffffu : (1u << fs) - 1u);
+                const int cnt = __popc(retired);
+                if (a.it_ns && lane == 0 && cnt) {
+                    const long long t = global_ns();
+                    for (int q = 0; q < cnt; q++) a.it_ns[it + q] = tprev + (t - tprev) * (q + 1) / cnt;
+                    tprev = t;
+                }
+                it += cnt;
+            }
             tile.sync();
             if (fs == 32) { j0 += 32; continue; }
             const long long jj = j0 + fs;
@@ -171,13 +195,15 @@ __global__ void __launch_bounds__(32) k_seq_walk(SeqArgs a) {
             auto next = [&](int l) { return l >= 0 ? a.arglow[l] : -1; };
             const int nl = chain(tile, a, (int)jj, sA, sB, sC, SEQ_CAP, next, adds, slots);
             if (nl == -2) {
-                if (lane == 0) { a.st->resume_dim = d; a.st->resume_pos = jj; }
+                if (lane == 0) { a.st->resume_dim = d; a.st->resume_pos = jj; a.st->resume_iter = it; }
                 goto out;
             }
             if (nl >= 0 && lane == 0) {
                 a.arglow[nl] = (int)jj;
                 if (a.twist) a.low[nl] = -1;
             }
+            if (a.it_ns && lane == 0) a.it_ns[it] = tprev = global_ns();
+            it++;
             tile.sync();
             j0 = jj + 1;
         }
@@ -338,6 +364,23 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
         a.start_dim = a.twist ? maxdim : 0;
         a.start_pos = 0;
         if (a.twist && maxdim < 1) a.start_dim = 0;  // nothing to reduce: the loop below runs no dimension
+        // the reference counts one iteration per column visited
+        // (twist.cu:36-86 visits the columns of dimension >= 1)
+        if (a.twist) iters = 1 + (long long)hstats[1];
+        SeqTracking *tk = ctx->seq_track;
+        a.it_base = 1;
+        if (tk) {
+            // the state the host replays from, and a stamp per iteration
+            tk->iters = iters;
+            tk->low0.resize(m);
+            tk->dim.resize(m);
+            a.it_ns = (long long *)ctx_alloc(ctx, S_SEQNS, sizeof(long long) * (size_t)(iters + 1));
+            if (!a.it_ns) return OPH_ERR_OOM;
+            OPH_CUDA_TRY(cudaMemsetAsync(a.it_ns, 0, sizeof(long long) * (size_t)(iters + 1), s));
+            OPH_CUDA_TRY(cudaMemcpyAsync(tk->low0.data(), w.low, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+            OPH_CUDA_TRY(cudaMemcpyAsync(tk->dim.data(), w.dim, (size_t)m, cudaMemcpyDeviceToHost, s));
+            OPH_CUDA_TRY(cudaStreamSynchronize(s));
+        }
         static bool attr = false;
         const size_t smem = 3 * SEQ_CAP * sizeof(int);
         if (!attr) {
@@ -357,12 +400,19 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
                 a.pool = w.pool;
                 a.start_dim = ctx->h_status->resume_dim;
                 a.start_pos = ctx->h_status->resume_pos;
+                a.it_base = ctx->h_status->resume_iter;
                 regrows++;
             }
         }
-        // the reference counts one iteration per column visited
-        // (twist.cu:36-86 visits the columns of dimension >= 1)
-        if (a.twist) iters = 1 + (long long)hstats[1];
+        if (tk) {
+            tk->ns.resize(iters);
+            if (a.twist && maxdim < 1) {
+                std::fill(tk->ns.begin(), tk->ns.end(), 0ll);
+            } else {
+                OPH_CUDA_TRY(cudaMemcpyAsync(tk->ns.data(), a.it_ns, sizeof(long long) * iters, cudaMemcpyDeviceToHost, s));
+                OPH_CUDA_TRY(cudaStreamSynchronize(s));
+            }
+        }
     } else {
         a.bhead = (int32_t *)ctx_alloc(ctx, S_TMP, sizeof(int32_t) * (3 * m + 1));
         if (!a.bhead) return OPH_ERR_OOM;

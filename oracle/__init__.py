@@ -214,3 +214,105 @@ def ref_run(bm, alg: str = "twist", col_width: int = 10, timeout: float = 600.0)
         iters = int(np.frombuffer(raw, np.int32, 1, 8 * m)[0])
         secs = float(np.frombuffer(raw, np.float64, 1, 8 * m + 4)[0])
         return low, ess, iters, secs
+
+
+def tracked(bm, algo: str, low_true):
+    """The reference's per-iteration progress trackers of standard, twist
+    and their parallel forms, restated step by step in Python for small
+    matrices (O(m) work per iteration, as the reference's own tracker).
+
+    The reduction follows reduce_col_host (algorithms/kernels_host.cu:62-75;
+    the device reduce_col, algorithms/kernels.cu:62-77, is the same without
+    the essential-estimate step) column by column in the algorithm's order
+    (standard.cu:17-53; twist.cu:36-86 with twist_step_host, twist.cu:1-8,
+    dimensions by nnz - 1 from the top, columns in order within one);
+    classes and ess are updated as the CPU forms do after each column
+    (standard.cu:26-37, twist.cu:50-64) or, for the parallel forms, by
+    update_classes and ess_hat over every column (kernels.cu:93-124).  After
+    each column the four sums of track_host (tracker.cu:136-172) are taken
+    with float32 accumulation, and normalised as openph.cu:184-193.
+
+    ``low_true`` is 0-based (-1 = none).  Returns (err_linf, err_lone,
+    err_redu, err_ess) as float32 arrays of num_iters entries, num_iters, and
+    the final 0-based low.
+    """
+    par = algo.endswith("_parallel")
+    twist = algo.startswith("twist")
+    m = bm.m
+    cols = [set(bm.rows[bm.colptr[j]:bm.colptr[j + 1]].tolist()) for j in range(m)]
+    low = [max(c) if c else -1 for c in cols]
+    arglow = [-1] * m
+    classes = [0] * m
+    ess = [1] * m
+    lt = np.asarray(low_true, np.int64)
+    ess_true = np.ones(m, np.int64)
+    for j in range(m):
+        if lt[j] > -1:
+            ess_true[j] = 0
+            ess_true[lt[j]] = 0
+    f32 = np.float32
+    norm1 = f32(0)
+    norminf = f32(0)
+    for v in (lt + 1):  # the 1-based low_true's norms (openph.cu:106-110)
+        norm1 = f32(norm1 + f32(abs(v)))
+        norminf = max(norminf, f32(abs(v)))
+    num_ess_true = f32(0)
+    for v in ess_true:
+        num_ess_true = f32(num_ess_true + f32(v))
+    out = []
+
+    def track():
+        s, mx, red, eh = f32(0), f32(0), f32(0), f32(0)
+        for i in range(m):
+            d = f32(abs(low[i] - int(lt[i])))
+            s = f32(s + d)
+            mx = max(mx, d)
+            red = f32(red + f32(1 if classes[i] == 0 else 0))
+            eh = f32(eh + f32(ess[i]))
+        out.append((mx, s, f32(red / f32(m)), f32(1) if eh == num_ess_true else f32(num_ess_true / eh)))
+
+    track()
+    if twist:
+        dims = [len(c) - 1 for c in cols]
+        order = [j for d in range(max(dims, default=-1), 0, -1) for j in range(m) if dims[j] == d]
+    else:
+        order = list(range(m))
+    for j in order:
+        lj = low[j]
+        while lj > -1 and arglow[lj] != -1:
+            if not par:
+                ess[lj] = 0
+            cols[j] ^= cols[arglow[lj]]
+            low[j] = max(cols[j]) if cols[j] else -1
+            lj = low[j]
+        if lj > -1:
+            arglow[lj] = j
+        if twist and low[j] > -1:
+            low[low[j]] = -1
+        if not par:
+            if low[j] > -1:
+                classes[j] = -1
+                classes[low[j]] = 1
+                ess[j] = 0
+                ess[low[j]] = 0
+            else:
+                classes[j] = 1
+        else:
+            for t in range(m):
+                if arglow[t] > -1:
+                    classes[arglow[t]] = -1
+                    classes[t] = 1
+            for t in range(m):
+                if low[t] > -1:
+                    ess[low[t]] = 0
+                if arglow[t] > -1:
+                    ess[arglow[t]] = 0
+                    ess[t] = 0
+        track()
+    n = len(out)
+    with np.errstate(divide="ignore", invalid="ignore"):  # an empty low_true has norm 0, as in the reference
+        linf = np.array([f32(o[0] / norminf) for o in out], np.float32)
+        lone = np.array([f32(o[1] / norm1) for o in out], np.float32)
+    redu = np.array([o[2] for o in out], np.float32)
+    eerr = np.array([o[3] for o in out], np.float32)
+    return linf, lone, redu, eerr, n, np.array(low, np.int32)
