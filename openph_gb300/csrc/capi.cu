@@ -7,6 +7,7 @@
 // ~17 cudaMalloc/cudaFree pairs per call, every call runs on the context's
 // own stream, and nothing uses global __device__ symbols, so distinct
 // contexts are independent.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -521,37 +522,31 @@ static oph_context *default_context(int device, int *rc) {
 
 }  // extern "C"
 
-// The reference's per-iteration trackers of a standard or twist reduction
-// (track_host, tracker.cu:136-172, after every column: standard.cu:44-49,
-// twist.cu:68-71; track on the device for the parallel forms,
-// standard_parallel.cu:40-43, twist_parallel.cu:75-78), replayed on the
-// host from the walk: the state after iteration k is every visited column at
-// its final low, twist's cleared rows at -1, every other column at its
-// initial low.  classes and ess follow each form's own updates: the CPU
-// forms classify the visited column (a zero column as 1) and clear ess at
-// the pair (ess_hat of the intermediate lows clears rows that are already
-// some earlier pivot's low); the parallel forms re-apply update_classes
-// (pivot pairs only) and ess_hat (every current low, and the pairs) after
-// each column, kernels.cu:93-124.  Out: 4 sums per entry, as Tracking::acc.
-static void replay_seq_trackers(const SeqTracking &tk, int algo, const std::vector<int32_t> &low_fin,
-                                const std::vector<int32_t> &low_true, const std::vector<int32_t> &ess_true,
-                                std::vector<double> &out) {
-    const int64_t m = (int64_t)low_fin.size();
-    const bool twist = algo == OPH_ALGO_TWIST || algo == OPH_ALGO_TWIST_PARALLEL;
-    const bool par = algo == OPH_ALGO_STANDARD_PARALLEL || algo == OPH_ALGO_TWIST_PARALLEL;
-    std::vector<int32_t> low(tk.low0);
-    std::vector<int8_t> cls(m, 0), ess(m, 1);
-    std::vector<int64_t> hist(m + 2, 0);  // counts of |low - low_true| (both in [-1, m))
+// The state behind the reference's tracker sums (track_host,
+// tracker.cu:136-172): the lows against low_true (sum and maximum of the
+// differences, the maximum through a count of every difference), the
+// unclassified columns, the essential estimate; changed one entry at a time.
+struct TrackState {
+    const std::vector<int32_t> &lt;
+    std::vector<int32_t> low;
+    std::vector<int8_t> cls, ess;
+    std::vector<int64_t> hist;
     double l1 = 0;
-    int64_t mx = 0, uncl = m, esum = m;
-    auto diff = [&](int64_t c) { return (int64_t)std::llabs((long long)low[c] - (long long)low_true[c]); };
-    for (int64_t c = 0; c < m; c++) {
-        const int64_t d = diff(c);
-        hist[d]++;
-        l1 += (double)d;
-        mx = std::max(mx, d);
+    int64_t mx = 0, uncl = 0, esum = 0;
+    TrackState(const std::vector<int32_t> &low0, const std::vector<int32_t> &low_true)
+        : lt(low_true), low(low0), cls(low0.size(), 0), ess(low0.size(), 1), hist(low0.size() + 2, 0) {
+        const int64_t m = (int64_t)low.size();
+        uncl = esum = m;
+        for (int64_t c = 0; c < m; c++) {
+            const int64_t d = diff(c);
+            hist[d]++;
+            l1 += (double)d;
+            mx = std::max(mx, d);
+        }
     }
-    auto set_low = [&](int64_t c, int32_t v) {
+    int64_t diff(int64_t c) const { return (int64_t)std::llabs((long long)low[c] - (long long)lt[c]); }
+    void set_low(int64_t c, int32_t v) {
+        if (low[c] == v) return;
         const int64_t d0 = diff(c);
         hist[d0]--;
         l1 -= (double)d0;
@@ -561,47 +556,67 @@ static void replay_seq_trackers(const SeqTracking &tk, int algo, const std::vect
         l1 += (double)d1;
         if (d1 > mx) mx = d1;
         while (mx > 0 && hist[mx] == 0) mx--;
-    };
-    auto set_cls = [&](int64_t c, int8_t v) {
+    }
+    void set_cls(int64_t c, int8_t v) {
         if (cls[c] == 0 && v != 0) uncl--;
         cls[c] = v;
-    };
-    auto clear_ess = [&](int64_t c) {
+    }
+    void clear_ess(int64_t c) {
         if (ess[c]) {
             ess[c] = 0;
             esum--;
         }
-    };
-    auto entry = [&](int64_t k) {
+    }
+    void entry(std::vector<double> &out, int64_t k) const {
         out[4 * k] = l1;
         out[4 * k + 1] = (double)mx;
         out[4 * k + 2] = (double)uncl;
         out[4 * k + 3] = (double)esum;
-    };
+    }
+};
+
+// The reference's per-iteration trackers of a standard or twist reduction
+// (after every column: standard.cu:44-49, twist.cu:68-71; on the device for
+// the parallel forms, standard_parallel.cu:40-43, twist_parallel.cu:75-78),
+// replayed on the host from the walk: the state after iteration k is every
+// visited column at its final low, twist's cleared rows at -1, every other
+// column at its initial low.  classes and ess follow each form's own
+// updates: the CPU forms classify the visited column (a zero column as 1)
+// and clear ess at the pair (reduce_col_host's clearing of the intermediate
+// lows only clears rows that are already some earlier pivot's low); the
+// parallel forms re-apply update_classes (pivot pairs only) and ess_hat
+// (every current low, and the pairs) after each column, kernels.cu:93-124.
+// Out: 4 sums per entry, as Tracking::acc.
+static void replay_seq_trackers(const SeqTracking &tk, int algo, const std::vector<int32_t> &low_fin,
+                                const std::vector<int32_t> &low_true, std::vector<double> &out) {
+    const int64_t m = (int64_t)low_fin.size();
+    const bool twist = algo == OPH_ALGO_TWIST || algo == OPH_ALGO_TWIST_PARALLEL;
+    const bool par = algo == OPH_ALGO_STANDARD_PARALLEL || algo == OPH_ALGO_TWIST_PARALLEL;
+    TrackState st(tk.low0, low_true);
     out.assign(4 * (size_t)tk.iters, 0.0);
-    entry(0);
+    st.entry(out, 0);
     int64_t k = 1;
     auto visit = [&](int64_t j) {
         const int32_t l = low_fin[j];
-        if (low[j] != l) set_low(j, l);
-        if (twist && l >= 0 && low[l] != -1) set_low(l, -1);
+        st.set_low(j, l);
+        if (twist && l >= 0) st.set_low(l, -1);
         if (l >= 0) {
-            set_cls(j, -1);
-            set_cls(l, 1);
-            clear_ess(j);
-            clear_ess(l);
+            st.set_cls(j, -1);
+            st.set_cls(l, 1);
+            st.clear_ess(j);
+            st.clear_ess(l);
         } else if (!par) {
-            set_cls(j, 1);
+            st.set_cls(j, 1);
         }
         if (par) {
             if (k == 1) {
                 for (int64_t c = 0; c < m; c++)
-                    if (low[c] >= 0) clear_ess(low[c]);
+                    if (st.low[c] >= 0) st.clear_ess(st.low[c]);
             } else if (l >= 0) {
-                clear_ess(l);
+                st.clear_ess(l);
             }
         }
-        if (k < tk.iters) entry(k);
+        if (k < tk.iters) st.entry(out, k);
         k++;
     };
     if (twist) {
@@ -612,6 +627,88 @@ static void replay_seq_trackers(const SeqTracking &tk, int algo, const std::vect
                 if (tk.dim[j] == d) visit(j);
     } else {
         for (int64_t j = 0; j < m; j++) visit(j);
+    }
+}
+
+// The same for the row forms (after every row i = m-1 .. 0: ph_row.cu:65-113,
+// ph_row_parallel.cu:44-83), from the walker's log of the rows that had
+// additions: each neighbour of the row's pivot took the pivot once and
+// moved to its logged new low.  The CPU form clears the row and the pivot
+// pair from ess before each addition and marks a neighbour that is now the
+// first column ever to hold its new low as a pair (a new low of -1 marks
+// nothing; the reference reads pivots[-1] there), in column order, and after
+// the last row marks every pair and classifies the remaining essentials
+// (ph_row.cu:91-103); the parallel form never fills arglow (classes stay 0)
+// and clears ess at every current low after each row.  time: the time
+// between two logged rows is shared evenly by the rows between them.
+static void replay_row_trackers(const SeqTracking &tk, int algo, const std::vector<int32_t> &low_true,
+                                std::vector<double> &out, std::vector<float> &ms) {
+    const int64_t m = (int64_t)tk.low0.size();
+    const bool par = algo == OPH_ALGO_PH_ROW_PARALLEL;
+    TrackState st(tk.low0, low_true);
+    std::vector<int32_t> pivots(m, -1);
+    for (int64_t j = 0; j < m; j++) {
+        const int32_t l = st.low[j];
+        if (l >= 0 && (pivots[l] == -1 || j < pivots[l])) pivots[l] = (int32_t)j;
+    }
+    out.assign(4 * (size_t)(m + 1), 0.0);
+    ms.assign((size_t)(m + 1), 0.0f);
+    st.entry(out, 0);
+    size_t e = 0;
+    long long tprev = tk.ev_t0;
+    int64_t kprev = 0;
+    std::vector<std::pair<int32_t, int32_t>> nb;
+    for (int64_t k = 1; k <= m; k++) {
+        const int64_t i = m - k;
+        nb.clear();
+        if (e + 5 <= tk.ev.size() && tk.ev[e] == (int)i) {
+            const int piv = tk.ev[e + 1], cnt = tk.ev[e + 2];
+            const long long t = (long long)(uint32_t)tk.ev[e + 3] | ((long long)tk.ev[e + 4] << 32);
+            for (int q = 0; q < cnt; q++) nb.emplace_back(tk.ev[e + 5 + 2 * q], tk.ev[e + 6 + 2 * q]);
+            e += 5 + 2 * (size_t)cnt;
+            std::sort(nb.begin(), nb.end());
+            for (const auto &pr : nb) {
+                const int32_t j = pr.first, nl = pr.second;
+                if (!par) {
+                    if (st.low[j] > -1) st.clear_ess(st.low[j]);
+                    st.clear_ess(piv);
+                    st.clear_ess(st.low[piv]);
+                }
+                st.set_low(j, nl);
+                if (!par && nl >= 0) {
+                    if (pivots[nl] == -1 || j < pivots[nl]) pivots[nl] = j;
+                    if (pivots[nl] == j) {
+                        st.set_cls(j, -1);
+                        st.set_cls(nl, 1);
+                        st.clear_ess(j);
+                        st.clear_ess(nl);
+                    }
+                }
+            }
+            for (int64_t q = kprev + 1; q <= k; q++) ms[q] = (float)((t - tprev) * 1e-6 / (double)(k - kprev));
+            tprev = t;
+            kprev = k;
+        }
+        if (par) {
+            if (k == 1) {
+                for (int64_t c = 0; c < m; c++)
+                    if (st.low[c] >= 0) st.clear_ess(st.low[c]);
+            } else {
+                for (const auto &pr : nb)
+                    if (pr.second >= 0) st.clear_ess(pr.second);
+            }
+        } else if (i == 0) {
+            for (int64_t c = 0; c < m; c++)
+                if (st.low[c] > -1) {
+                    st.clear_ess(c);
+                    st.clear_ess(st.low[c]);
+                    st.set_cls(c, -1);
+                    st.set_cls(st.low[c], 1);
+                }
+            for (int64_t c = 0; c < m; c++)
+                if (st.ess[c] == 1 && st.cls[c] == 0) st.set_cls(c, 2);
+        }
+        st.entry(out, k);
     }
 }
 
@@ -692,12 +789,10 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
         d_acc = (double *)ctx_alloc(ctx, S_TRACK, sizeof(double) * (16 + 4 * 2));
         if (!d_acc) return OPH_ERR_OOM;
     }
-    // standard and twist (both forms) record an entry per column, replayed
-    // on the host after the walk; the row forms the initial and final state
+    // the sequential algorithms record an entry per column (standard, twist)
+    // or row (the row forms), replayed on the host after the walk
     SeqTracking stk;
-    const bool per_col = track && m > 0 &&
-                         (algo == OPH_ALGO_STANDARD || algo == OPH_ALGO_STANDARD_PARALLEL ||
-                          algo == OPH_ALGO_TWIST || algo == OPH_ALGO_TWIST_PARALLEL);
+    const bool per_col = track && m > 0 && algo != OPH_ALGO_PMS;
     if (per_col) ctx->seq_track = &stk;
     Outputs o;
     o.low = d_out;
@@ -727,24 +822,29 @@ __attribute__((visibility("default"))) int oph_openph(const char *algstr, const 
                                          cudaMemcpyDeviceToHost, s));
         }
     }
-    std::vector<int32_t> h_low0, h_lt, h_et;
+    std::vector<int32_t> h_low0, h_lt;  // the final lows (0-based) and low_true, for the replay
     if (per_col && stk.iters > 0) {
         h_low0.resize(m);
         h_lt.resize(m);
-        h_et.resize(m);
         OPH_CUDA_TRY(cudaMemcpyAsync(h_low0.data(), w.low, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
         OPH_CUDA_TRY(cudaMemcpyAsync(h_lt.data(), lt0, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
-        OPH_CUDA_TRY(cudaMemcpyAsync(h_et.data(), esst, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
     }
     OPH_CUDA_TRY(cudaStreamSynchronize(s));
     if (num_iters) *num_iters = it;
     const int last = it - 1 < m ? it - 1 : m;
-    const bool replayed = per_col && stk.iters == it && (int64_t)stk.ns.size() == it;
-    if (replayed) replay_seq_trackers(stk, algo, h_low0, h_lt, h_et, entries);
+    const bool rows = algo == OPH_ALGO_PH_ROW || algo == OPH_ALGO_PH_ROW_PARALLEL;
+    const bool replayed = per_col && stk.iters == it &&
+                          (rows ? stk.rows_ok : (int64_t)stk.ns.size() == it);
+    std::vector<float> row_ms;
+    if (replayed) {
+        if (rows) replay_row_trackers(stk, algo, h_lt, entries, row_ms);
+        else replay_seq_trackers(stk, algo, h_low0, h_lt, entries);
+    }
     if (time_track && m >= 1) {
         time_track[0] = 0.0f;
         if (replayed) {
-            for (int k = 1; k <= last; k++) time_track[k] = (float)((stk.ns[k] - stk.ns[k - 1]) * 1e-6);
+            for (int k = 1; k <= last; k++)
+                time_track[k] = rows ? row_ms[k] : (float)((stk.ns[k] - stk.ns[k - 1]) * 1e-6);
         } else if (per_sweep) {
             for (int k = 1; k < last && k - 1 < (int)tr.sweep_ms.size(); k++) time_track[k] = tr.sweep_ms[k - 1];
             time_track[last] = (int)tr.sweep_ms.size() >= last ? tr.sweep_ms[last - 1] : info.device_ms;

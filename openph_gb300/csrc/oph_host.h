@@ -135,6 +135,12 @@ struct SeqTracking {
     std::vector<int8_t> dim;    // nnz - 1 per column (twist's visit order)
     std::vector<long long> ns;  // end of iteration k (k = 0: the walk's start)
     long long iters = 0;        // entries: 1 + iterations
+    // the row forms: each row that had additions, as the walker logged it
+    // ({row, pivot, k, end ns (two ints)} and k {column, new low} pairs),
+    // and the walk's start; rows_ok is false when the log ran out of room
+    std::vector<int> ev;
+    long long ev_t0 = 0;
+    bool rows_ok = false;
 };
 
 struct Context {

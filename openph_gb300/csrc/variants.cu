@@ -46,6 +46,12 @@ struct SeqArgs {
     int row_quirk;     // row: keep the reference CPU form's running ess estimate
     long long *it_ns;  // standard / twist with trackers: end of every iteration (globaltimer), or nullptr
     long long it_base; //   the iteration this launch starts at (1, or where an interrupted walk stopped)
+    // row with trackers: a log of the rows that had additions, each as
+    // {row, pivot, neighbours k, end time (ns, two ints)} then k pairs
+    // {column, its new low}; ev_cap ints, the length in ev[-2..-1] (int64),
+    // nullptr without trackers
+    int *ev;
+    long long ev_cap;
 };
 
 __device__ __forceinline__ long long global_ns() {
@@ -251,6 +257,10 @@ __global__ void __launch_bounds__(ROW_THREADS) k_row_walk(SeqArgs a) {
     long long i = a.start_pos;
     __shared__ int s_fail;
     if (threadIdx.x == 0) s_fail = 0;
+    if (a.ev && threadIdx.x == 0) {
+        long long *t0 = reinterpret_cast<long long *>(a.ev) - 2;
+        if (*t0 == 0) *t0 = global_ns();  // the first launch of the walk
+    }
     while (i >= 0) {
         if (wid == 0) {
             long long r = i, found = -1;
@@ -299,6 +309,31 @@ __global__ void __launch_bounds__(ROW_THREADS) k_row_walk(SeqArgs a) {
         }
         __syncthreads();
         if (s_fail) break;
+        if (a.ev && threadIdx.x == 0) {
+            // the row's additions, for the host's tracker replay (a row that
+            // failed is walked again after the regrow, and logged then)
+            long long *len = reinterpret_cast<long long *>(a.ev) - 1;
+            const long long at = *len, need = 5 + 2ll * (n - 1);
+            if (at >= 0 && at + need <= a.ev_cap) {
+                int *e = a.ev + at;
+                const long long t = global_ns();
+                e[0] = (int)i;
+                e[1] = piv;
+                e[2] = n - 1;
+                e[3] = (int)(t & 0xffffffffll);
+                e[4] = (int)(t >> 32);
+                int q = 5;
+                for (int k = 0; k < n; k++) {
+                    const int j = a.blist[k];
+                    if (j == piv) continue;
+                    e[q++] = j;
+                    e[q++] = a.low[j];
+                }
+                *len = at + need;
+            } else {
+                *len = -1;  // out of room: the host keeps the final entry only
+            }
+        }
         if (a.row_quirk) {
             for (int k = threadIdx.x; k < n; k += ROW_THREADS) {
                 const int j = a.blist[k];
@@ -420,6 +455,20 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
         a.blist = w.worklist;
         a.ess = d_ess;
         a.row_quirk = (algo == OPH_ALGO_PH_ROW) && d_ess != nullptr;
+        SeqTracking *tk = ctx->seq_track;
+        long long *ev_base = nullptr;
+        if (tk) {
+            // the initial lows and a log of the walk's additions for the
+            // host's replay: {start ns, length} then the records
+            tk->iters = iters;
+            tk->low0.resize(m);
+            OPH_CUDA_TRY(cudaMemcpyAsync(tk->low0.data(), w.low, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, s));
+            a.ev_cap = 8 * (long long)m + (1 << 20);
+            ev_base = (long long *)ctx_alloc(ctx, S_SEQNS, 16 + sizeof(int) * (size_t)a.ev_cap);
+            if (!ev_base) return OPH_ERR_OOM;
+            OPH_CUDA_TRY(cudaMemsetAsync(ev_base, 0, 16, s));
+            a.ev = reinterpret_cast<int *>(ev_base + 2);
+        }
         static bool attr = false;
         const size_t smem = (size_t)(ROW_THREADS / 32) * 3 * ROW_CAP * sizeof(int);
         if (!attr) {
@@ -444,6 +493,18 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
             if (g != OPH_OK) return g;
             a.pool = w.pool;
             regrows++;
+        }
+        if (tk) {
+            long long hdr[2] = {0, 0};
+            OPH_CUDA_TRY(cudaMemcpyAsync(hdr, ev_base, 16, cudaMemcpyDeviceToHost, s));
+            OPH_CUDA_TRY(cudaStreamSynchronize(s));
+            tk->ev_t0 = hdr[0];
+            tk->rows_ok = hdr[1] >= 0;
+            tk->ev.resize(hdr[1] > 0 ? (size_t)hdr[1] : 0);
+            if (!tk->ev.empty()) {
+                OPH_CUDA_TRY(cudaMemcpyAsync(tk->ev.data(), a.ev, sizeof(int) * tk->ev.size(), cudaMemcpyDeviceToHost, s));
+                OPH_CUDA_TRY(cudaStreamSynchronize(s));
+            }
         }
     }
     cudaEventRecord(ctx->ev[1], s);

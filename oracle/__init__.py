@@ -217,9 +217,10 @@ def ref_run(bm, alg: str = "twist", col_width: int = 10, timeout: float = 600.0)
 
 
 def tracked(bm, algo: str, low_true):
-    """The reference's per-iteration progress trackers of standard, twist
-    and their parallel forms, restated step by step in Python for small
-    matrices (O(m) work per iteration, as the reference's own tracker).
+    """The reference's per-iteration progress trackers of standard, twist,
+    the row algorithm and their parallel forms, restated step by step in
+    Python for small matrices (O(m) work per iteration, as the reference's
+    own tracker).  The row forms follow _tracked_rows.
 
     The reduction follows reduce_col_host (algorithms/kernels_host.cu:62-75;
     the device reduce_col, algorithms/kernels.cu:62-77, is the same without
@@ -272,12 +273,15 @@ def tracked(bm, algo: str, low_true):
         out.append((mx, s, f32(red / f32(m)), f32(1) if eh == num_ess_true else f32(num_ess_true / eh)))
 
     track()
-    if twist:
+    order = []
+    if algo in ("ph_row", "ph_row_parallel"):
+        _tracked_rows(cols, low, classes, ess, par, track)
+    elif twist:
         dims = [len(c) - 1 for c in cols]
         order = [j for d in range(max(dims, default=-1), 0, -1) for j in range(m) if dims[j] == d]
     else:
         order = list(range(m))
-    for j in order:
+    for j in (order if algo not in ("ph_row", "ph_row_parallel") else []):
         lj = low[j]
         while lj > -1 and arglow[lj] != -1:
             if not par:
@@ -316,3 +320,65 @@ def tracked(bm, algo: str, low_true):
     redu = np.array([o[2] for o in out], np.float32)
     eerr = np.array([o[3] for o in out], np.float32)
     return linf, lone, redu, eerr, n, np.array(low, np.int32)
+
+
+def _tracked_rows(cols, low, classes, ess, par, track):
+    """The row algorithm's loop for oracle.tracked, one tracker entry per row
+    i = m-1 .. 0.  CPU form (ph_row.cu:38-121): the pivot of row i is the
+    first column ever to hold low i; every later column of its dimension
+    list with that low takes the pivot once (left_to_right_neighbours_host,
+    ph_row.cu:2-31: ess cleared at the row and the pivot pair before the
+    addition, a column that is then the first ever to hold its new low
+    marked as a pair; the reference reads pivots[-1] for a new low of -1,
+    taken here as no mark), and after row 0 every pair is marked and the
+    remaining essentials classified 2 (ph_row.cu:91-103).  Parallel form
+    (ph_row_parallel.cu:20-89): the pivot is the least column with low i
+    (mark_neighbours), every other takes it, arglow stays empty, so
+    update_classes marks nothing and ess_hat clears every current low."""
+    m = len(cols)
+    dims = [len(c) - 1 for c in cols]
+    pivots = [-1] * m
+    for j in range(m):
+        if low[j] != -1 and (pivots[low[j]] == -1 or j < pivots[low[j]]):
+            pivots[low[j]] = j
+    for i in range(m - 1, -1, -1):
+        if not par:
+            piv = pivots[i]
+            if piv != -1:
+                nbs = [c for c in range(piv + 1, m) if dims[c] == dims[piv] and low[c] == low[piv]]
+                for j in nbs:
+                    if low[j] > -1:
+                        ess[low[j]] = 0
+                    ess[piv] = 0
+                    ess[low[piv]] = 0
+                    cols[j] ^= cols[piv]
+                    low[j] = max(cols[j]) if cols[j] else -1
+                    if low[j] != -1 and (pivots[low[j]] == -1 or j < pivots[low[j]]):
+                        pivots[low[j]] = j
+                    if low[j] != -1 and pivots[low[j]] == j:
+                        classes[j] = -1
+                        classes[low[j]] = 1
+                        ess[j] = 0
+                        ess[low[j]] = 0
+            if i == 0:
+                for c in range(m):
+                    if low[c] > -1:
+                        ess[c] = 0
+                        ess[low[c]] = 0
+                        classes[c] = -1
+                        classes[low[c]] = 1
+                for c in range(m):
+                    if ess[c] == 1 and classes[c] == 0:
+                        classes[c] = 2
+        else:
+            nbs = [c for c in range(m) if low[c] == i]
+            if nbs:
+                piv = min(nbs)
+                for j in nbs:
+                    if j > piv:
+                        cols[j] ^= cols[piv]
+                        low[j] = max(cols[j]) if cols[j] else -1
+            for c in range(m):
+                if low[c] > -1:
+                    ess[low[c]] = 0
+        track()

@@ -1,7 +1,8 @@
 """Per-iteration progress trackers of the sequential algorithms (the
-reference's track_host after every column: standard.cu:44-49, twist.cu:68-71;
-track after every column of the parallel forms: standard_parallel.cu:40-43,
-twist_parallel.cu:75-78; tracker.cu:92-172).  The oracle restates those loops
+reference's track_host after every column or row: standard.cu:44-49,
+twist.cu:68-71, ph_row.cu:107-110; track on the device for the parallel
+forms: standard_parallel.cu:40-43, twist_parallel.cu:75-78,
+ph_row_parallel.cu:76-79; tracker.cu:92-172).  The oracle restates those loops
 step by step (oracle.tracked); openph() keeps them from the GPU walk."""
 import numpy as np
 import pytest
@@ -10,7 +11,7 @@ import oracle
 from cases import small_cases
 from openph_gb300 import complexes as cx
 
-ALGOS = ["standard", "twist", "standard_parallel", "twist_parallel"]
+ALGOS = ["standard", "twist", "standard_parallel", "twist_parallel", "ph_row", "ph_row_parallel"]
 CASES = small_cases()
 
 
@@ -27,10 +28,11 @@ def test_restated_reduction_matches_the_oracle(built, name):
     bm = _cases()[name]
     want_s, _, _ = oracle.standard(bm)
     want_t, _, _ = oracle.twist(bm)
-    for algo, want in (("standard", want_s), ("twist", want_t)):
+    want_r, _, _ = oracle.ph_row(bm)
+    for algo, want in (("standard", want_s), ("twist", want_t), ("ph_row", want_r), ("ph_row_parallel", want_r)):
         *_, n, low = oracle.tracked(bm, algo, want_t)
         np.testing.assert_array_equal(low, want)
-        assert n == (bm.m + 1 if algo == "standard" else 1 + int((np.diff(bm.colptr) - 1 >= 1).sum()))
+        assert n == (1 + int((np.diff(bm.colptr) - 1 >= 1).sum()) if algo == "twist" else bm.m + 1)
 
 
 @pytest.mark.gpu
