@@ -286,6 +286,11 @@ def test_pms_trackers_per_sweep(cuda_lib):
     for arr in (lone, linf, redu):
         assert np.all(np.isfinite(arr[:n])) and np.all(arr[:n] >= 0)
     assert np.all(redu[:n] <= 1.0) and np.all((eerr[:n] > 0) & (eerr[:n] <= 1.0))
+    # what the schedule fixes although its interleaving does not: a column is
+    # classified once for good (unclassified never grows) and the essential
+    # estimate only loses rows (ess_true / ess_hat never falls)
+    assert np.all(np.diff(redu[:n]) <= 0)
+    assert np.all(np.diff(eerr[:n]) >= 0)
     assert np.all(tt[1:n] > 0) and tt[0] == 0
     assert np.all(lone[n:] == -1)
 
