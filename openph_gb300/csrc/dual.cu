@@ -241,10 +241,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tsums(long long *__restri
     if (threadIdx.x == 0) *total = carry;
 }
 
-// (scan 3) the offsets: out[i] = sum of cnt[0 .. i)
+// Segment of column c of a store whose column offsets are `off` (the layout
+// of k_setup_columns: room for the header, capacities in 16-byte units).
+__device__ __forceinline__ int64_t seg_start(int64_t c, int64_t off) { return 8 * c + 4 * ((off + 3) >> 2); }
+
+// (scan 3) the offsets: out[i] = sum of cnt[0 .. i); with `cur`, also each
+// column's scatter cursor: the pool index just past its last row slot
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int *__restrict__ cnt, int64_t n,
                                                              const long long *__restrict__ tsum,
-                                                             int64_t *__restrict__ out) {
+                                                             int64_t *__restrict__ out,
+                                                             unsigned long long *__restrict__ cur) {
     __shared__ long long red[33];
     for (int64_t t = blockIdx.x; t * SCAN_TILE < n; t += gridDim.x) {
         const int64_t base = t * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
@@ -253,7 +259,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_apply(const int *__restri
         long long run = tsum[t] + block_exclusive((long long)v[0] + v[1] + v[2] + v[3], red);
 #pragma unroll
         for (int q = 0; q < SCAN_ITEMS; q++) {
-            if (base + q < n) out[base + q] = run;
+            if (base + q < n) {
+                out[base + q] = run;
+                if (cur) cur[base + q] = (unsigned long long)(seg_start(base + q, run) + SEG_HDR + v[q]);
+            }
             run += v[q];
         }
     }
@@ -281,15 +290,12 @@ __global__ void k_dual_count(const int64_t *__restrict__ colptr, const int32_t *
     }
 }
 
-// Segment of column c of a store whose column offsets are `off` (the layout
-// of k_setup_columns: room for the header, capacities in 16-byte units).
-__device__ __forceinline__ int64_t seg_start(int64_t c, int64_t off) { return 8 * c + 4 * ((off + 3) >> 2); }
 
 // every entry of D into its column of D' (row m-1-j), slots from the top;
-// equal targets within the warp take their slots with one atomic
+// equal targets within the warp take their slots with one atomic on the
+// column's cursor, which holds the pool index itself (no offset lookup)
 __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
-                               const int64_t *__restrict__ dcolptr, int *__restrict__ cursor,
-                               int *__restrict__ pool, int roff) {
+                               unsigned long long *__restrict__ cursor, int *__restrict__ pool, int roff) {
     const int lane = threadIdx.x & 31;
     for (int64_t j0 = blockIdx.x * (int64_t)blockDim.x; j0 < m; j0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t j = j0 + threadIdx.x;
@@ -301,13 +307,12 @@ __global__ void k_dual_scatter(const int64_t *__restrict__ colptr, const int32_t
             const int c = t < n ? (int)(m - 1 - rows[lo + t]) : -1;
             const unsigned peers = __match_any_sync(0xffffffffu, c);
             const int leader = __ffs(peers) - 1;
-            int top = 0;
-            if (c >= 0 && lane == leader) top = atomicSub(&cursor[c], __popc(peers));
+            unsigned long long top = 0;
+            if (c >= 0 && lane == leader) top = atomicAdd(&cursor[c], 0ull - (unsigned long long)__popc(peers));
             top = __shfl_sync(0xffffffffu, top, leader);
             if (c >= 0) {
                 // the lower lane (the smaller column of D) takes the higher slot
-                const int pos = top - 1 - __popc(peers & ((1u << lane) - 1u));
-                pool[seg_start(c, dcolptr[c]) + SEG_HDR + pos] = val;
+                pool[(int64_t)top - 1 - __popc(peers & ((1u << lane) - 1u))] = val;
             }
         }
     }
@@ -723,17 +728,18 @@ bool host_prefers_dual(int64_t m, const int64_t *colptr, const int32_t *rows) {
     return lo >= 0 && hi > lo && count[lo] * DUAL_RATIO <= count[hi];
 }
 
-// Layout of the transpose's temporaries: the column offsets of D', the counts
-// (then the cursors), the three queues of longer columns, the radix sort's
-// scratch, four counters and the scan's tile sums.
+// Layout of the transpose's temporaries: the column offsets of D', the
+// counts, the scatter's cursors, the three queues of longer columns, the
+// radix sort's scratch, four counters and the scan's tile sums.
 struct DualTmp {
-    int64_t o_dcolptr, o_cnt, o_long, o_mid, o_wide, o_scr, o_ctr, o_tsum, bytes;
+    int64_t o_dcolptr, o_cnt, o_cur, o_long, o_mid, o_wide, o_scr, o_ctr, o_tsum, bytes;
     DualTmp(int64_t m, int64_t nnz) {
         auto r256 = [](int64_t b) { return (b + 255) & ~255ll; };
         const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
         o_dcolptr = 0;
         o_cnt = r256(8 * (m + 1));
-        o_long = o_cnt + r256(4 * m);
+        o_cur = o_cnt + r256(4 * m);
+        o_long = o_cur + r256(8 * m);
         o_mid = o_long + r256(4 * m);
         o_wide = o_mid + r256(4 * m);
         o_scr = o_wide + r256(4 * m);
@@ -753,6 +759,7 @@ int dual_build_store(cudaStream_t s, int sm_count, const int64_t *colptr, const 
     char *buf = (char *)tmp;
     int64_t *dcolptr = (int64_t *)(buf + L.o_dcolptr);
     int *cnt = (int *)(buf + L.o_cnt), *long_list = (int *)(buf + L.o_long), *mid_list = (int *)(buf + L.o_mid);
+    unsigned long long *cur = (unsigned long long *)(buf + L.o_cur);
     int *wide_list = (int *)(buf + L.o_wide), *scratch = (int *)(buf + L.o_scr), *ctr = (int *)(buf + L.o_ctr);
     long long *tsum = (long long *)(buf + L.o_tsum);
     const int64_t ntiles = (m + SCAN_TILE - 1) / SCAN_TILE;
@@ -764,8 +771,8 @@ int dual_build_store(cudaStream_t s, int sm_count, const int64_t *colptr, const 
     k_dual_count<<<gm, 256, 0, s>>>(colptr, rows, m, cnt);
     k_scan_sums<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum);
     k_scan_tsums<<<1, SCAN_THREADS, 0, s>>>(tsum, ntiles, dcolptr + m);
-    k_scan_apply<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum, dcolptr);
-    k_dual_scatter<<<gm, 256, 0, s>>>(colptr, rows, m, dcolptr, cnt, pool, roff);
+    k_scan_apply<<<gs, SCAN_THREADS, 0, s>>>(cnt, m, tsum, dcolptr, cur);
+    k_dual_scatter<<<gm, 256, 0, s>>>(colptr, rows, m, cur, pool, roff);
     k_dual_finish<<<gm, 256, 0, s>>>(dcolptr, colptr, m, pool, seg, low, dim, mid_list, &ctr[2], seg_base);
     k_dual_finish_warp<<<sm_count * 8, FIN_WARPS * 32, 0, s>>>(dcolptr, pool, low, mid_list, &ctr[2], wide_list,
                                                              &ctr[3], long_list, &ctr[0]);
