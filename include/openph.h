@@ -94,7 +94,9 @@ typedef struct {
     int64_t pool_bytes;      /* column-store bytes in use at the end           */
     int32_t regrows;         /* times the column store had to grow             */
     float device_ms;         /* device time of the reduction (CUDA events)     */
-    int32_t dual;            /* 1 when pms reduced the anti-transpose          */
+    int32_t dual;            /* 1 when pms reduced the anti-transpose, 2 when
+                                some blocks of D were reduced on D' and the
+                                others on D                                   */
 } oph_info;
 
 /* A context owns one CUDA stream on one device plus cached device buffers;
@@ -169,7 +171,8 @@ typedef struct {
 typedef struct {
     int64_t completed, pending, active, sweeps, regrows;
     int64_t pool_bytes_in_use, columns_in_use, arena_bytes;
-    int64_t dual_admitted;  /* requests reduced through their anti-transpose */
+    int64_t dual_admitted;  /* requests with a part reduced through their
+                               anti-transpose (split by block or whole)   */
 } oph_server_counters;
 
 int oph_server_create(int device, int64_t budget_bytes, int32_t max_active, oph_server **out);
@@ -265,14 +268,21 @@ int oph_context_set_tier0(oph_context *ctx, int32_t lanes, int32_t cap);
  *                    one dimension bucket, distinct buckets from distinct
  *                    ones), has at least 2^17 columns and its top bucket
  *                    holds at least 8 times the columns of the bottom one
- *                    (Rips complexes), else D
+ *                    (Rips complexes); else, from 2^17 columns, a choice
+ *                    per block (one dimension's columns with their rows,
+ *                    which reduce independently of the others): D' for a
+ *                    block whose row simplices have at most two cofaces on
+ *                    average (the triangles of a triangulated surface, as in
+ *                    lower-star images), D for the others; else D
  *   OPH_DUAL_NEVER   always D
  *   OPH_DUAL_ALWAYS  D' whenever the input is graded
+ *   OPH_DUAL_BLOCKS  the per-block choice at any size
  * Reductions with per-sweep trackers (oph_openph with tracker outputs)
  * always reduce D, whose progress the trackers describe.  Default AUTO. */
 #define OPH_DUAL_AUTO 0
 #define OPH_DUAL_NEVER 1
 #define OPH_DUAL_ALWAYS 2
+#define OPH_DUAL_BLOCKS 3
 int oph_context_set_dual(oph_context *ctx, int32_t mode);
 
 /* Testing hooks: cap the sweep count (0 = default) and the initial column

@@ -23,7 +23,7 @@ from . import _build
 ALGORITHMS = ("standard", "twist", "ph_row", "standard_parallel", "twist_parallel", "ph_row_parallel", "pms")
 
 OPH_OK, OPH_ERR_BAD_INPUT, OPH_ERR_OOM, OPH_ERR_OVERFLOW, OPH_ERR_TIMEOUT, OPH_ERR_CUDA, OPH_ERR_ALGO = range(7)
-OPH_DUAL_AUTO, OPH_DUAL_NEVER, OPH_DUAL_ALWAYS = range(3)
+OPH_DUAL_AUTO, OPH_DUAL_NEVER, OPH_DUAL_ALWAYS, OPH_DUAL_BLOCKS = range(4)
 
 
 class OphError(RuntimeError):
@@ -364,9 +364,12 @@ class Context:
     def set_dual(self, mode):
         """Which matrix pms reduces: "auto" (the anti-transpose for graded
         inputs of >= 2^17 columns whose top dimension bucket holds >= 8x the
-        columns of the bottom one), "never" or "always" (the anti-transpose
-        when graded)."""
-        code = {"auto": OPH_DUAL_AUTO, "never": OPH_DUAL_NEVER, "always": OPH_DUAL_ALWAYS}.get(mode, mode)
+        columns of the bottom one, else at that size a choice per dimension
+        block), "never", "always" (the anti-transpose when graded) or
+        "blocks" (the per-block choice at any size: D' for a block whose row
+        simplices have at most two cofaces on average, D for the others)."""
+        code = {"auto": OPH_DUAL_AUTO, "never": OPH_DUAL_NEVER, "always": OPH_DUAL_ALWAYS,
+                "blocks": OPH_DUAL_BLOCKS}.get(mode, mode)
         rc = lib().oph_context_set_dual(self._h, int(code))
         if rc != OPH_OK:
             raise OphError(rc, "oph_context_set_dual")

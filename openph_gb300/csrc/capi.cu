@@ -193,6 +193,44 @@ struct Outputs {
     int count = 0;
 };
 
+// pms with some blocks of D reduced on D' and the others on D (dual_choose's
+// DUAL_CHOICE_SPLIT): D' first, its columns of the D-reduced blocks
+// pre-cleared; then D, with its columns of the D'-reduced blocks and every
+// row the D' reduction paired pre-cleared; the lows put together in w.low.
+static int reduce_split(Context *ctx, Work &w, oph_info *info) {
+    const int64_t m = w.m;
+    uint8_t *pre = (uint8_t *)ctx_alloc(ctx, S_PRECLEAR, m);
+    if (!pre) return OPH_ERR_OOM;
+    Work wd;
+    int rc;
+    if ((rc = dual_setup(ctx, w, wd)) || (rc = split_preclear_dual(ctx, w, pre))) return rc;
+    DevStatus hs;
+    if ((rc = ctx_sync_status(ctx, wd, &hs))) return rc;
+    if (hs.error) return OPH_ERR_BAD_INPUT;
+    wd.preclear = pre;
+    oph_info a{}, b{};
+    if ((rc = run_pms(ctx, wd, &a))) return rc;
+    int32_t *mapped = nullptr;
+    if ((rc = dual_lows(ctx, wd, &mapped)) || (rc = split_preclear_primal(ctx, m, mapped, pre))) return rc;
+    if ((rc = setup_store(ctx, w, true))) return rc;
+    ctx->launches += 3;
+    if ((rc = ctx_sync_status(ctx, w, &hs))) return rc;
+    if (hs.error || hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;
+    w.preclear = pre;
+    rc = run_pms(ctx, w, &b);
+    w.preclear = nullptr;
+    if (rc || (rc = split_merge(ctx, w.low, mapped, m))) return rc;
+    info->sweeps = a.sweeps + b.sweeps;
+    info->num_iters = a.num_iters + b.num_iters;
+    info->additions = a.additions + b.additions;
+    info->slots_moved = a.slots_moved + b.slots_moved;
+    info->pool_bytes = std::max(a.pool_bytes, b.pool_bytes);
+    info->regrows = a.regrows + b.regrows;
+    info->device_ms = a.device_ms + b.device_ms;
+    info->dual = 2;
+    return OPH_OK;
+}
+
 // Runs `algo` on the CSC already in w.colptr / w.rows and writes outputs.
 static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_info *info) {
     cudaStream_t s = ctx->stream;
@@ -210,14 +248,18 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
     // checks (bounds first) whenever it runs
     const bool grades = pms && !ctx->track && ctx->dual != OPH_DUAL_NEVER && m > 0;
     if (!w.checked && !grades && (rc = check_csc(ctx, w.colptr, w.rows, m, w.nnz, nullptr, 0))) return rc;
-    bool dual = false;
+    int choice = DUAL_CHOICE_D;
     if (pms && !ctx->track) {
         bool bad = false;
-        if ((rc = dual_choose(ctx, w, ctx->dual, &dual, &bad))) return rc;
+        if ((rc = dual_choose(ctx, w, ctx->dual, &choice, &bad))) return rc;
         if (bad) return OPH_ERR_BAD_INPUT;
     }
+    const bool dual = choice == DUAL_CHOICE_DUAL;
+    const bool split = choice == DUAL_CHOICE_SPLIT && m > 0;
     Work wd;
-    if (dual) {
+    if (split) {
+        // reduce_split builds both stores itself
+    } else if (dual) {
         // D' built straight into its column store, with its buckets, left[]
         // and beta
         if ((rc = dual_setup(ctx, w, wd))) return rc;
@@ -232,16 +274,20 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
         cudaEventElapsedTime(&ctx->prof.setup_ms, ctx->ev[2], ctx->ev[3]);
     }
     DevStatus hs;
-    if ((rc = ctx_sync_status(ctx, wr, &hs))) return rc;
-    if (hs.error) return OPH_ERR_BAD_INPUT;
-    // the Phase I scan keeps one running maximum per dimension bucket -1 ..
-    // MAXC-2 (D's buckets, checked by dual_choose when D' is reduced)
-    if (pms && !dual && hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;
+    if (!split) {
+        if ((rc = ctx_sync_status(ctx, wr, &hs))) return rc;
+        if (hs.error) return OPH_ERR_BAD_INPUT;
+        // the Phase I scan keeps one running maximum per dimension bucket -1 ..
+        // MAXC-2 (D's buckets, checked by dual_choose when D' is reduced)
+        if (pms && !dual && hs.max_dim > MAXC - 2) return OPH_ERR_BAD_INPUT;
+    }
     const int row_quirk = algo == OPH_ALGO_PH_ROW;
     if (row_quirk && o.ess) k_fill_i32<<<grid_for(ctx, m), 256, 0, s>>>(o.ess, m, 1);
     oph_info local{};
     if (m > 0) {
-        if (pms) {
+        if (split) {
+            rc = reduce_split(ctx, w, &local);
+        } else if (pms) {
             rc = run_pms(ctx, wr, &local);
         } else {
             rc = run_sequential(ctx, w, algo, row_quirk ? o.ess : nullptr, &local);
@@ -257,7 +303,7 @@ static int reduce_core(Context *ctx, int algo, Work &w, const Outputs &o, oph_in
         if ((rc = dual_lows(ctx, wd, &mapped))) return rc;
         OPH_CUDA_TRY(cudaMemcpyAsync(w.low, mapped, sizeof(int32_t) * m, cudaMemcpyDeviceToDevice, s));
     }
-    local.dual = dual ? 1 : 0;
+    if (!split) local.dual = dual ? 1 : 0;
     if (m > 0) {
         k_finalize1<<<grid_for(ctx, m), 256, 0, s>>>(w.low, m, o.one_based, ess_mode, o.inst_off, o.count, o.low,
                                                      o.ess, o.arglow);
@@ -926,7 +972,7 @@ struct TuneBatch { int32_t count; const int64_t *col_off, *colptr; const int32_t
 extern "C" {
 
 __attribute__((visibility("default"))) int oph_context_set_dual(oph_context *ctx, int32_t mode) {
-    if (!ctx || mode < OPH_DUAL_AUTO || mode > OPH_DUAL_ALWAYS) return OPH_ERR_BAD_INPUT;
+    if (!ctx || mode < OPH_DUAL_AUTO || mode > OPH_DUAL_BLOCKS) return OPH_ERR_BAD_INPUT;
     ctx->dual = mode;
     return OPH_OK;
 }

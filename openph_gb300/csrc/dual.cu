@@ -637,6 +637,43 @@ __global__ void k_dual_low(const int32_t *__restrict__ low_d, int64_t m, int32_t
     }
 }
 
+// ----------------------------------------------------- blocks on D or D'
+// The blocks of D (a bucket's columns with the rows they hold, all from one
+// other bucket) reduce independently: a column only ever adds columns whose
+// low lies in its own row bucket, all of them in its own bucket.  So each
+// block may be reduced on D or on D' and the low pairs put together.
+
+// D' columns pre-cleared for the D' reduction: the rows (reversed) of every
+// column of a block reduced on D.  A simplex's cofaces all lie in one
+// bucket, so a D' column is either all D-block or all D'-block.
+__global__ void k_split_clear_dual(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
+                                   const int8_t *__restrict__ bucket, const uint8_t *__restrict__ split,
+                                   uint8_t *__restrict__ clear) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        if (split[bucket[j] + 1]) continue;
+        for (int64_t k = colptr[j]; k < colptr[j + 1]; k++) clear[m - 1 - rows[k]] = 1;
+    }
+}
+
+// D's columns pre-cleared for the D reduction: those of the blocks reduced
+// on D', and every row D' paired (low_D(j) = i makes column i positive: the
+// twist clearing, across blocks).
+__global__ void k_split_clear_primal(const int8_t *__restrict__ bucket, const uint8_t *__restrict__ split,
+                                     const int32_t *__restrict__ low_dual, int64_t m, uint8_t *__restrict__ clear) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x) {
+        if (split[bucket[j] + 1]) clear[j] = 1;
+        const int i = low_dual[j];
+        if (i >= 0) clear[i] = 1;
+    }
+}
+
+// The D'-block columns take their lows from the D' reduction.
+__global__ void k_split_merge(int32_t *__restrict__ low, const int32_t *__restrict__ low_dual,
+                              const int8_t *__restrict__ bucket, const uint8_t *__restrict__ split, int64_t m) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < m; j += (int64_t)gridDim.x * blockDim.x)
+        if (split[bucket[j] + 1]) low[j] = low_dual[j];
+}
+
 static int grid_of(int sm_count, int64_t n) {
     int64_t g = (n + 255) / 256, cap = (int64_t)sm_count * 16;
     return (int)std::max<int64_t>(1, std::min(g, cap));
@@ -649,15 +686,24 @@ struct Grade {
     int mixed, bad;
 };
 
-size_t dual_grade_tmp_bytes(int64_t m) { return sizeof(Grade) + 256 + (size_t)(m > 0 ? m : 1); }
+// The grading's temporaries: its tallies, each column's bucket (one byte)
+// and the per-block choice (MAXC bytes, by column bucket + 1).
+static size_t r256(size_t b) { return (b + 255) & ~(size_t)255; }
+size_t dual_grade_tmp_bytes(int64_t m) { return r256(sizeof(Grade)) + r256((size_t)(m > 0 ? m : 1)) + 256; }
+void dual_split_arrays(void *tmp, int64_t m, const int8_t **bucket, const uint8_t **split) {
+    char *base = (char *)tmp + r256(sizeof(Grade));
+    *bucket = (const int8_t *)base;
+    *split = (const uint8_t *)(base + r256((size_t)(m > 0 ? m : 1)));
+}
 
 int dual_grade(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m, int64_t nnz,
-               int mode, void *tmp, bool *use, bool *bad_input, int *launches) {
-    *use = false;
+               int mode, void *tmp, int *choice, bool *bad_input, int *launches) {
+    *choice = DUAL_CHOICE_D;
     *bad_input = false;
     if (mode == OPH_DUAL_NEVER || m == 0) return OPH_OK;
     Grade *d = (Grade *)tmp;
-    int8_t *bucket = (int8_t *)tmp + ((sizeof(Grade) + 255) & ~(size_t)255);
+    int8_t *bucket = (int8_t *)tmp + r256(sizeof(Grade));
+    uint8_t *split_d = (uint8_t *)bucket + r256((size_t)m);
     Grade init{};
     for (int b = 0; b < MAXC; b++) init.tab[b] = TAB_NONE;
     OPH_CUDA_TRY(cudaMemcpyAsync(d, &init, sizeof(Grade), cudaMemcpyHostToDevice, s));
@@ -684,18 +730,44 @@ int dual_grade(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_
             if (lo < 0) lo = b;
             hi = b;
         }
-    if (mode == OPH_DUAL_ALWAYS) *use = true;
-    else *use = m >= DUAL_MIN_M && lo >= 0 && hi > lo && g.count[lo] * DUAL_RATIO <= g.count[hi];
+    if (mode == OPH_DUAL_ALWAYS ||
+        (mode == OPH_DUAL_AUTO && m >= DUAL_MIN_M && lo >= 0 && hi > lo && g.count[lo] * DUAL_RATIO <= g.count[hi])) {
+        *choice = DUAL_CHOICE_DUAL;
+        return OPH_OK;
+    }
+    if (mode != OPH_DUAL_BLOCKS && !(mode == OPH_DUAL_AUTO && m >= DUAL_MIN_M)) return OPH_OK;
+    // per block (the columns of bucket b with their rows, bucket tab[b]):
+    // D' when its row simplices have at most two cofaces on average, as in
+    // a triangulated surface, where every column of D' holds at most two
+    // rows and so does every sum of them (a union-find walk), while D's
+    // columns grow into the boundaries of ever larger regions
+    uint8_t split[MAXC] = {};
+    bool any_split = false, any_d = false;
+    for (int b = 1; b < MAXC; b++) {
+        if (!g.count[b] || g.tab[b] == TAB_NONE) continue;
+        const int r = g.tab[b] + 1;
+        split[b] = r >= 0 && r < MAXC && (unsigned long long)b * g.count[b] <= 2ull * g.count[r];
+        if (split[b]) any_split = true;
+        else any_d = true;
+    }
+    if (!any_split) return OPH_OK;
+    if (!any_d) {
+        *choice = DUAL_CHOICE_DUAL;
+        return OPH_OK;
+    }
+    OPH_CUDA_TRY(cudaMemcpyAsync(split_d, split, MAXC, cudaMemcpyHostToDevice, s));
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    *choice = DUAL_CHOICE_SPLIT;
     return OPH_OK;
 }
 
-int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input) {
-    *use = false;
+int dual_choose(Context *ctx, const Work &w, int mode, int *choice, bool *bad_input) {
+    *choice = DUAL_CHOICE_D;
     *bad_input = false;
     if (mode == OPH_DUAL_NEVER || w.m == 0) return OPH_OK;
     void *tmp = ctx_alloc(ctx, S_DGRADE, dual_grade_tmp_bytes(w.m));
     if (!tmp) return OPH_ERR_OOM;
-    return dual_grade(ctx->stream, ctx->sm_count, w.colptr, w.rows, w.m, w.nnz, mode, tmp, use, bad_input,
+    return dual_grade(ctx->stream, ctx->sm_count, w.colptr, w.rows, w.m, w.nnz, mode, tmp, choice, bad_input,
                       &ctx->launches);
 }
 
@@ -797,6 +869,48 @@ int dual_setup(Context *ctx, const Work &w, Work &wd) {
     if (!tmp) return OPH_ERR_OOM;
     return dual_build_store(ctx->stream, ctx->sm_count, w.colptr, w.rows, w.m, w.nnz, wd.pool, 0, 0, wd.seg, wd.low,
                             wd.dim, wd.rec, wd.beta, tmp, &ctx->launches);
+}
+
+void split_clear_dual(cudaStream_t s, int sm_count, const void *grade_tmp, const int64_t *colptr,
+                      const int32_t *rows, int64_t m, uint8_t *clear) {
+    const int8_t *bucket;
+    const uint8_t *split;
+    dual_split_arrays(const_cast<void *>(grade_tmp), m, &bucket, &split);
+    k_split_clear_dual<<<grid_of(sm_count, m), 256, 0, s>>>(colptr, rows, m, bucket, split, clear);
+}
+
+void split_clear_primal(cudaStream_t s, int sm_count, const void *grade_tmp, int64_t m, const int32_t *low_dual,
+                        uint8_t *clear) {
+    const int8_t *bucket;
+    const uint8_t *split;
+    dual_split_arrays(const_cast<void *>(grade_tmp), m, &bucket, &split);
+    k_split_clear_primal<<<grid_of(sm_count, m), 256, 0, s>>>(bucket, split, low_dual, m, clear);
+}
+
+int split_preclear_dual(Context *ctx, const Work &w, uint8_t *clear) {
+    OPH_CUDA_TRY(cudaMemsetAsync(clear, 0, w.m, ctx->stream));
+    split_clear_dual(ctx->stream, ctx->sm_count, ctx->bufs[S_DGRADE].ptr, w.colptr, w.rows, w.m, clear);
+    ctx->launches++;
+    OPH_CUDA_TRY(cudaGetLastError());
+    return OPH_OK;
+}
+
+int split_preclear_primal(Context *ctx, int64_t m, const int32_t *low_dual, uint8_t *clear) {
+    OPH_CUDA_TRY(cudaMemsetAsync(clear, 0, m, ctx->stream));
+    split_clear_primal(ctx->stream, ctx->sm_count, ctx->bufs[S_DGRADE].ptr, m, low_dual, clear);
+    ctx->launches++;
+    OPH_CUDA_TRY(cudaGetLastError());
+    return OPH_OK;
+}
+
+int split_merge(Context *ctx, int32_t *low, const int32_t *low_dual, int64_t m) {
+    const int8_t *bucket;
+    const uint8_t *split;
+    dual_split_arrays(ctx->bufs[S_DGRADE].ptr, m, &bucket, &split);
+    k_split_merge<<<grid_of(ctx, m), 256, 0, ctx->stream>>>(low, low_dual, bucket, split, m);
+    ctx->launches++;
+    OPH_CUDA_TRY(cudaGetLastError());
+    return OPH_OK;
 }
 
 int dual_lows(Context *ctx, const Work &wd, int32_t **low) {

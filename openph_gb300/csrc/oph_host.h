@@ -50,6 +50,7 @@ struct Work {
     DevStatus *st = nullptr;
     bool ascending = false;           // pms: buckets in ascending order (the anti-transpose)
     bool checked = false;             // colptr/rows already passed the structural check
+    const uint8_t *preclear = nullptr;  // pms: columns cleared before Phase 0 (m bytes), or none
 };
 
 struct Context;
@@ -82,11 +83,29 @@ int run_sequential(Context *ctx, Work &w, int algo, int32_t *d_ess, oph_info *in
 // maps wd's lows back to D's.
 // The automatic choice: D' for matrices of at least DUAL_MIN_M columns whose
 // top bucket holds DUAL_RATIO times the bottom one's columns (below that
-// size the few more sweeps and the transpose cost more than D's additions).
+// size the few more sweeps and the transpose cost more than D's additions);
+// else, at that size, a choice per block (a bucket's columns with their
+// rows): D' for the blocks whose row simplices have at most two cofaces on
+// average, D for the others (DUAL_CHOICE_SPLIT when both occur).
 constexpr unsigned long long DUAL_RATIO = 8;
 constexpr int64_t DUAL_MIN_M = 1 << 17;
-int dual_choose(Context *ctx, const Work &w, int mode, bool *use, bool *bad_input);
+enum { DUAL_CHOICE_D = 0, DUAL_CHOICE_DUAL = 1, DUAL_CHOICE_SPLIT = 2 };
+int dual_choose(Context *ctx, const Work &w, int mode, int *choice, bool *bad_input);
 int dual_setup(Context *ctx, const Work &w, Work &wd);
+// DUAL_CHOICE_SPLIT (after dual_choose, whose grading they read): the D'
+// columns of the D-reduced blocks pre-cleared; then D's columns of the
+// D'-reduced blocks and every row the D' reduction paired; then the lows of
+// the D'-reduced blocks' columns taken from low_dual (D'-reduced, mapped).
+int split_preclear_dual(Context *ctx, const Work &w, uint8_t *clear);
+int split_preclear_primal(Context *ctx, int64_t m, const int32_t *low_dual, uint8_t *clear);
+int split_merge(Context *ctx, int32_t *low, const int32_t *low_dual, int64_t m);
+// The two pre-clears on any stream, for callers with their own buffers (the
+// request server): grade_tmp is dual_grade's tmp, clear the m columns' flags
+// (set, never reset).
+void split_clear_dual(cudaStream_t s, int sm_count, const void *grade_tmp, const int64_t *colptr,
+                      const int32_t *rows, int64_t m, uint8_t *clear);
+void split_clear_primal(cudaStream_t s, int sm_count, const void *grade_tmp, int64_t m, const int32_t *low_dual,
+                        uint8_t *clear);
 // The same pieces for callers with their own buffers (the request server):
 // dual_grade grades a device CSC (synchronous; tmp of dual_grade_tmp_bytes);
 // host_prefers_dual makes the automatic choice on a host CSC;
@@ -97,7 +116,9 @@ int dual_setup(Context *ctx, const Work &w, Work &wd);
 // dual_tmp_bytes).
 size_t dual_grade_tmp_bytes(int64_t m);
 int dual_grade(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m, int64_t nnz,
-               int mode, void *tmp, bool *use, bool *bad_input, int *launches);
+               int mode, void *tmp, int *choice, bool *bad_input, int *launches);
+// each column's bucket and the per-block choice inside dual_grade's tmp
+void dual_split_arrays(void *tmp, int64_t m, const int8_t **bucket, const uint8_t **split);
 bool host_prefers_dual(int64_t m, const int64_t *colptr, const int32_t *rows);
 size_t dual_tmp_bytes(int64_t m, int64_t nnz);
 int dual_build_store(cudaStream_t s, int sm_count, const int64_t *colptr, const int32_t *rows, int64_t m,
@@ -181,7 +202,7 @@ struct Context {
 enum Slot {
     S_STATUS, S_COLPTR, S_ROWS, S_LOW, S_CLASSES, S_CLEAR, S_DIM, S_FIRST, S_LEFT, S_BETA, S_WORK, S_WIDE, S_SEG,
     S_ROWPIV, S_AGG, S_POOL, S_POOL2, S_ESS, S_ARGLOW, S_COO_R, S_COO_C, S_LOWTRUE, S_TRACK, S_INSTOFF, S_TMP,
-    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_IASC, S_IBUCKET, S_IOPEN, S_RANGES, S_SEQNS, S_NSLOTS
+    S_ULIST, S_KAGG, S_ESSHAT, S_SLIST, S_DGRADE, S_DCOLPTR, S_DSORT, S_DTEMP, S_DLOW, S_BITMAP, S_CHECK, S_IASC, S_IBUCKET, S_IOPEN, S_RANGES, S_SEQNS, S_PRECLEAR, S_NSLOTS
 };
 
 }  // namespace oph

@@ -56,10 +56,12 @@ constexpr int P1_TILE = P1_THREADS * P1_ITEMS;
 // mark_pivots_and_clear (pms_functions.cu:33-53): low_j == beta_j >= 0 means
 // row low_j first appears in column j, so j is a final pivot; the column of
 // row low_j is positive and is cleared (the clear is applied by Phase I).
+// A column cleared before Phase 0 publishes nothing (one this kernel clears
+// meanwhile is positive, so it is no pivot either way).
 __global__ void k_phase0(PmsArgs a, int64_t c0, int64_t c1) {
     for (int64_t j = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < c1; j += (int64_t)gridDim.x * blockDim.x) {
         int lj = a.low[j];
-        if (lj >= 0 && lj == a.beta[j]) {
+        if (lj >= 0 && lj == a.beta[j] && !a.clear[j]) {
             a.classes[j] = -1;
             const long long sj = a.seg[j];
             rec_publish<false>(a.rec, lj, (int)j, a.pool[sj], sj, a.pool + sj + SEG_HDR);
@@ -1574,8 +1576,10 @@ struct ChainResult {
 // reads that row's pivot record; two barriers of those 31 warps per
 // addition.  Warp 31 prefetches ahead of them (chain_prefetcher).  A pivot
 // row below the window undoes that addition's toggles and ends the chain
-// (`fell`): the caller hands the column to the merge path.  n, lj: the
-// column's length and low; lo: its lowest row.
+// (`fell`): the caller hands the column to the merge path.  After
+// a.chain_cap additions (if set) the chain stops with the column unresolved,
+// its low's pivot known: the next sweep's Phase I sees a repeat and hands it
+// back.  n, lj: the column's length and low; lo: its lowest row.
 template <class W>
 __device__ ChainResult bitmap_chain(const PmsArgs &a, int j, int lj, int n, int lo, int w0, W word,
                                     long long &adds, long long &slots) {
@@ -1603,7 +1607,7 @@ __device__ ChainResult bitmap_chain(const PmsArgs &a, int j, int lj, int n, int 
     if (wid == nw - 1) {
         chain_prefetcher(a, word, w0, &s_cur, &s_done, s_ctmp);
     } else if (h.x >= 0 && h.x < j) {
-        for (int par = 0;; par ^= 1) {
+        for (int par = 0, steps = 1;; par ^= 1, steps++) {
             const int np = h.y;
             const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
             int d = 0;
@@ -1672,7 +1676,7 @@ __device__ ChainResult bitmap_chain(const PmsArgs &a, int j, int lj, int n, int 
                 made = true;
                 break;
             }
-            if (h.x < 0 || h.x >= j) break;
+            if (h.x < 0 || h.x >= j || steps == a.chain_cap) break;
         }
     }
     if (tid == 0) s_done = 1;
@@ -1758,7 +1762,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
     } else {
         const int lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
         const int ntg = blockDim.x - 32;  // toggling threads: every warp but the last
-        for (int par = 0;; par ^= 1) {
+        for (int par = 0, steps = 1;; par ^= 1, steps++) {
             const int np = h.y;
             const int *P = np <= 4 ? nullptr : a.pool + 4ll * (unsigned)h.w + SEG_HDR;
             const int p2 = np >= 2 ? (P ? e.z : rec_entry(e, np - 2)) : -1;
@@ -1843,7 +1847,7 @@ __device__ bool reduce_column_bitmap(const PmsArgs &a, int j, uint32_t *bm, int6
             e = s_rec[par][1];
             mark_clear<false>(a, lj, tid == 0);
             if (h.z == j) { made_pivot = true; break; }  // the beta check: row lj first appears in j
-            if (h.x < 0 || h.x >= j) break;
+            if (h.x < 0 || h.x >= j || steps == a.chain_cap) break;
         }
     }
     const int lo_row = s_lo;
@@ -2526,7 +2530,8 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
 
     OPH_CUDA_TRY(cudaMemsetAsync(w.first, 0x7f, sizeof(int32_t) * m, s));
     OPH_CUDA_TRY(cudaMemsetAsync(w.classes, 0, m, s));
-    OPH_CUDA_TRY(cudaMemsetAsync(w.clear, 0, m, s));
+    if (w.preclear) OPH_CUDA_TRY(cudaMemcpyAsync(w.clear, w.preclear, m, cudaMemcpyDeviceToDevice, s));
+    else OPH_CUDA_TRY(cudaMemsetAsync(w.clear, 0, m, s));
 
     Tracking *tr = ctx->track;
     if (tr) {

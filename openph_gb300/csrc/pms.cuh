@@ -54,6 +54,11 @@ struct PmsArgs {
     // tier (a bitmap across a cluster's shared memory) instead of the
     // global bitmap (0: tier 3 keeps them)
     int cluster_tier;
+    // the bitmap tiers' additions per column per sweep (0: no limit); a
+    // column that reaches it is written back unresolved and goes on in the
+    // next sweep, so no sweep waits on one long chain (the request server,
+    // whose sweeps serve every active request)
+    int chain_cap;
     // per-instance bucket order (the server, whose instances are reduced on
     // D or on their anti-transpose; nullptr: `ascending` above for all):
     // iasc[b] = 1 for an instance in ascending order, ibucket[b * MAXC + d]

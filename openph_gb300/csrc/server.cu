@@ -105,6 +105,14 @@ struct Request {
     int sweeps = 0, status = OPH_OK, slot = -1;
     bool done = false;
     bool dual = false;  // reduced through its anti-transpose
+    // some dimension blocks on D', the others on D: first the D' part (dual
+    // set), then, re-queued at the head, the D part with the D' part's pairs
+    // cleared; the grading (buckets, per-block choice) and the D' part's
+    // lows (mapped to D) stay on the device until the end
+    bool split = false;
+    int phase = 0;
+    void *d_grade = nullptr;
+    int32_t *d_mapped = nullptr;  // 2m ints
     int64_t c0 = -1, reg = -1, reg_ints = 0;
     int64_t ring_off = -1;  // low then ess in the pinned result ring (ints), or -1
     bool listed = false;    // in the Phase I list: its sweeps have begun
@@ -246,6 +254,24 @@ __global__ void k_srv_out_dual2(int64_t m, int64_t c0, PmsArgs a, int32_t *out) 
         out[m + (m - 1 - c)] = 0;
     }
 }
+// The same for the D part of a split request: the columns of the D'-reduced
+// blocks take the lows its D' part found (mapped, local), then the ess pass
+// runs over the merged lows.
+__global__ void k_srv_out_split1(int64_t m, int64_t c0, PmsArgs a, const int8_t *__restrict__ bucket,
+                                 const uint8_t *__restrict__ split, const int32_t *__restrict__ mapped, int32_t *out) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int l = a.low[c0 + jj];
+        const int32_t v = split[bucket[jj] + 1] ? mapped[jj] : (l >= 0 ? (int32_t)(l - c0) : -1);
+        out[jj] = v;
+        out[m + jj] = v >= 0 ? 0 : 1;
+    }
+}
+__global__ void k_srv_out_split2(int64_t m, int32_t *out) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int v = out[jj];
+        if (v >= 0) out[m + v] = 0;
+    }
+}
 // ... then the columns become inert (no low, cleared, no instance).
 __global__ void k_srv_inert(int64_t m, int64_t c0, PmsArgs a) {
     for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
@@ -285,6 +311,10 @@ __global__ void k_srv_sweep_reset(DevStatus *st) {
 }
 
 // ------------------------------------------------------------------ server
+// The bitmap tiers' additions per column and sweep: a long chain goes on in
+// the next sweep instead of holding every active request's sweep.
+constexpr int SERVE_CHAIN_CAP = 128;
+
 struct Server {
     Context *ctx = nullptr;  // owns the stream and the device buffers
     cudaStream_t sub_stream = nullptr;  // submissions: copy, check, grade
@@ -360,10 +390,16 @@ struct Server {
             dual_build_store(s, ctx->sm_count, d_colptr, d_rows, r->m, r->nnz, a.pool + reg, reg, (int)c0,
                              a.seg + c0, a.low + c0, const_cast<int8_t *>(a.dim) + c0, a.rec + c0,
                              const_cast<int32_t *>(a.beta) + c0, tmp, nullptr);
+            // a split request's D' part: its columns of the D-reduced blocks
+            // pre-cleared (Phase 0 skips them, Phase I zeroes them)
+            if (r->split) split_clear_dual(s, ctx->sm_count, r->d_grade, d_colptr, d_rows, r->m, a.clear + c0);
         } else if (r->m > 0) {
             k_srv_init<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, b, reg, a);
             k_srv_left<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, a);
             k_srv_beta<<<grid(r->m), 256, 0, s>>>(r->m, c0, a);
+            // a split request's D part: the D'-reduced blocks' columns and
+            // every row its D' part paired pre-cleared
+            if (r->split) split_clear_primal(s, ctx->sm_count, r->d_grade, r->m, r->d_mapped, a.clear + c0);
         }
         if (r->m > 0) admitted_rng.emplace_back(c0, r->m);
         dual_admitted += r->dual ? 1 : 0;
@@ -376,10 +412,13 @@ struct Server {
             // released after the sweep's synchronisation
             staged.emplace_back(stg, stage_ints);
         }
-        // the device copy is freed in stream order after those kernels
-        cudaFreeAsync(r->d_buf, s);
-        r->d_buf = nullptr;
-        r->t_admit = now_ms();
+        // the device copy is freed in stream order after those kernels (a
+        // split request's D part reads it again)
+        if (!(r->split && r->phase == 0)) {
+            cudaFreeAsync(r->d_buf, s);
+            r->d_buf = nullptr;
+        }
+        if (r->t_admit == 0) r->t_admit = now_ms();
         slots[b] = r;
         admitted++;
         return 0;
@@ -396,11 +435,23 @@ struct Server {
             Request *r = done[k];
             const int64_t m = r->m;
             if (m == 0) continue;
+            if (r->split && r->phase == 0) {
+                // the D' part's lows, mapped to D, kept for the D part
+                k_srv_out_dual1<<<grid(m), 256, 0, s>>>(m, r->d_mapped);
+                k_srv_out_dual2<<<grid(m), 256, 0, s>>>(m, r->c0, a, r->d_mapped);
+                continue;
+            }
             int64_t out = pool.alloc(2 * m + 4, 64);
             if (out >= 0) outs.emplace_back(out, 2 * m + 4);
             else out = r->reg;  // the request's own region is no longer read
             dptr[k] = a.pool + out;
-            if (r->dual) {
+            if (r->split) {
+                const int8_t *bucket;
+                const uint8_t *split;
+                dual_split_arrays(r->d_grade, m, &bucket, &split);
+                k_srv_out_split1<<<grid(m), 256, 0, s>>>(m, r->c0, a, bucket, split, r->d_mapped, dptr[k]);
+                k_srv_out_split2<<<grid(m), 256, 0, s>>>(m, dptr[k]);
+            } else if (r->dual) {
                 k_srv_out_dual1<<<grid(m), 256, 0, s>>>(m, dptr[k]);
                 k_srv_out_dual2<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
             } else {
@@ -411,6 +462,10 @@ struct Server {
         for (size_t k = 0; k < done.size(); k++) {
             Request *r = done[k];
             if (r->m == 0) continue;
+            if (r->split && r->phase == 0) {
+                k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
+                continue;
+            }
             if (h_ring) {
                 std::lock_guard<std::mutex> lk(mu);
                 r->ring_off = ring.alloc(2 * r->m, 16);
@@ -424,6 +479,12 @@ struct Server {
                 cudaMemcpyAsync(r->ess.data(), dptr[k] + r->m, sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
             }
             k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
+            if (r->split) {
+                cudaFreeAsync(r->d_grade, s);
+                cudaFreeAsync(r->d_mapped, s);
+                r->d_grade = nullptr;
+                r->d_mapped = nullptr;
+            }
         }
         cudaStreamSynchronize(s);
         for (auto &o : outs) pool.release(o.first, o.second);
@@ -436,6 +497,16 @@ struct Server {
                 retired_cols.emplace_back(r->c0, std::max<int64_t>(r->m, 1));
                 pool.release(r->reg, r->reg_ints);
                 slots[r->slot] = nullptr;
+                if (r->split && r->phase == 0) {
+                    // the D part next, ahead of every queued request
+                    r->phase = 1;
+                    r->dual = false;
+                    r->listed = false;
+                    r->c0 = r->reg = -1;
+                    r->slot = -1;
+                    pending.push_front(r);
+                    continue;
+                }
                 r->t_done = t;
                 r->done = true;
                 completed++;
@@ -716,6 +787,8 @@ __attribute__((visibility("default"))) int oph_server_create(int device, int64_t
     if (ok) ok = sweep_grids(ctx, mc, (mc + 2047) / 2048, &sv->g) == OPH_OK;
     // columns wider than a CTA's shared window go to the cluster tier
     a.cluster_tier = ok && sv->g.g4 > 0;
+    // no sweep waits on one long chain of the bitmap tiers
+    a.chain_cap = getenv("OPH_SERVE_CHAIN_CAP") ? atoi(getenv("OPH_SERVE_CHAIN_CAP")) : SERVE_CHAIN_CAP;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->sub_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (ok) ok = cudaStreamCreateWithFlags(&sv->adm_stream, cudaStreamNonBlocking) == cudaSuccess;
     if (ok) ok = cudaEventCreateWithFlags(&sv->adm_done, cudaEventDisableTiming) == cudaSuccess;
@@ -798,12 +871,31 @@ int submit_copy(oph_server *sv, int64_t m, int64_t nnz, const int64_t *colptr, c
         cudaStreamSynchronize(s);
         return e != cudaSuccess ? OPH_ERR_CUDA : OPH_ERR_BAD_INPUT;
     }
-    bool use = false, bad_g = false;
+    int choice = DUAL_CHOICE_D;
+    bool bad_g = false;
     void *gtmp = nullptr;
+    int32_t *mapped = nullptr;
     if (m >= DUAL_MIN_M && cudaMallocAsync(&gtmp, dual_grade_tmp_bytes(m), s) == cudaSuccess) {
-        if (dual_grade(s, sv->ctx->sm_count, cp, rw, m, nnz, OPH_DUAL_AUTO, gtmp, &use, &bad_g, nullptr) != OPH_OK)
-            use = false;
-        cudaFreeAsync(gtmp, s);
+        if (dual_grade(s, sv->ctx->sm_count, cp, rw, m, nnz, OPH_DUAL_AUTO, gtmp, &choice, &bad_g, nullptr) != OPH_OK ||
+            bad_g)
+            choice = DUAL_CHOICE_D;
+        // a split request keeps its grading, and room for its D' part's lows
+        if (choice == DUAL_CHOICE_SPLIT && cudaMallocAsync(&mapped, sizeof(int32_t) * 2 * m, s) != cudaSuccess) {
+            cudaGetLastError();
+            choice = DUAL_CHOICE_D;
+        }
+        if (choice != DUAL_CHOICE_SPLIT) {
+            cudaFreeAsync(gtmp, s);
+            gtmp = nullptr;
+        }
+        // the worker uses both on its own streams
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            cudaFreeAsync(buf, s);
+            if (gtmp) cudaFreeAsync(gtmp, s);
+            if (mapped) cudaFreeAsync(mapped, s);
+            cudaStreamSynchronize(s);
+            return OPH_ERR_CUDA;
+        }
     } else {
         cudaGetLastError();
     }
@@ -811,12 +903,17 @@ int submit_copy(oph_server *sv, int64_t m, int64_t nnz, const int64_t *colptr, c
     r->m = m;
     r->nnz = nnz;
     r->d_buf = buf;
-    r->dual = use && !bad_g;
+    r->dual = choice != DUAL_CHOICE_D;
+    r->split = choice == DUAL_CHOICE_SPLIT;
+    r->d_grade = gtmp;
+    r->d_mapped = mapped;
     r->t_submit = now_ms();
     {
         std::lock_guard<std::mutex> lk(sv->mu);
         if (sv->error) {
             cudaFreeAsync(buf, s);
+            if (gtmp) cudaFreeAsync(gtmp, s);
+            if (mapped) cudaFreeAsync(mapped, s);
             delete r;
             return sv->error;
         }
@@ -888,6 +985,9 @@ __attribute__((visibility("default"))) int oph_server_wait(oph_server *sv, int64
         info->submit_ms = r->t_submit;
         info->done_ms = r->t_done;
     }
+    // device buffers a failed request still holds
+    for (void *p : {r->d_buf, r->d_grade, static_cast<void *>(r->d_mapped)})
+        if (p) cudaFree(p);
     delete r;
     return rc;
 }
@@ -919,7 +1019,8 @@ __attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
     if (sv->worker.joinable()) sv->worker.join();
     cudaSetDevice(sv->ctx->device);
     for (auto &kv : sv->all) {
-        if (kv.second->d_buf) cudaFree(kv.second->d_buf);
+        for (void *p : {kv.second->d_buf, kv.second->d_grade, static_cast<void *>(kv.second->d_mapped)})
+            if (p) cudaFree(p);
         delete kv.second;
     }
     if (sv->sub_stream) cudaStreamDestroy(sv->sub_stream);

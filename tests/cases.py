@@ -92,3 +92,39 @@ def mixed_buckets():
     """A matrix whose columns of three rows take them from two buckets (the
     triangle's edges, and three vertices), so its buckets are not graded."""
     return BoundaryMatrix.from_columns([[], [], [], [0, 1], [0, 2], [1, 2], [3, 4, 5], [0, 1, 2]])
+
+
+def lower_star_volume(n, seed, sigma=1.5):
+    """The lower-star filtration of a smoothed random n x n x n volume on its
+    Freudenthal triangulation (each grid cube cut into six tetrahedra along
+    its main diagonal): a simplex valued by its largest vertex, ties by
+    dimension then vertex tuple.  Every triangle has at most two
+    tetrahedra, edges and triangles have many cofaces."""
+    from itertools import combinations, permutations
+    rng = np.random.default_rng(seed)
+    f = rng.standard_normal((n, n, n))
+    if sigma > 0:  # separable box-blur passes, a cheap smoothing
+        for ax in range(3):
+            for _ in range(int(sigma * 2)):
+                f = (f + np.roll(f, 1, axis=ax) + np.roll(f, -1, axis=ax)) / 3.0
+    val = f.ravel() + rng.random(n ** 3) * 1e-9
+    vid = lambda x, y, z: (x * n + y) * n + z
+    tets = set()
+    for x in range(n - 1):
+        for y in range(n - 1):
+            for z in range(n - 1):
+                for perm in permutations(range(3)):
+                    p = [x, y, z]
+                    vs = [vid(*p)]
+                    for ax in perm:
+                        p[ax] += 1
+                        vs.append(vid(*p))
+                    tets.add(tuple(sorted(vs)))
+    simplices = set((v,) for v in range(n ** 3))
+    for t in tets:
+        for k in (2, 3, 4):
+            simplices.update(combinations(t, k))
+    simplices = sorted(simplices, key=lambda s: (max(val[list(s)]), len(s), s))
+    pos = {s: i for i, s in enumerate(simplices)}
+    cols = [[] if len(s) == 1 else sorted(pos[s[:y] + s[y + 1:]] for y in range(len(s))) for s in simplices]
+    return BoundaryMatrix.from_columns(cols)

@@ -1,6 +1,7 @@
 """pms on the anti-transpose (OPH_DUAL_*): every output equal to the oracle's
-twist on D, the automatic choice per matrix, the fall-back to D for inputs
-whose buckets are not graded, batches, and the drop-in call."""
+twist on D, the automatic choice per matrix, the choice per dimension block
+(some blocks on D', the others on D), the fall-back to D for inputs whose
+buckets are not graded, batches, and the drop-in call."""
 import numpy as np
 import pytest
 
@@ -8,7 +9,7 @@ import oracle
 from openph_gb300 import complexes as cx
 from openph_gb300.api import Context
 
-from cases import mixed_buckets, random_complex, simplex_skeleton, small_cases
+from cases import lower_star_volume, mixed_buckets, random_complex, simplex_skeleton, small_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -23,7 +24,7 @@ def dctx(cuda_lib):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-@pytest.mark.parametrize("mode", ["always", "never", "auto"])
+@pytest.mark.parametrize("mode", ["always", "never", "auto", "blocks"])
 def test_small_cases(dctx, name, mode):
     bm = CASES[name]
     dctx.set_dual(mode)
@@ -36,7 +37,7 @@ def test_small_cases(dctx, name, mode):
     j = np.nonzero(want >= 0)[0]
     want_arg[want[j]] = j
     np.testing.assert_array_equal(arglow, want_arg)
-    if mode != "auto":  # every small case is graded
+    if mode in ("always", "never"):  # every small case is graded
         assert info["dual"] == (1 if mode == "always" else 0)
 
 
@@ -47,25 +48,86 @@ def test_larger_complexes_both_ways(dctx, seed):
             simplex_skeleton(8, seed=40 + seed, max_dim=4)]
     for bm in mats:
         want, want_ess, _ = oracle.twist(bm)
-        for mode in ("always", "never"):
+        for mode in ("always", "never", "blocks"):
             dctx.set_dual(mode)
             low, ess, info = dctx.reduce(bm, "pms")
             np.testing.assert_array_equal(low, want, err_msg=f"{mode} m={bm.m}")
             np.testing.assert_array_equal(ess, want_ess, err_msg=f"{mode} m={bm.m}")
-            assert info["dual"] == (1 if mode == "always" else 0)
+            if mode != "blocks":
+                assert info["dual"] == (1 if mode == "always" else 0)
     dctx.set_dual("auto")
+
+
+@pytest.mark.parametrize("shape", [(12, 12, 1.0), (40, 56, 2.0), (64, 33, 4.0), (97, 80, 3.0)])
+def test_lower_star_split_by_block(dctx, shape):
+    """A lower-star image's edges-on-vertices block on D, its
+    triangles-on-edges block on D' (every edge has at most two triangles):
+    the D' part first, then D with the edges it paired cleared; low and ess
+    equal to the oracle's twist on D."""
+    h, w, sigma = shape
+    bm = cx.lower_star_image(h, w, seed=h + w, sigma=sigma)
+    want, want_ess, _ = oracle.twist(bm)
+    dctx.set_dual("blocks")
+    low, ess, arglow, info = dctx.reduce(bm, "pms", with_arglow=True)
+    dctx.set_dual("auto")
+    assert info["dual"] == 2
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+    want_arg = np.full(bm.m, -1, np.int32)
+    j = np.nonzero(want >= 0)[0]
+    want_arg[want[j]] = j
+    np.testing.assert_array_equal(arglow, want_arg)
+
+
+@pytest.mark.parametrize("n,seed", [(6, 1), (10, 2), (13, 3)])
+def test_lower_star_volume_split(dctx, n, seed):
+    """A 3-D lower-star volume: tetrahedra-on-triangles on D' (a triangle has
+    at most two tetrahedra), triangles-on-edges and edges-on-vertices on D,
+    with the triangles D' paired cleared; equal to the oracle's twist."""
+    bm = lower_star_volume(n, seed)
+    want, want_ess, _ = oracle.twist(bm)
+    dctx.set_dual("blocks")
+    low, ess, info = dctx.reduce(bm, "pms")
+    dctx.set_dual("auto")
+    assert info["dual"] == 2
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_split_pool_regrow(dctx):
+    """A split reduction whose D part (the triangles of a 3-D volume) grows
+    its columns past a column store holding only the packed input."""
+    bm = lower_star_volume(10, 5)
+    want, want_ess, _ = oracle.twist(bm)
+    with Context(0) as c:
+        c.set_limits(initial_pool_bytes=1)
+        c.set_dual("blocks")
+        low, ess, info = c.reduce(bm, "pms")
+    assert info["dual"] == 2 and info["regrows"] > 0
+    np.testing.assert_array_equal(low, want)
+    np.testing.assert_array_equal(ess, want_ess)
 
 
 def test_auto_choice(dctx):
     """Rips complexes of 2^17 columns or more (top bucket >= 8x the bottom
-    one) go to D'; a smaller one, and a lower-star image (triangles about
-    twice the vertices) of any size, stay on D."""
+    one) go to D'; a smaller one stays on D; a lower-star image of that size
+    (triangles about twice the vertices, edges with at most two triangles)
+    is split by block, a smaller one stays on D."""
     dctx.set_dual("auto")
     _, _, info = dctx.reduce(cx.rips_cube(100, seed=1), "pms")  # 166,750 columns
     assert info["dual"] == 1
     _, _, info = dctx.reduce(cx.rips_cube(30, seed=1), "pms")
     assert info["dual"] == 0
-    _, _, info = dctx.reduce(cx.lower_star_image(256, 256, seed=2), "pms")
+    bm = cx.lower_star_image(256, 256, seed=2)
+    low, ess, info = dctx.reduce(bm, "pms")
+    assert info["dual"] == 2
+    dctx.set_dual("never")
+    low_d, ess_d, info_d = dctx.reduce(bm, "pms")
+    dctx.set_dual("auto")
+    assert info_d["dual"] == 0
+    np.testing.assert_array_equal(low, low_d)
+    np.testing.assert_array_equal(ess, ess_d)
+    _, _, info = dctx.reduce(cx.lower_star_image(64, 64, seed=2), "pms")
     assert info["dual"] == 0
     _, _, info = dctx.reduce(CASES["empty5"], "pms")
     assert info["dual"] == 0

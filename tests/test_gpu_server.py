@@ -141,8 +141,9 @@ def test_device_submission_rejects_malformed(cuda_lib):
 def dual_mix():
     """Requests of at least 2^17 columns whose top dimension dwarfs the
     bottom one (reduced through their anti-transpose, as a single-matrix
-    reduction would), a lower-star image of the same size (stays on D) and
-    small complexes, with the oracle's answers."""
+    reduction would), a lower-star image of the same size (split by block:
+    its D' part, then its D part) and small complexes, with the oracle's
+    answers."""
     reqs = [cx.rips_torus(400, 150_000, seed=41), cx.rips_cube(95, seed=42), cx.lower_star_image(160, 160, seed=43),
             cx.rips_cube(20, seed=44), cx.rips_torus(60, 8000, seed=45), cx.rips_torus(400, 140_000, seed=46)]
     return reqs, [oracle.twist(bm)[:2] for bm in reqs]
@@ -156,7 +157,8 @@ def test_anti_transpose_requests_in_the_mix(cuda_lib, dual_mix):
         tickets = [srv.submit(bm) for bm in reqs]
         mixed = [srv.wait(t)[:2] for t in tickets]
         st = srv.stats()
-    assert st["dual_admitted"] == sum(info["dual"] for _, _, info in alone) == 3
+    assert [info["dual"] for _, _, info in alone] == [1, 1, 2, 0, 0, 1]
+    assert st["dual_admitted"] == 4  # requests with a part on the anti-transpose
     for (wl, we), (lm, em), (la, ea, _) in zip(want, mixed, alone):
         np.testing.assert_array_equal(lm, wl)
         np.testing.assert_array_equal(em, we)
@@ -180,7 +182,7 @@ def test_anti_transpose_requests_arriving_while_running(cuda_lib, dual_mix):
         th.join()
         res = {k: srv.wait(t) for k, t in out.items()}
         st = srv.stats()
-    assert st["dual_admitted"] == 6
+    assert st["dual_admitted"] == 8
     for k, i in enumerate(order):
         np.testing.assert_array_equal(res[k][0], want[i][0])
         np.testing.assert_array_equal(res[k][1], want[i][1])
@@ -198,7 +200,7 @@ def test_anti_transpose_device_submission(cuda_lib, dual_mix):
     with Server(0, budget_bytes=8 << 30, max_active=8) as srv:
         tickets = [srv.submit_device(Dev(reqs[0])), srv.submit(reqs[2]), srv.submit_device(Dev(reqs[1]))]
         res = [srv.wait(t) for t in tickets]
-        assert srv.stats()["dual_admitted"] == 2
+        assert srv.stats()["dual_admitted"] == 3
     for (low, ess, _), i in zip(res, (0, 2, 1)):
         np.testing.assert_array_equal(low, want[i][0])
         np.testing.assert_array_equal(ess, want[i][1])
