@@ -105,14 +105,21 @@ struct Request {
     int sweeps = 0, status = OPH_OK, slot = -1;
     bool done = false;
     bool dual = false;  // reduced through its anti-transpose
-    // some dimension blocks on D', the others on D: first the D' part (dual
-    // set), then, re-queued at the head, the D part with the D' part's pairs
-    // cleared; the grading (buckets, per-block choice) and the D' part's
-    // lows (mapped to D) stay on the device until the end
+    // some dimension blocks on D', the others on D: the request itself is
+    // the D' part (dual set); after its first sweep an internal request for
+    // the D part (user set) joins the head of the queue, its columns of the
+    // D'-reduced blocks and of the rows the D' part has paired by then
+    // cleared.  The grading (buckets, per-block choice), the D' part's lows
+    // (mapped to D, then a scratch ess) and the D part's lows stay on the
+    // device until both parts have converged.
     bool split = false;
-    int phase = 0;
+    Request *user = nullptr;      // a D part: the request it belongs to
+    Request *part = nullptr;      // a split request: its D part, once made
+    int parts_left = 0;           // a split request: parts not yet converged
+    bool part_done = false;       // a split request: its D' part converged
+    int64_t sweep0 = 0;           // the server's sweep count at admission
     void *d_grade = nullptr;
-    int32_t *d_mapped = nullptr;  // 2m ints
+    int32_t *d_mapped = nullptr;  // 3m ints: D' part's lows (mapped), ess scratch, D part's lows
     int64_t c0 = -1, reg = -1, reg_ints = 0;
     int64_t ring_off = -1;  // low then ess in the pinned result ring (ints), or -1
     bool listed = false;    // in the Phase I list: its sweeps have begun
@@ -254,16 +261,34 @@ __global__ void k_srv_out_dual2(int64_t m, int64_t c0, PmsArgs a, int32_t *out) 
         out[m + (m - 1 - c)] = 0;
     }
 }
-// The same for the D part of a split request: the columns of the D'-reduced
-// blocks take the lows its D' part found (mapped, local), then the ess pass
-// runs over the merged lows.
-__global__ void k_srv_out_split1(int64_t m, int64_t c0, PmsArgs a, const int8_t *__restrict__ bucket,
-                                 const uint8_t *__restrict__ split, const int32_t *__restrict__ mapped, int32_t *out) {
+// A split request's D part converged: its local lows, kept until the D'
+// part has converged too.
+__global__ void k_srv_save_local(int64_t m, int64_t c0, PmsArgs a, int32_t *__restrict__ out) {
     for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
         const int l = a.low[c0 + jj];
-        const int32_t v = split[bucket[jj] + 1] ? mapped[jj] : (l >= 0 ? (int32_t)(l - c0) : -1);
+        out[jj] = l >= 0 ? (int32_t)(l - c0) : -1;
+    }
+}
+// Both parts converged: the columns of the D'-reduced blocks take the lows
+// the D' part found (mapped), the others the D part's; then the ess pass
+// runs over the merged lows.
+__global__ void k_srv_out_split1(int64_t m, const int8_t *__restrict__ bucket, const uint8_t *__restrict__ split,
+                                 const int32_t *__restrict__ mapped, const int32_t *__restrict__ lowd, int32_t *out) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = split[bucket[jj] + 1] ? mapped[jj] : lowd[jj];
         out[jj] = v;
         out[m + jj] = v >= 0 ? 0 : 1;
+    }
+}
+// The D part's clears when its D' part is still being reduced: the columns
+// of the D'-reduced blocks, and the D column m-1-c of every D' column c the
+// D' part has made a pivot so far (its pair makes that column positive; a
+// pivot's class is final, so a concurrent sweep can only add to the set).
+__global__ void k_srv_split_clear_live(int64_t m, int64_t c0_dual, int64_t c0, PmsArgs a,
+                                       const int8_t *__restrict__ bucket, const uint8_t *__restrict__ split) {
+    for (int64_t jj = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; jj < m; jj += (int64_t)gridDim.x * blockDim.x) {
+        if (split[bucket[jj] + 1]) a.clear[c0 + jj] = 1;
+        if (a.classes[c0_dual + jj] == -1) a.clear[c0 + (m - 1 - jj)] = 1;
     }
 }
 __global__ void k_srv_out_split2(int64_t m, int32_t *out) {
@@ -344,6 +369,7 @@ struct Server {
     std::deque<Request *> pending;
     std::map<int64_t, Request *> all;
     std::vector<Request *> slots;
+    std::vector<Request *> all_split;  // split requests admitted without their D part yet (worker only)
     std::thread worker;
     bool stop = false;
     int64_t next_ticket = 1;
@@ -398,8 +424,19 @@ struct Server {
             k_srv_left<<<grid(r->m), 256, 0, s>>>(d_colptr, d_rows, r->m, c0, a);
             k_srv_beta<<<grid(r->m), 256, 0, s>>>(r->m, c0, a);
             // a split request's D part: the D'-reduced blocks' columns and
-            // every row its D' part paired pre-cleared
-            if (r->split) split_clear_primal(s, ctx->sm_count, r->d_grade, r->m, r->d_mapped, a.clear + c0);
+            // the rows its D' part has paired pre-cleared (from the D' part's
+            // pivots while it runs, else from its lows)
+            if (r->user) {
+                Request *u = r->user;
+                if (!u->part_done) {
+                    const int8_t *bucket;
+                    const uint8_t *split;
+                    dual_split_arrays(u->d_grade, r->m, &bucket, &split);
+                    k_srv_split_clear_live<<<grid(r->m), 256, 0, s>>>(r->m, u->c0, c0, a, bucket, split);
+                } else {
+                    split_clear_primal(s, ctx->sm_count, u->d_grade, r->m, u->d_mapped, a.clear + c0);
+                }
+            }
         }
         if (r->m > 0) admitted_rng.emplace_back(c0, r->m);
         dual_admitted += r->dual ? 1 : 0;
@@ -414,11 +451,13 @@ struct Server {
         }
         // the device copy is freed in stream order after those kernels (a
         // split request's D part reads it again)
-        if (!(r->split && r->phase == 0)) {
+        if (!(r->split && !r->user)) {
             cudaFreeAsync(r->d_buf, s);
             r->d_buf = nullptr;
         }
         if (r->t_admit == 0) r->t_admit = now_ms();
+        r->sweep0 = sweeps;
+        if (r->split && !r->user) all_split.push_back(r);
         slots[b] = r;
         admitted++;
         return 0;
@@ -426,30 +465,50 @@ struct Server {
 
     // Retires every converged request: output kernels for all of them, then
     // the copies to the host, one synchronisation, then the notifications.
+    // A part of a split request keeps its lows on the device; the request is
+    // finished by the later of its two parts.
     void retire_all(const std::vector<Request *> &done) {
         if (done.empty()) return;
         cudaStream_t s = ctx->stream;
-        std::vector<std::pair<int64_t, int64_t>> outs;
-        std::vector<int32_t *> dptr(done.size(), nullptr);
-        for (size_t k = 0; k < done.size(); k++) {
-            Request *r = done[k];
-            const int64_t m = r->m;
-            if (m == 0) continue;
-            if (r->split && r->phase == 0) {
-                // the D' part's lows, mapped to D, kept for the D part
-                k_srv_out_dual1<<<grid(m), 256, 0, s>>>(m, r->d_mapped);
-                k_srv_out_dual2<<<grid(m), 256, 0, s>>>(m, r->c0, a, r->d_mapped);
+        std::vector<Request *> users;  // requests whose results go out now
+        for (Request *r : done) {
+            if (!r->split) {
+                users.push_back(r);
                 continue;
             }
-            int64_t out = pool.alloc(2 * m + 4, 64);
-            if (out >= 0) outs.emplace_back(out, 2 * m + 4);
-            else out = r->reg;  // the request's own region is no longer read
-            dptr[k] = a.pool + out;
+            Request *u = r->user ? r->user : r;
+            const int64_t m = r->m;
+            if (r->user) {
+                k_srv_save_local<<<grid(m), 256, 0, s>>>(m, r->c0, a, u->d_mapped + 2 * m);
+            } else {
+                k_srv_out_dual1<<<grid(m), 256, 0, s>>>(m, u->d_mapped);
+                k_srv_out_dual2<<<grid(m), 256, 0, s>>>(m, r->c0, a, u->d_mapped);
+            }
+            k_srv_inert<<<grid(m), 256, 0, s>>>(m, r->c0, a);
+            if (--u->parts_left == 0) users.push_back(u);
+        }
+        std::vector<std::pair<int64_t, int64_t>> outs;
+        std::vector<int32_t *> dptr(users.size(), nullptr);
+        for (size_t k = 0; k < users.size(); k++) {
+            Request *r = users[k];
+            const int64_t m = r->m;
+            if (m == 0) continue;
+            const int64_t out = pool.alloc(2 * m + 4, 64);
+            if (out >= 0) {
+                outs.emplace_back(out, 2 * m + 4);
+                dptr[k] = a.pool + out;
+            } else {
+                // the request's own region is no longer read; a split
+                // request's results go over its D' part's lows (each thread
+                // reads its own element first) and the ess scratch after them
+                dptr[k] = r->split ? r->d_mapped : a.pool + r->reg;
+            }
             if (r->split) {
                 const int8_t *bucket;
                 const uint8_t *split;
                 dual_split_arrays(r->d_grade, m, &bucket, &split);
-                k_srv_out_split1<<<grid(m), 256, 0, s>>>(m, r->c0, a, bucket, split, r->d_mapped, dptr[k]);
+                k_srv_out_split1<<<grid(m), 256, 0, s>>>(m, bucket, split, r->d_mapped, r->d_mapped + 2 * m,
+                                                         dptr[k]);
                 k_srv_out_split2<<<grid(m), 256, 0, s>>>(m, dptr[k]);
             } else if (r->dual) {
                 k_srv_out_dual1<<<grid(m), 256, 0, s>>>(m, dptr[k]);
@@ -459,13 +518,9 @@ struct Server {
                 k_srv_out2<<<grid(m), 256, 0, s>>>(m, r->c0, a, dptr[k]);
             }
         }
-        for (size_t k = 0; k < done.size(); k++) {
-            Request *r = done[k];
+        for (size_t k = 0; k < users.size(); k++) {
+            Request *r = users[k];
             if (r->m == 0) continue;
-            if (r->split && r->phase == 0) {
-                k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
-                continue;
-            }
             if (h_ring) {
                 std::lock_guard<std::mutex> lk(mu);
                 r->ring_off = ring.alloc(2 * r->m, 16);
@@ -478,14 +533,15 @@ struct Server {
                 cudaMemcpyAsync(r->low.data(), dptr[k], sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
                 cudaMemcpyAsync(r->ess.data(), dptr[k] + r->m, sizeof(int32_t) * r->m, cudaMemcpyDeviceToHost, s);
             }
-            k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
+            if (!r->split) k_srv_inert<<<grid(r->m), 256, 0, s>>>(r->m, r->c0, a);
+        }
+        for (Request *r : users)
             if (r->split) {
                 cudaFreeAsync(r->d_grade, s);
                 cudaFreeAsync(r->d_mapped, s);
                 r->d_grade = nullptr;
                 r->d_mapped = nullptr;
             }
-        }
         cudaStreamSynchronize(s);
         for (auto &o : outs) pool.release(o.first, o.second);
         const double t = now_ms();
@@ -497,22 +553,43 @@ struct Server {
                 retired_cols.emplace_back(r->c0, std::max<int64_t>(r->m, 1));
                 pool.release(r->reg, r->reg_ints);
                 slots[r->slot] = nullptr;
-                if (r->split && r->phase == 0) {
-                    // the D part next, ahead of every queued request
-                    r->phase = 1;
-                    r->dual = false;
-                    r->listed = false;
-                    r->c0 = r->reg = -1;
-                    r->slot = -1;
-                    pending.push_front(r);
-                    continue;
+                r->slot = -1;
+                if (r->split && !r->user) r->part_done = true;
+            }
+            for (Request *r : users) {
+                if (r->part) {
+                    delete r->part;
+                    r->part = nullptr;
                 }
                 r->t_done = t;
+                if (r->split) r->sweeps = (int)(sweeps - r->sweep0);
                 r->done = true;
                 completed++;
             }
         }
         cv_done.notify_all();
+    }
+
+    // After a sweep: the D part of every split request whose D' part has
+    // been swept once, at the head of the queue.
+    void spawn_parts() {
+        std::lock_guard<std::mutex> lk(mu);
+        for (Request *u : all_split)
+            if (!u->part && u->parts_left == 2 && (u->part_done || (u->slot >= 0 && slots[u->slot] == u && u->listed))) {
+                Request *b = new Request();
+                b->m = u->m;
+                b->nnz = u->nnz;
+                b->d_buf = u->d_buf;  // freed by the D part's admission
+                u->d_buf = nullptr;
+                b->split = true;
+                b->user = u;
+                b->ticket = -1;
+                b->t_submit = u->t_submit;
+                u->part = b;
+                pending.push_front(b);
+            }
+        all_split.erase(std::remove_if(all_split.begin(), all_split.end(), [](Request *u) { return u->part != nullptr; }),
+                        all_split.end());
     }
 
     // Moves the pool region of request r to one twice as large.
@@ -609,6 +686,13 @@ struct Server {
                         std::lock_guard<std::mutex> lk(mu);
                         Request *r = pending.front();
                         pending.pop_front();
+                        if (r->user) {  // a split request's D part: the request fails
+                            Request *u = r->user;
+                            if (r->d_buf) cudaFree(r->d_buf);
+                            u->part = nullptr;
+                            delete r;
+                            r = u;
+                        }
                         r->status = OPH_ERR_OOM;
                         r->done = true;
                         cv_done.notify_all();
@@ -690,6 +774,7 @@ struct Server {
                 if (slots[b] && slots[b]->listed && h_ireps[b] == 0 && !h_iover[b]) done.push_back(slots[b]);
             const double t_swept = now_ms();
             retire_all(done);
+            spawn_parts();
             if (trace)
                 fprintf(stderr, "server sweep %lld: span %lld cols, %d active, %lld admitted, %zu retired | "
                                 "round %.3f ms (sweep+admit %.3f, retire %.3f)\n",
@@ -879,8 +964,8 @@ int submit_copy(oph_server *sv, int64_t m, int64_t nnz, const int64_t *colptr, c
         if (dual_grade(s, sv->ctx->sm_count, cp, rw, m, nnz, OPH_DUAL_AUTO, gtmp, &choice, &bad_g, nullptr) != OPH_OK ||
             bad_g)
             choice = DUAL_CHOICE_D;
-        // a split request keeps its grading, and room for its D' part's lows
-        if (choice == DUAL_CHOICE_SPLIT && cudaMallocAsync(&mapped, sizeof(int32_t) * 2 * m, s) != cudaSuccess) {
+        // a split request keeps its grading, and room for its parts' lows
+        if (choice == DUAL_CHOICE_SPLIT && cudaMallocAsync(&mapped, sizeof(int32_t) * 3 * m, s) != cudaSuccess) {
             cudaGetLastError();
             choice = DUAL_CHOICE_D;
         }
@@ -905,6 +990,7 @@ int submit_copy(oph_server *sv, int64_t m, int64_t nnz, const int64_t *colptr, c
     r->d_buf = buf;
     r->dual = choice != DUAL_CHOICE_D;
     r->split = choice == DUAL_CHOICE_SPLIT;
+    r->parts_left = r->split ? 2 : 0;
     r->d_grade = gtmp;
     r->d_mapped = mapped;
     r->t_submit = now_ms();
@@ -1018,6 +1104,17 @@ __attribute__((visibility("default"))) int oph_server_destroy(oph_server *sv) {
     sv->cv_work.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
     cudaSetDevice(sv->ctx->device);
+    // internal D parts of split requests left by a failure
+    for (Request *r : sv->slots)
+        if (r && r->user) {
+            if (r->d_buf) cudaFree(r->d_buf);
+            delete r;
+        }
+    for (Request *r : sv->pending)
+        if (r->user) {
+            if (r->d_buf) cudaFree(r->d_buf);
+            delete r;
+        }
     for (auto &kv : sv->all) {
         for (void *p : {kv.second->d_buf, kv.second->d_grade, static_cast<void *>(kv.second->d_mapped)})
             if (p) cudaFree(p);
