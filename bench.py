@@ -739,21 +739,30 @@ def run_serve(args, local, pool, cores, count, reqs_async):
     total_m = sum(bm.m for _, bm in reqs)
     log(f"serve: {n} requests, {total_m} columns")
     torch.cuda.set_device(local)
-    # plain: one at a time, service time of each
+    # plain: one at a time, service time of each; two passes over the
+    # stream, the faster one kept (the first also grows the context's
+    # buffers to the largest request)
     ctx = api.Context(local)
     for _, bm in reqs[:3]:
         ctx.reduce(bm, "pms")
-    service, plain_low, plain_ess = [], [], []
+    passes, plain_low, plain_ess = [], [], []
     with ClockSampler(local) as clocks_plain:
-        for _, bm in reqs:
-            t0 = time.perf_counter()
-            low, ess, _ = ctx.reduce(bm, "pms")
-            service.append(time.perf_counter() - t0)
-            plain_low.append(low)
-            plain_ess.append(ess)
+        for p in range(2):
+            service = []
+            for _, bm in reqs:
+                t0 = time.perf_counter()
+                low, ess, _ = ctx.reduce(bm, "pms")
+                service.append(time.perf_counter() - t0)
+                if p == 0:
+                    plain_low.append(low)
+                    plain_ess.append(ess)
+            passes.append(np.array(service))
     ctx.close()
-    service = np.array(service)
+    service = min(passes, key=lambda v: v.sum())
     plain_rate = n / service.sum()
+    kinds = sorted({k for k, _ in reqs})
+    log("serve: plain passes (ms) " + ", ".join(f"{1e3 * v.sum():.1f}" for v in passes) + " | by kind: " +
+        ", ".join(f"{kd} {1e3 * sum(t for (k, _), t in zip(reqs, service) if k == kd):.1f}" for kd in kinds))
 
     srv = api.Server(local, budget_bytes=SERVE["budget_bytes"], max_active=4096)
     for _, bm in reqs[:3]:  # warm-up
@@ -821,7 +830,9 @@ def run_serve(args, local, pool, cores, count, reqs_async):
                    "m_range": [SERVE["m_lo"], SERVE["m_hi"]], "budget_gb": SERVE["budget_bytes"] / (1 << 30),
                    "kinds": sorted({k for k, _ in reqs}), "seed": SERVE["seed"]},
         "plain_sequential": {"complexes_per_s": plain_rate, "mean_service_ms": 1e3 * service.mean(),
-                             "api": "oph_reduce (host CSC in, host low/ess out), one request at a time",
+                             "passes_ms": [1e3 * float(v.sum()) for v in passes],
+                             "api": "oph_reduce (host CSC in, host low/ess out), one request at a time; "
+                                    "the faster of two passes over the stream",
                              "clocks": clocks_plain.summary()},
         "served_over_plain_at_saturation": best["served_per_s"] / plain_rate,
         "p50_ms_at_saturation": best["p50_ms"], "p99_ms_at_saturation": best["p99_ms"],
