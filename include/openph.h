@@ -154,7 +154,12 @@ int oph_reduce_batch_device(oph_context *ctx, int algo, int32_t count, const int
  * max_active requests are on the device at once.  Each request is reduced on
  * the matrix a single-matrix pms reduction would choose for it (OPH_DUAL_AUTO
  * below: a Rips-like request through its anti-transpose, built at
- * admission), and the results are identical to that reduction's.
+ * admission; a request split by block as two parts side by side, the D part
+ * joining after the D' part's first sweep), and the results are identical to
+ * that reduction's.  A chain of additions in the bitmap tiers stops after 128
+ * additions a sweep (environment variable OPH_SERVE_CHAIN_CAP, read at
+ * creation; 0 for no limit) and goes on in the next sweep, so no sweep of
+ * every active request waits on one long chain.
  */
 typedef struct oph_server oph_server;
 

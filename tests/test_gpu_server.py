@@ -39,6 +39,25 @@ def test_results_same_alone_and_in_the_mix(cuda_lib):
         np.testing.assert_array_equal(em, want_ess)
 
 
+@pytest.mark.parametrize("cap", ["1", "3", "0"])
+def test_chain_cap(cuda_lib, monkeypatch, cap):
+    """Bitmap-tier chains cut after every `cap` additions (0: never) and taken
+    up again in later sweeps: the same results, on requests whose long
+    columns go through the bitmap tiers (a torus through its anti-transpose,
+    a lower-star image and a 3-D volume on D)."""
+    from cases import lower_star_volume
+    monkeypatch.setenv("OPH_SERVE_CHAIN_CAP", cap)
+    reqs = [cx.rips_torus(400, 150_000, seed=61), cx.lower_star_image(120, 120, seed=62, sigma=6.0),
+            lower_star_volume(12, 63), cx.rips_cube(40, seed=64)]
+    with Server(0, budget_bytes=4 << 30, max_active=8) as srv:
+        tickets = [srv.submit(bm) for bm in reqs]
+        res = [srv.wait(t) for t in tickets]
+    for bm, (low, ess, info) in zip(reqs, res):
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
+
+
 def test_arrivals_while_running(cuda_lib):
     """Requests submitted from another thread while earlier ones are on the
     device are folded into the running batch."""
