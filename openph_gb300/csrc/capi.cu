@@ -496,6 +496,8 @@ static int batch_core(oph_context *ctx, int algo, int32_t count, const int64_t *
     w.colptr = d_colptr;
     w.rows = d_rows_g;
     w.checked = true;
+    w.inst_off = d_col_off;
+    w.inst_count = count;
     Outputs o;
     o.low = d_low;
     o.ess = d_ess;

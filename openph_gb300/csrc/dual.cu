@@ -609,6 +609,303 @@ __global__ void __launch_bounds__(LS_THREADS) k_dual_sort_long(const int64_t *__
     }
 }
 
+// ------------------------------------------- the transpose of a batch
+// A block-diagonal matrix (instance b in columns, and rows, [off[b],
+// off[b+1])) whose instances have at most IT_COLS columns, at most IT_ROWS
+// distinct rows and D' columns of at most IT_MAXCOL rows (batches of small
+// complexes) is transposed per instance with every count and cursor in
+// shared memory, where the general transpose above takes a global atomic
+// per entry and a sort per column after its scatter.  An instance's D'
+// columns are contiguous and so are their entries, which start after the
+// entries of every later instance (nnz - colptr[off[b+1]]): no global scan.
+// k_dual_inst_a, a CTA per instance:
+//   rows      the instance's rows marked in a bitmap of its columns, ranked
+//             by popcount: each distinct row q gets a dense index d(q)
+//             (a Rips filtration interleaves its triangles, never rows, with
+//             its edges, so rows are few but spread over the columns);
+//   count     entries per dense row (shared atomics), their exclusive prefix
+//             in D' order (descending q): off[d];
+//   headers   every D' column of the instance: segment, header, bucket of
+//             D's column in the reversed position, low -1 if empty;
+//   chunks    whole columns of at most IT_CAP entries (chunk k: the columns
+//             whose entries start in [k IT_SPAN, (k+1) IT_SPAN)), each
+//             described in a global list;
+//   partition every entry (d, q, column) into its chunk's range of a
+//             scratch array (shared cursors).
+// k_dual_inst_b, a CTA per chunk (of every instance at once): its entries
+// into shared memory, counted and placed per column (the chunk's columns
+// are contiguous: its count prefix in D' order gives their starts), every
+// column sorted by a warp there, then written out with its low.
+// An instance outside those bounds sets *fail and the caller builds the
+// whole store with the general transpose instead.
+constexpr int IT_COLS = 1 << 19, IT_WORDS = IT_COLS / 32, IT_ROWS = 8192, IT_CAP = 3072, IT_MAXCOL = 512,
+              IT_CHUNKS = 512;
+constexpr int IT_SPAN = IT_CAP - IT_MAXCOL;
+constexpr int ITA_THREADS = 1024, ITB_THREADS = 256;
+constexpr size_t ITA_SMEM = sizeof(uint32_t) * IT_WORDS + sizeof(uint16_t) * IT_WORDS + sizeof(int) * IT_ROWS +
+                            sizeof(int) * 5 * IT_CHUNKS;
+constexpr size_t ITB_SMEM = sizeof(unsigned long long) * IT_CAP + sizeof(int) * (3 * IT_CAP + 1);
+struct ItChunk {
+    int b, lo, hi, dmin, dmax, pad[3];
+};
+// a scratch entry: dense row (13 bits) | q (19 bits) | column of the instance (32 bits)
+__device__ __forceinline__ unsigned long long it_pack(int d, int q, int jl) {
+    return ((unsigned long long)(((unsigned)d << 19) | (unsigned)q) << 32) | (unsigned)jl;
+}
+
+__global__ void __launch_bounds__(ITA_THREADS, 1)
+    k_dual_inst_a(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m, int64_t nnz,
+                  const int64_t *__restrict__ inst_off, int count, int *__restrict__ pool, int64_t *__restrict__ seg,
+                  int32_t *__restrict__ low, int8_t *__restrict__ dim, unsigned long long *__restrict__ scratch,
+                  ItChunk *__restrict__ chunks, int *nchunks, int *fail) {
+    extern __shared__ __align__(16) unsigned char ita_smem[];  // ITA_SMEM bytes
+    uint32_t *bits = reinterpret_cast<uint32_t *>(ita_smem);             // IT_WORDS
+    uint16_t *wrank = reinterpret_cast<uint16_t *>(bits + IT_WORDS);     // IT_WORDS: set bits in earlier words
+    int *off = reinterpret_cast<int *>(wrank + IT_WORDS);                // IT_ROWS: counts, then prefixes
+    int *c_lo = off + IT_ROWS, *c_hi = c_lo + IT_CHUNKS, *c_dmin = c_hi + IT_CHUNKS, *c_dmax = c_dmin + IT_CHUNKS,
+        *c_cur = c_dmax + IT_CHUNKS;
+    __shared__ long long red[33];
+    __shared__ int s_bad, s_base, s_rows;
+    const int tid = threadIdx.x;
+    constexpr int T = ITA_THREADS;
+    for (int b = blockIdx.x; b < count; b += gridDim.x) {
+        const int64_t o0 = inst_off[b], o1 = inst_off[b + 1], mb = o1 - o0;
+        const int64_t e0 = colptr[o0], e1 = colptr[o1];
+        const int total = (int)(e1 - e0);
+        const int64_t A = nnz - e1;
+        if (tid == 0) s_bad = (mb > IT_COLS || (e1 - e0) >= (1ll << 30)) ? 1 : 0;
+        for (int w = tid; w < IT_WORDS; w += T) bits[w] = 0;
+        for (int d = tid; d < IT_ROWS; d += T) off[d] = 0;
+        __syncthreads();
+        if (s_bad) {
+            if (tid == 0) atomicExch(fail, 1);
+            __syncthreads();
+            continue;  // the whole store is rebuilt by the general transpose
+        }
+        // the rows that occur, four loads in flight per thread
+        for (int64_t e = e0 + tid; e < e1; e += 4 * T) {
+            int64_t q[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) q[u] = e + u * T < e1 ? (int64_t)rows[e + u * T] - o0 : -2;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (q[u] == -2) continue;
+                if (q[u] < 0 || q[u] >= mb) s_bad = 1;
+                else atomicOr(&bits[q[u] >> 5], 1u << (q[u] & 31));
+            }
+        }
+        __syncthreads();
+        {  // exclusive popcount prefix over the words: thread t holds words [PER t, PER (t+1))
+            constexpr int PER = IT_WORDS / T;
+            int v[PER], sum = 0;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                v[k] = __popc(bits[PER * tid + k]);
+                sum += v[k];
+            }
+            int run = (int)block_exclusive(sum, red);
+            if (tid == T - 1) s_rows = run + sum;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                wrank[PER * tid + k] = (uint16_t)min(run, 65535);
+                run += v[k];
+            }
+        }
+        __syncthreads();
+        const int D = s_rows;
+        if (s_bad || D > IT_ROWS) {
+            if (tid == 0) atomicExch(fail, 1);
+            __syncthreads();
+            continue;
+        }
+        // the dense index of row q: its rank among the rows that occur
+        auto dense = [&](int64_t q) -> int {
+            return wrank[q >> 5] + __popc(bits[q >> 5] & ((1u << (q & 31)) - 1u));
+        };
+        for (int64_t e = e0 + tid; e < e1; e += 4 * T) {
+            int d[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) d[u] = e + u * T < e1 ? dense((int64_t)rows[e + u * T] - o0) : -1;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (d[u] >= 0) atomicAdd(&off[d[u]], 1);
+        }
+        __syncthreads();
+        {  // exclusive prefix in D' order (descending d): thread t holds d in [IT_ROWS - PER (t+1), IT_ROWS - PER t)
+            constexpr int PER = IT_ROWS / T;
+            const int dtop = IT_ROWS - PER * tid;
+            int v[PER], sum = 0;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                v[k] = off[dtop - 1 - k];
+                sum += v[k];
+                if (v[k] > IT_MAXCOL) s_bad = 1;
+            }
+            int run = (int)block_exclusive(sum, red);
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                off[dtop - 1 - k] = run;
+                run += v[k];
+            }
+        }
+        __syncthreads();
+        const int K = total / IT_SPAN + 1;
+        if (s_bad || K > IT_CHUNKS) {
+            if (tid == 0) atomicExch(fail, 1);
+            __syncthreads();
+            continue;
+        }
+        // entries of the columns of dense rows >= d: off[d - 1] (total for d = 0)
+        auto above = [&](int d) -> int { return d == 0 ? total : off[d - 1]; };
+        for (int64_t q = tid; q < mb; q += T) {
+            const int64_t c = m - 1 - (o0 + q);
+            const int d = dense(q);
+            const bool occ = (bits[q >> 5] >> (q & 31)) & 1u;
+            // a row that occurs: its own prefix; one that does not: the
+            // entries of the rows above it, those of dense index >= d
+            // (above(D) = 0: the prefix past the last row that occurs)
+            const int rel = occ ? off[d] : above(d);
+            const int n = occ ? above(d) - off[d] : 0;
+            const int64_t a = A + rel;
+            const int64_t s = seg_start(c, a), e = seg_start(c + 1, a + n);
+            *reinterpret_cast<int4 *>(pool + s) = make_int4(n, (int)(e - s - SEG_HDR), 0, 0);
+            seg[c] = s;
+            const int64_t nd = colptr[o0 + q + 1] - colptr[o0 + q];
+            dim[c] = (int8_t)(nd - 1 > 126 ? 126 : nd - 1);
+            if (n == 0) low[c] = -1;
+        }
+        for (int k = tid; k < K; k += T) {
+            c_lo[k] = INT_MAX;
+            c_hi[k] = -1;
+            c_dmin[k] = INT_MAX;
+            c_dmax[k] = -1;
+            c_cur[k] = 0;
+        }
+        __syncthreads();
+        for (int d = tid; d < D; d += T) {
+            const int k = off[d] / IT_SPAN;
+            atomicMin(&c_lo[k], off[d]);
+            atomicMax(&c_hi[k], above(d));
+            atomicMin(&c_dmin[k], d);
+            atomicMax(&c_dmax[k], d);
+        }
+        if (tid == 0) s_base = atomicAdd(nchunks, K);
+        __syncthreads();
+        for (int k = tid; k < K; k += T) {
+            ItChunk ch;
+            ch.b = b;
+            ch.lo = c_hi[k] < 0 ? -1 : c_lo[k];  // -1: no column starts in this span
+            ch.hi = c_hi[k];
+            ch.dmin = c_dmin[k];
+            ch.dmax = c_dmax[k];
+            ch.pad[0] = ch.pad[1] = ch.pad[2] = 0;
+            chunks[s_base + k] = ch;
+        }
+        // partition: every entry into its chunk's range of the scratch, four
+        // columns a thread at a time (their offsets, then their rows, in flight)
+        for (int64_t j0 = tid; j0 < mb; j0 += 4 * T) {
+            int64_t lo[4], hi[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int64_t jl = j0 + u * T;
+                lo[u] = jl < mb ? colptr[o0 + jl] : 0;
+                hi[u] = jl < mb ? colptr[o0 + jl + 1] : 0;
+            }
+            int qs[4][MAXC - 1];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int t = 0; t < MAXC - 1; t++)
+                    qs[u][t] = lo[u] + t < hi[u] ? (int)((int64_t)rows[lo[u] + t] - o0) : -1;
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int t = 0; t < MAXC - 1; t++) {
+                    if (qs[u][t] < 0) continue;
+                    const int d = dense(qs[u][t]);
+                    const int k = off[d] / IT_SPAN;
+                    const int slot = atomicAdd(&c_cur[k], 1);
+                    scratch[A + c_lo[k] + slot] = it_pack(d, qs[u][t], (int)(j0 + u * T));
+                }
+        }
+        __syncthreads();  // the shared arrays are reset for the next instance
+    }
+}
+
+__global__ void __launch_bounds__(ITB_THREADS, 3)
+    k_dual_inst_b(int64_t m, int64_t nnz, const int64_t *__restrict__ colptr, const int64_t *__restrict__ inst_off,
+                  int *__restrict__ pool, int32_t *__restrict__ low, const unsigned long long *__restrict__ scratch,
+                  const ItChunk *__restrict__ chunks, const int *nchunks, int roff) {
+    extern __shared__ __align__(16) unsigned char itb_smem[];  // ITB_SMEM bytes
+    unsigned long long *pairs = reinterpret_cast<unsigned long long *>(itb_smem);  // IT_CAP
+    int *placed = reinterpret_cast<int *>(pairs + IT_CAP);                       // IT_CAP
+    int *start = placed + IT_CAP;                                                // IT_CAP + 1
+    int *qof = start + IT_CAP + 1;                                               // IT_CAP
+    __shared__ long long red[33];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    constexpr int T = ITB_THREADS;
+    const int nch = *nchunks;
+    for (int idx = blockIdx.x; idx < nch; idx += gridDim.x) {
+        const ItChunk ch = chunks[idx];
+        if (ch.lo < 0) continue;  // uniform: every thread read the same descriptor
+        const int64_t o0 = inst_off[ch.b];
+        const int64_t A = nnz - colptr[inst_off[ch.b + 1]];
+        const int len = ch.hi - ch.lo, span = ch.dmax - ch.dmin + 1;
+        if (len > IT_CAP || span > IT_CAP) continue;  // not reached: each column of the chunk holds a row
+        for (int i = tid; i <= span; i += T) start[i] = 0;
+        __syncthreads();
+        for (int i = tid; i < len; i += T) {
+            const unsigned long long pr = scratch[A + ch.lo + i];
+            pairs[i] = pr;
+            const int x = (int)(pr >> 51) - ch.dmin;
+            atomicAdd(&start[x], 1);
+            qof[x] = (int)((pr >> 32) & ((1u << 19) - 1u));
+        }
+        __syncthreads();
+        {  // exclusive prefix in D' order (descending d): slot i holds d = dmax - i
+            constexpr int PER = IT_CAP / T;
+            int v[PER], sum = 0;
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                const int i = tid * PER + k;
+                v[k] = i < span ? start[span - 1 - i] : 0;
+                sum += v[k];
+            }
+            int run = (int)block_exclusive(sum, red);
+#pragma unroll
+            for (int k = 0; k < PER; k++) {
+                const int i = tid * PER + k;
+                if (i < span) start[span - 1 - i] = run;
+                run += v[k];
+            }
+        }
+        __syncthreads();
+        // each entry into its column's slots (start[] moves to each column's end)
+        for (int i = tid; i < len; i += T) {
+            const unsigned long long pr = pairs[i];
+            const int x = (int)(pr >> 51) - ch.dmin, jl = (int)(pr & 0xffffffffu);
+            const int slot = atomicAdd(&start[x], 1);
+            placed[slot] = roff + (int)(m - 1 - (o0 + jl));
+        }
+        __syncthreads();
+        // a warp per column: its slots [end of the column before it in D' order, its end)
+        for (int x = span - 1 - wid; x >= 0; x -= T / 32) {
+            const int s0 = x == span - 1 ? 0 : start[x + 1];
+            const int n = start[x] - s0;
+            if (n == 0) continue;
+            int *R = placed + s0;
+            const int top = n <= 32 ? warp_sort_column<1>(R, n)
+                                    : n <= 128 ? warp_sort_column<4>(R, n) : warp_sort_column<16>(R, n);
+            __syncwarp();
+            const int64_t c = m - 1 - (o0 + qof[x]);
+            int *dst = pool + seg_start(c, A + ch.lo + s0) + SEG_HDR;
+            for (int t = lane; t < n; t += 32) dst[t] = R[t];
+            if (lane == 0) low[c] = top;
+        }
+        __syncthreads();
+    }
+}
+
 // per row i of D' (column j = m-1-i of D): the pivot record reset, left[i] =
 // m-1-low_D(j) (or -1 for an empty column), beta[left] = the largest row
 __global__ void k_dual_rec(const int64_t *__restrict__ colptr, const int32_t *__restrict__ rows, int64_t m,
@@ -856,6 +1153,46 @@ int dual_build_store(cudaStream_t s, int sm_count, const int64_t *colptr, const 
     return OPH_OK;
 }
 
+// The transpose of a batch's instances (k_dual_inst_a, k_dual_inst_b) into
+// wd's store, then the records; *done false when an instance is out of
+// bounds (the caller then runs dual_build_store, which rewrites everything).
+static int dual_build_store_inst(Context *ctx, const Work &w, Work &wd, bool *done) {
+    cudaStream_t s = ctx->stream;
+    *done = false;
+    const int64_t max_chunks = w.nnz / IT_SPAN + w.inst_count + 1;
+    unsigned long long *scratch =
+        (unsigned long long *)ctx_alloc(ctx, S_DTEMP, sizeof(unsigned long long) * (w.nnz > 0 ? w.nnz : 1));
+    char *meta = (char *)ctx_alloc(ctx, S_DCOLPTR, 256 + sizeof(ItChunk) * max_chunks);
+    if (!scratch || !meta) return OPH_ERR_OOM;
+    int *fail = (int *)meta, *nchunks = fail + 1;
+    ItChunk *chunks = reinterpret_cast<ItChunk *>(meta + 256);
+    if (cudaFuncSetAttribute(k_dual_inst_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ITA_SMEM) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_dual_inst_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ITB_SMEM) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return OPH_OK;
+    }
+    OPH_CUDA_TRY(cudaMemsetAsync(meta, 0, 8, s));
+    const int ga = std::max(1, std::min(w.inst_count, ctx->sm_count));
+    k_dual_inst_a<<<ga, ITA_THREADS, ITA_SMEM, s>>>(w.colptr, w.rows, w.m, w.nnz, w.inst_off, w.inst_count, wd.pool, wd.seg,
+                                             wd.low, wd.dim, scratch, chunks, nchunks, fail);
+    k_dual_inst_b<<<4 * ctx->sm_count, ITB_THREADS, ITB_SMEM, s>>>(w.m, w.nnz, w.colptr, w.inst_off, wd.pool, wd.low,
+                                                             scratch, chunks, nchunks, 0);
+    ctx->launches += 2;
+    OPH_CUDA_TRY(cudaGetLastError());
+    int h_fail = 0;
+    OPH_CUDA_TRY(cudaMemcpyAsync(&h_fail, fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+    OPH_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_fail) return OPH_OK;
+    OPH_CUDA_TRY(cudaMemsetAsync(wd.beta, 0xff, sizeof(int32_t) * w.m, s));
+    k_dual_rec<<<grid_of(ctx, w.m), 256, 0, s>>>(w.colptr, w.rows, w.m, wd.rec, wd.beta, 0);
+    ctx->launches++;
+    OPH_CUDA_TRY(cudaGetLastError());
+    *done = true;
+    return OPH_OK;
+}
+
 int dual_setup(Context *ctx, const Work &w, Work &wd) {
     wd = w;
     wd.ascending = true;
@@ -865,6 +1202,11 @@ int dual_setup(Context *ctx, const Work &w, Work &wd) {
     int rc = init_store(ctx, wd);
     if (rc) return rc;
     if (w.m == 0) return OPH_OK;
+    if (w.inst_off && w.inst_count > 0 && !getenv("OPH_NO_INST_TRANSPOSE")) {
+        bool done = false;
+        if ((rc = dual_build_store_inst(ctx, w, wd, &done))) return rc;
+        if (done) return OPH_OK;
+    }
     void *tmp = ctx_alloc(ctx, S_DSORT, dual_tmp_bytes(w.m, w.nnz));
     if (!tmp) return OPH_ERR_OOM;
     return dual_build_store(ctx->stream, ctx->sm_count, w.colptr, w.rows, w.m, w.nnz, wd.pool, 0, 0, wd.seg, wd.low,

@@ -51,6 +51,8 @@ struct Work {
     bool ascending = false;           // pms: buckets in ascending order (the anti-transpose)
     bool checked = false;             // colptr/rows already passed the structural check
     const uint8_t *preclear = nullptr;  // pms: columns cleared before Phase 0 (m bytes), or none
+    const int64_t *inst_off = nullptr;  // a batch: its instances' column offsets (device, inst_count + 1)
+    int inst_count = 0;
 };
 
 struct Context;

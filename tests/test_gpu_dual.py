@@ -176,6 +176,58 @@ def test_batch(dctx, mode):
         np.testing.assert_array_equal(ess, want_ess)
 
 
+def star(n_leaves):
+    """A vertex joined to n_leaves others: its column of D' holds n_leaves rows."""
+    from openph_gb300.complexes import BoundaryMatrix
+    return BoundaryMatrix.from_columns([[] for _ in range(n_leaves + 1)] + [[0, i] for i in range(1, n_leaves + 1)])
+
+
+@pytest.mark.parametrize("odd", ["window", "wide_column", "none"])
+def test_batch_transpose_fallback(dctx, odd):
+    """A batch whose instances all fit the per-instance transpose (rows within
+    16,384 of their first column, D' columns of at most 512 rows) takes it;
+    one instance outside those bounds (a 90x90 lower-star image, 24K vertices
+    and edges; a vertex of 600 edges) sends the whole batch to the general
+    transpose.  Every instance equal to the oracle's twist either way."""
+    mats = [cx.rips_mixed(30, seed=3), cx.rips_mixed(12, seed=5), star(40)]
+    if odd == "window":
+        mats.insert(1, cx.lower_star_image(90, 90, seed=4, sigma=3.0))
+    elif odd == "wide_column":
+        mats.insert(1, star(600))
+    dctx.set_dual("always")
+    lows, esss, info = dctx.reduce_batch(mats, "pms")
+    dctx.set_dual("auto")
+    assert info["dual"] == 1
+    for bm, low, ess in zip(mats, lows, esss):
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_batch_transpose_both_ways(dctx, monkeypatch):
+    """64 instances of the batched mix through the per-instance transpose and
+    through the general one (OPH_NO_INST_TRANSPOSE): both equal to the oracle,
+    and the first launches fewer set-up kernels (it was taken, not fallen back
+    from)."""
+    col_off, colptr, rows, npts, _ = cx.rips_mixed_batch(64, seed=11)
+    jobs = [(colptr[col_off[b]:col_off[b + 1] + 1] - colptr[col_off[b]],
+             rows[colptr[col_off[b]]:colptr[col_off[b + 1]]]) for b in range(64)]
+    want = oracle.twist_many(jobs)
+    launches = []
+    for inst in (True, False):
+        if not inst:
+            monkeypatch.setenv("OPH_NO_INST_TRANSPOSE", "1")
+        dctx.set_profile(True)
+        low, ess, info = dctx.reduce_batch_packed(col_off, colptr, rows, "pms")
+        launches.append(dctx.last_profile()["kernel_launches"])
+        dctx.set_profile(False)
+        assert info["dual"] == 1
+        for b in range(64):
+            np.testing.assert_array_equal(low[col_off[b]:col_off[b + 1]], want[b][0])
+            np.testing.assert_array_equal(ess[col_off[b]:col_off[b + 1]], want[b][1])
+    assert launches[0] < launches[1], launches
+
+
 def test_drop_in_call_without_trackers(cuda_lib):
     """openph() with no tracker outputs takes D' on a large Rips complex
     (1-based COO in, 1-based lows out); with trackers it reduces D."""
