@@ -2271,6 +2271,83 @@ __global__ void k_iota(int32_t *p, int64_t n) {
         p[i] = (int32_t)i;
 }
 
+// The first Phase I list: the columns with a low, in order.  A zero column
+// never adds, repeats a low or becomes a pivot, so Phase I has nothing to do
+// for it (on the anti-transpose of a Rips complex that is every column of
+// the top dimension, most of the matrix).  Per tile of P1_TILE columns:
+// the count, their exclusive scan (one block), then the ordered scatter.
+__global__ void __launch_bounds__(P1_THREADS) k_list_count(PmsArgs a, int64_t m) {
+    __shared__ int s_cnt;
+    for (int64_t t = blockIdx.x; t * P1_TILE < m; t += gridDim.x) {
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        const int64_t base = t * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
+        int c = 0;
+#pragma unroll
+        for (int k = 0; k < P1_ITEMS; k++) c += base + k < m && a.low[base + k] >= 0;
+        c = __reduce_add_sync(0xffffffffu, c);
+        if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_cnt, c);
+        __syncthreads();
+        if (threadIdx.x == 0) a.kagg[t] = s_cnt;
+        __syncthreads();
+    }
+}
+__global__ void k_list_scan(PmsArgs a, int64_t ntiles) {
+    __shared__ int wsum[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int carry = 0;
+    for (int64_t b0 = 0; b0 < ntiles; b0 += blockDim.x) {
+        const int64_t t = b0 + threadIdx.x;
+        const int v = t < ntiles ? a.kagg[t] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        int before = carry, total = 0;
+        for (int w = 0; w < nw; w++) {
+            if (w < wid) before += wsum[w];
+            total += wsum[w];
+        }
+        if (t < ntiles) a.kagg[t] = before + incl - v;
+        carry += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) a.st->ucount[0] = carry;
+}
+__global__ void __launch_bounds__(P1_THREADS) k_list_scatter(PmsArgs a, int64_t m) {
+    __shared__ int wsum[P1_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t t = blockIdx.x; t * P1_TILE < m; t += gridDim.x) {
+        const int64_t base = t * P1_TILE + (int64_t)threadIdx.x * P1_ITEMS;
+        unsigned keep = 0;
+        int cnt = 0;
+#pragma unroll
+        for (int k = 0; k < P1_ITEMS; k++)
+            if (base + k < m && a.low[base + k] >= 0) {
+                keep |= 1u << k;
+                cnt++;
+            }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += u;
+        }
+        if (lane == 31) wsum[wid] = incl;
+        __syncthreads();
+        int off = a.kagg[t] + incl - cnt;
+        for (int w = 0; w < wid; w++) off += wsum[w];
+#pragma unroll
+        for (int k = 0; k < P1_ITEMS; k++)
+            if (keep & (1u << k)) a.ulist[off++] = (int32_t)(base + k);
+        __syncthreads();  // wsum is rewritten by the next tile
+    }
+}
+
 // ---------------------------------------------------------------- trackers
 // The reference's essential estimate after an iteration (ess_hat,
 // src/cuda/algorithms/kernels.cu:114-124): a row that is some column's low,
@@ -2522,10 +2599,18 @@ int run_pms(Context *ctx, Work &w, oph_info *info) {
     a.bm = (uint32_t *)ctx_alloc(ctx, S_BITMAP, sizeof(uint32_t) * (size_t)a.bm_words * g.g3);
     if (!a.bm) return OPH_ERR_OOM;
     OPH_CUDA_TRY(cudaMemsetAsync(a.bm, 0, sizeof(uint32_t) * (size_t)a.bm_words * g.g3, s));
-    if (a.ulist) {
+    if (a.ulist && ctx->track) {
+        // the trackers count the zero columns that Phase I classifies
         k_iota<<<g.m, 256, 0, s>>>(a.ulist, m);
         const int mi = (int)m;
         OPH_CUDA_TRY(cudaMemcpyAsync(&w.st->ucount[0], &mi, sizeof(int), cudaMemcpyHostToDevice, s));
+    } else if (a.ulist) {
+        const int64_t lt = (m + P1_TILE - 1) / P1_TILE;
+        const int gl = (int)std::max<int64_t>(1, std::min<int64_t>(lt, (int64_t)ctx->sm_count * 8));
+        k_list_count<<<gl, P1_THREADS, 0, s>>>(a, m);
+        k_list_scan<<<1, 1024, 0, s>>>(a, lt);
+        k_list_scatter<<<gl, P1_THREADS, 0, s>>>(a, m);
+        ctx->launches += 2;
     }
 
     OPH_CUDA_TRY(cudaMemsetAsync(w.first, 0x7f, sizeof(int32_t) * m, s));
