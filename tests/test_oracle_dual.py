@@ -57,3 +57,37 @@ def test_rips_work_moves_to_the_vertices(built):
     _, _, st = oracle.twist(bm)
     _, _, st_d = oracle.standard(anti_transpose(bm))
     assert st_d["additions"] * 5 < st["additions"]
+
+
+def keep_columns(bm, mask):
+    """bm with the columns outside mask emptied."""
+    from openph_gb300.complexes import BoundaryMatrix
+    return BoundaryMatrix.from_columns([list(bm.column(j)) if mask[j] else [] for j in range(bm.m)])
+
+
+@pytest.mark.parametrize("case", ["lower_star", "volume", "random", "skeleton"])
+def test_blocks_reduce_independently(built, case):
+    """The per-block form the GPU path takes, on the oracle: the blocks of D
+    (a bucket's columns with their rows) reduce on their own, some on D' and
+    the others on D, the D part with the rows the D' part paired cleared
+    (left as zero columns); the merged lows and the ess drawn from them
+    equal twist on the whole of D."""
+    from cases import lower_star_volume
+    bm = {"lower_star": lambda: cx.lower_star_image(14, 11, seed=4, sigma=1.5),
+          "volume": lambda: lower_star_volume(5, 6),
+          "random": lambda: random_complex(16, 0.5, 0.6, seed=7),
+          "skeleton": lambda: simplex_skeleton(7, seed=8, max_dim=3)}[case]()
+    want, want_ess, _ = oracle.twist(bm)
+    dims = np.diff(bm.colptr) - 1
+    top = int(dims.max())
+    for dual_dims in ({top}, {top, top - 1}, {1}):
+        on_dual = np.isin(dims, list(dual_dims)) & (dims >= 1)
+        low_d, _, _ = oracle.standard(anti_transpose(keep_columns(bm, on_dual)))
+        mapped = mapped_back(low_d)
+        # twist's clearing across blocks: a row the D' part paired is zero
+        cleared = np.zeros(bm.m, bool)
+        cleared[mapped[mapped >= 0]] = True
+        low_p, _, _ = oracle.twist(keep_columns(bm, ~on_dual & ~cleared))
+        low = np.where(on_dual, mapped, low_p)
+        np.testing.assert_array_equal(low, want, err_msg=str(dual_dims))
+        np.testing.assert_array_equal(oracle.essential_from_low(low), want_ess, err_msg=str(dual_dims))
