@@ -571,11 +571,12 @@ struct Server {
     }
 
     // After a sweep: the D part of every split request whose D' part has
-    // been swept once, at the head of the queue.
+    // been swept once (or has converged already, in that sweep), at the
+    // head of the queue.
     void spawn_parts() {
         std::lock_guard<std::mutex> lk(mu);
         for (Request *u : all_split)
-            if (!u->part && u->parts_left == 2 && (u->part_done || (u->slot >= 0 && slots[u->slot] == u && u->listed))) {
+            if (!u->part && (u->part_done || (u->slot >= 0 && slots[u->slot] == u && u->listed))) {
                 Request *b = new Request();
                 b->m = u->m;
                 b->nnz = u->nnz;
