@@ -1162,8 +1162,8 @@ static int dual_build_store_inst(Context *ctx, const Work &w, Work &wd, bool *do
     const int64_t max_chunks = w.nnz / IT_SPAN + w.inst_count + 1;
     unsigned long long *scratch =
         (unsigned long long *)ctx_alloc(ctx, S_DTEMP, sizeof(unsigned long long) * (w.nnz > 0 ? w.nnz : 1));
-    char *meta = (char *)ctx_alloc(ctx, S_DCOLPTR, 256 + sizeof(ItChunk) * max_chunks);
-    if (!scratch || !meta) return OPH_ERR_OOM;
+    char *meta = scratch ? (char *)ctx_alloc(ctx, S_DCOLPTR, 256 + sizeof(ItChunk) * max_chunks) : nullptr;
+    if (!scratch || !meta) return OPH_OK;  // no room for its scratch: the general transpose
     int *fail = (int *)meta, *nchunks = fail + 1;
     ItChunk *chunks = reinterpret_cast<ItChunk *>(meta + 256);
     if (cudaFuncSetAttribute(k_dual_inst_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ITA_SMEM) !=
