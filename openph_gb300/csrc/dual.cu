@@ -369,39 +369,49 @@ __global__ void k_dual_finish(const int64_t *__restrict__ dcolptr, const int64_t
     }
 }
 
+// One stage of the network (SIZE, STRIDE as template arguments, so that
+// every index into v is a constant and v stays in registers), then the next.
+template <int K, int SIZE, int STRIDE>
+__device__ __forceinline__ void warp_sort_stage(int (&v)[K], int lane) {
+    if constexpr (STRIDE > 0) {
+        if constexpr (STRIDE < K) {
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const int q = k ^ STRIDE;
+                if (q > k) {
+                    const bool up = ((lane * K + k) & SIZE) == 0;
+                    const int x = v[k], y = v[q];
+                    v[k] = up ? min(x, y) : max(x, y);
+                    v[q] = up ? max(x, y) : min(x, y);
+                }
+            }
+        } else {
+            constexpr int LS = STRIDE / K;
+            const bool lower = (lane & LS) == 0;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                const bool up = ((lane * K + k) & SIZE) == 0;
+                const int o = __shfl_xor_sync(0xffffffffu, v[k], LS);
+                v[k] = (lower == up) ? min(v[k], o) : max(v[k], o);
+            }
+        }
+        warp_sort_stage<K, SIZE, STRIDE / 2>(v, lane);
+    }
+}
+template <int K, int SIZE>
+__device__ __forceinline__ void warp_sort_sizes(int (&v)[K], int lane) {
+    if constexpr (SIZE <= 32 * K) {
+        warp_sort_stage<K, SIZE, SIZE / 2>(v, lane);
+        warp_sort_sizes<K, SIZE * 2>(v, lane);
+    }
+}
+
 // Ascending order of the warp's 32 K values, lane l holding elements
 // l K .. l K + K - 1: a bitonic network, in registers within a lane and by
 // shuffles across lanes (K a power of two).
 template <int K>
 __device__ __forceinline__ void warp_sort_reg(int (&v)[K]) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int size = 2; size <= 32 * K; size <<= 1) {
-#pragma unroll
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            if (stride < K) {
-#pragma unroll
-                for (int k = 0; k < K; k++) {
-                    const int q = k ^ stride;
-                    if (q > k) {
-                        const bool up = ((lane * K + k) & size) == 0;
-                        const int x = v[k], y = v[q];
-                        v[k] = up ? min(x, y) : max(x, y);
-                        v[q] = up ? max(x, y) : min(x, y);
-                    }
-                }
-            } else {
-                const int ls = stride / K;
-                const bool lower = (lane & ls) == 0;
-#pragma unroll
-                for (int k = 0; k < K; k++) {
-                    const bool up = ((lane * K + k) & size) == 0;
-                    const int o = __shfl_xor_sync(0xffffffffu, v[k], ls);
-                    v[k] = (lower == up) ? min(v[k], o) : max(v[k], o);
-                }
-            }
-        }
-    }
+    warp_sort_sizes<K, 2>(v, threadIdx.x & 31);
 }
 
 // A column of n <= 32 K rows at R sorted by the warp; returns the low.
@@ -420,7 +430,15 @@ __device__ __forceinline__ int warp_sort_column(int *R, int n) {
     for (int k = 0; k + 1 < K; k++) asc &= v[k] <= v[k + 1];
     const int next_first = __shfl_down_sync(0xffffffffu, v[0], 1);
     if (lane < 31) asc &= v[K - 1] <= next_first;
-    if (__all_sync(0xffffffffu, asc)) return __shfl_sync(0xffffffffu, v[(n - 1) % K], (n - 1) / K);
+    if (__all_sync(0xffffffffu, asc)) {
+        // the last element: lane (n-1)/K, slot (n-1)%K (selected with
+        // constant indices, so that v stays in registers)
+        int last = INT_MIN;
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (k == (n - 1) % K) last = v[k];
+        return __shfl_sync(0xffffffffu, last, (n - 1) / K);
+    }
     warp_sort_reg<K>(v);
     int top = INT_MIN;
 #pragma unroll
