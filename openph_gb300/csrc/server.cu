@@ -178,7 +178,7 @@ __global__ void k_srv_init_cols(int64_t m, int64_t c0, int b, PmsArgs a) {
     }
 }
 
-// The Phase I list with this round's admitted column ranges merged in: the
+// The Phase I list with the column ranges admitted since the last sweep merged in: the
 // sorted list `in` (*in_count columns) and the ranges [r0[q], r0[q] + len of
 // q) (ascending, disjoint from every listed column; pre[q] = columns of the
 // ranges before q, pre[K] = all of them) into the sorted list `out`.
@@ -351,7 +351,7 @@ struct Server {
     SweepGrids g{};
     int *h_ireps = nullptr, *h_iover = nullptr;
     // the Phase I list: lp = which of its two arrays is current; the ranges
-    // admitted this round (for k_srv_merge), their device copy; the column
+    // admitted since the last sweep (for k_srv_merge), their device copy; the column
     // ranges of retired requests, free once a sweep has dropped them
     int lp = 0;
     std::vector<std::pair<int64_t, int64_t>> admitted_rng;
