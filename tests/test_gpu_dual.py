@@ -158,7 +158,7 @@ def test_dual_does_few_additions_on_rips(dctx):
     assert info["additions"] * 100 < st["additions"]
 
 
-@pytest.mark.parametrize("mode", ["always", "auto", "never"])
+@pytest.mark.parametrize("mode", ["always", "auto", "never", "blocks"])
 def test_batch(dctx, mode):
     from cases import empty_columns, triangle
     from openph_gb300.complexes import BoundaryMatrix
@@ -171,6 +171,21 @@ def test_batch(dctx, mode):
     for bm, low, ess in zip(mats, lows, esss):
         if bm.m == 0:
             continue
+        want, want_ess, _ = oracle.twist(bm)
+        np.testing.assert_array_equal(low, want)
+        np.testing.assert_array_equal(ess, want_ess)
+
+
+def test_batch_of_images_split_by_block(dctx):
+    """A batch of lower-star images reduced block by block (the batch's
+    triangles on its anti-transpose, built per instance, its edges on D):
+    every instance equal to the oracle's twist."""
+    mats = [cx.lower_star_image(h, w, seed=h * w, sigma=2.0) for h, w in ((12, 9), (20, 20), (7, 31), (33, 25))]
+    dctx.set_dual("blocks")
+    lows, esss, info = dctx.reduce_batch(mats, "pms")
+    dctx.set_dual("auto")
+    assert info["dual"] == 2
+    for bm, low, ess in zip(mats, lows, esss):
         want, want_ess, _ = oracle.twist(bm)
         np.testing.assert_array_equal(low, want)
         np.testing.assert_array_equal(ess, want_ess)
