@@ -18,6 +18,9 @@ columns), with two more objects beside it:
   server, served complexes/s and p50/p99 latency at saturation, against plain
   sequential pms on the same GPU; every request is checked against plain pms
   and against the oracle's twist.
+* ``variants``: the reference's six other algorithms (standard, twist,
+  ph_row and their parallel forms) and pms on one 128x128 lower-star image,
+  device time of one reduction each, every low checked against the oracle.
 
 For the headline, one step = one full reduction of the complex (set-up,
 sweeps, outputs) by the library's own choice of matrix.  ``value`` is
@@ -59,6 +62,7 @@ sys.path.insert(0, str(ROOT))
 WORKLOAD = {"name": "rips_torus", "points": 400, "target_m": 5_000_000, "seed": 2,
             "torus": {"R": 2.0, "r": 1.0, "sigma": 0.05}}
 BATCH = {"count": 4096, "seed": 4, "lo": 20, "hi": 120}
+VARIANTS = {"side": 128, "seed": 3}
 SERVE = {"requests": 160, "m_lo": 1_000, "m_hi": 2_000_000, "seed": 5, "budget_bytes": 150 * (1 << 30),
          "rates_x_plain": [0.5, 1, 2, 4, 8, 16, 32]}
 L2_FLUSH_BYTES = 512 << 20
@@ -154,6 +158,15 @@ def _job_twist_full(job):
     low, ess, st = oracle.twist(_bm(colptr, rows))
     st["wall"] = time.perf_counter() - t0
     return low, ess, st
+
+
+def _job_variants_oracle(job):
+    """The oracle's twist on the variants' image (regenerated here)."""
+    from openph_gb300 import complexes as cx
+    import oracle
+    side, seed = job
+    low, _, _ = oracle.twist(cx.lower_star_image(side, side, seed=seed))
+    return low
 
 
 def _job_fixed_full(job):
@@ -712,6 +725,33 @@ def run_batch(args, local, pool, cores, count, before_timing=None):
     }
 
 
+# ------------------------------------------------------------ variants
+def run_variants(local, pool):
+    """The six other algorithms of the reference (standard, twist, ph_row and
+    their parallel forms, each a single persistent GPU walker here) and pms
+    on one lower-star image, one reduction each after a warm-up, device time
+    of the call; every low checked against the oracle's twist."""
+    from openph_gb300 import api
+    from openph_gb300 import complexes as cx
+    side, seed = VARIANTS["side"], VARIANTS["seed"]
+    want_async = pool.apply_async(_job_variants_oracle, ((side, seed),))
+    bm = cx.lower_star_image(side, side, seed=seed)
+    out = {}
+    ctx = api.Context(local)
+    for algo in ("standard", "twist", "ph_row", "standard_parallel", "twist_parallel", "ph_row_parallel", "pms"):
+        ctx.reduce(bm, algo)
+        low, _, info = ctx.reduce(bm, algo)
+        out[algo] = {"device_ms": info["device_ms"], "cols_per_s": bm.m / (info["device_ms"] / 1e3),
+                     "low": low}
+    ctx.close()
+    want = want_async.get()
+    for algo, v in out.items():
+        v["low_equal_oracle"] = bool(np.array_equal(v.pop("low"), want))
+    log("variants: " + ", ".join(f"{a} {v['device_ms']:.1f} ms" for a, v in out.items()))
+    return {"matrix": f"lower-star image {side}x{side} (seed {seed}), {bm.m} columns", "algorithms": out,
+            "api": "oph_reduce (host CSC in), device time of the reduction (CUDA events)"}
+
+
 # --------------------------------------------------------------- serve
 def serve_jobs(count, seed):
     """Request mix: sizes log-uniform in [m_lo, m_hi], kind uniform over the
@@ -924,6 +964,10 @@ def run_ours(args, ws, rank, local):
             "frac_of_peak": ab["total"] / step_s / 1e9 / line["roofline"]["peak"],
             "definition": "4 (nnz + m + 1) + 4 m + 4 (|P| + |T| + |T xor P|) over the CPU twist's additions on "
                           "D, per reduction; not a bandwidth achieved (the anti-transpose avoids that work)"}
+    if args.workload == "all":
+        variants = run_variants(local, pool)
+        ok &= all(v["low_equal_oracle"] for v in variants["algorithms"].values())
+        line["variants"] = variants
     if serve_async is not None:
         serve = run_serve(args, local, pool, cores, args.count or SERVE["requests"], serve_async)
         ok &= serve["parity"]["served_equals_plain"] and serve["parity"]["oracle_equal"]
