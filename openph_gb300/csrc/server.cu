@@ -1082,9 +1082,10 @@ __attribute__((visibility("default"))) int oph_server_wait(oph_server *sv, int64
 __attribute__((visibility("default"))) int oph_server_stats(oph_server *sv, oph_server_counters *out) {
     if (!sv || !out) return OPH_ERR_BAD_INPUT;
     std::lock_guard<std::mutex> lk(sv->mu);
-    // requests as submitted: the D part of a split request is not one
+    // requests as submitted: a split request counts once, by its D' part
+    // while that is on the device, else by its D part
     int64_t active = 0, pending = 0;
-    for (auto *r : sv->slots) active += r != nullptr && !r->user;
+    for (auto *r : sv->slots) active += r != nullptr && (!r->user || r->user->slot < 0);
     for (auto *r : sv->pending) pending += !r->user;
     out->completed = sv->completed;
     out->pending = pending;
