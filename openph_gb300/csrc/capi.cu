@@ -221,7 +221,7 @@ static int reduce_split(Context *ctx, Work &w, oph_info *info) {
     w.preclear = nullptr;
     if (rc || (rc = split_merge(ctx, w.low, mapped, m))) return rc;
     info->sweeps = a.sweeps + b.sweeps;
-    info->num_iters = a.num_iters + b.num_iters;
+    info->num_iters = info->sweeps + 1;  // as for pms on one matrix: sweeps + 1
     info->additions = a.additions + b.additions;
     info->slots_moved = a.slots_moved + b.slots_moved;
     info->pool_bytes = std::max(a.pool_bytes, b.pool_bytes);
