@@ -91,3 +91,21 @@ def test_blocks_reduce_independently(built, case):
         low = np.where(on_dual, mapped, low_p)
         np.testing.assert_array_equal(low, want, err_msg=str(dual_dims))
         np.testing.assert_array_equal(oracle.essential_from_low(low), want_ess, err_msg=str(dual_dims))
+
+
+@pytest.mark.parametrize("keep", [0.0, 0.3, 1.0])
+def test_blocks_with_partial_clearing(built, keep):
+    """The served form clears only the rows its D' part has paired by the
+    time its D part starts: any subset of those clears (none, some, all)
+    leaves the D part's lows exact."""
+    bm = cx.lower_star_image(13, 12, seed=9, sigma=1.5)
+    want, _, _ = oracle.twist(bm)
+    dims = np.diff(bm.colptr) - 1
+    on_dual = dims == 2
+    mapped = mapped_back(oracle.standard(anti_transpose(keep_columns(bm, on_dual)))[0])
+    paired = mapped[mapped >= 0]
+    rng = np.random.default_rng(11)
+    cleared = np.zeros(bm.m, bool)
+    cleared[paired[rng.random(len(paired)) < keep]] = True
+    low_p, _, _ = oracle.twist(keep_columns(bm, ~on_dual & ~cleared))
+    np.testing.assert_array_equal(np.where(on_dual, mapped, low_p), want)
