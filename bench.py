@@ -18,6 +18,9 @@ columns), with two more objects beside it:
   server, served complexes/s and p50/p99 latency at saturation, against plain
   sequential pms on the same GPU; every request is checked against plain pms
   and against the oracle's twist.
+* ``configs``: the 50-point Rips cube (20,875 columns) and the 512x512
+  lower-star image (1,568,771 columns), pms device and end-to-end time, low
+  and ess checked against the oracle's twist.
 * ``variants``: the reference's six other algorithms (standard, twist,
   ph_row and their parallel forms) and pms on one 128x128 lower-star image,
   device time of one reduction each, every low checked against the oracle.
@@ -63,6 +66,7 @@ WORKLOAD = {"name": "rips_torus", "points": 400, "target_m": 5_000_000, "seed": 
             "torus": {"R": 2.0, "r": 1.0, "sigma": 0.05}}
 BATCH = {"count": 4096, "seed": 4, "lo": 20, "hi": 120}
 VARIANTS = {"side": 128, "seed": 3}
+CONFIGS = {"rips_cube_points": 50, "rips_cube_seed": 1, "lower_star_side": 512, "lower_star_seed": 3}
 SERVE = {"requests": 160, "m_lo": 1_000, "m_hi": 2_000_000, "seed": 5, "budget_bytes": 150 * (1 << 30),
          "rates_x_plain": [0.5, 1, 2, 4, 8, 16, 32]}
 L2_FLUSH_BYTES = 512 << 20
@@ -158,6 +162,16 @@ def _job_twist_full(job):
     low, ess, st = oracle.twist(_bm(colptr, rows))
     st["wall"] = time.perf_counter() - t0
     return low, ess, st
+
+
+def _job_config_oracle(job):
+    """The oracle's twist on config 0 or 2 (regenerated here)."""
+    from openph_gb300 import complexes as cx
+    import oracle
+    kind, size, seed = job
+    bm = cx.rips_cube(size, seed=seed) if kind == "rips_cube" else cx.lower_star_image(size, size, seed=seed)
+    low, ess, _ = oracle.twist(bm)
+    return kind, low, ess
 
 
 def _job_variants_oracle(job):
@@ -725,6 +739,44 @@ def run_batch(args, local, pool, cores, count, before_timing=None):
     }
 
 
+# ------------------------------------------------------------- configs
+def run_configs(local, pool):
+    """The two single-complex configurations beside the headline: the
+    50-point Rips cube (20,875 columns) and the 512x512 lower-star image
+    (1,568,771 columns), pms through the library's own choice of matrix;
+    device time (CUDA events) and wall time of the call with host CSC in and
+    host low/ess out, the fastest of five after two warm-ups; low and ess
+    checked against the oracle's twist (in the worker pool, waited for here,
+    before the serve timing)."""
+    from openph_gb300 import api
+    from openph_gb300 import complexes as cx
+    jobs = [("rips_cube", CONFIGS["rips_cube_points"], CONFIGS["rips_cube_seed"]),
+            ("lower_star", CONFIGS["lower_star_side"], CONFIGS["lower_star_seed"])]
+    want_async = pool.map_async(_job_config_oracle, jobs, chunksize=1)
+    out = {}
+    ctx = api.Context(local)
+    for kind, size, seed in jobs:
+        bm = cx.rips_cube(size, seed=seed) if kind == "rips_cube" else cx.lower_star_image(size, size, seed=seed)
+        for _ in range(2):
+            ctx.reduce(bm, "pms")
+        dev, wall = [], []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            low, ess, info = ctx.reduce(bm, "pms")
+            wall.append(time.perf_counter() - t0)
+            dev.append(info["device_ms"])
+        out[kind] = {"columns": bm.m, "device_ms": min(dev), "wall_ms": 1e3 * min(wall),
+                     "cols_per_s": bm.m / (min(dev) / 1e3), "e2e_cols_per_s": bm.m / min(wall),
+                     "matrix_reduced": {0: "D", 1: "D'", 2: "per block (D and D')"}[info["dual"]],
+                     "sweeps": info["sweeps"], "low": low, "ess": ess}
+    ctx.close()
+    for kind, low, ess in want_async.get():
+        v = out[kind]
+        v["low_ess_equal_oracle"] = bool(np.array_equal(v.pop("low"), low) and np.array_equal(v.pop("ess"), ess))
+    log("configs: " + ", ".join(f"{k} {v['device_ms']:.2f} ms" for k, v in out.items()))
+    return out
+
+
 # ------------------------------------------------------------ variants
 def run_variants(local, pool):
     """The six other algorithms of the reference (standard, twist, ph_row and
@@ -965,6 +1017,9 @@ def run_ours(args, ws, rank, local):
             "definition": "4 (nnz + m + 1) + 4 m + 4 (|P| + |T| + |T xor P|) over the CPU twist's additions on "
                           "D, per reduction; not a bandwidth achieved (the anti-transpose avoids that work)"}
     if args.workload == "all":
+        configs = run_configs(local, pool)
+        ok &= all(v["low_ess_equal_oracle"] for v in configs.values())
+        line["configs"] = configs
         variants = run_variants(local, pool)
         ok &= all(v["low_equal_oracle"] for v in variants["algorithms"].values())
         line["variants"] = variants
