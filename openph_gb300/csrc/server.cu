@@ -22,13 +22,19 @@
 // (the automatic rule of dual.cu, decided at submission): a Rips-like
 // request goes through its anti-transpose, built at admission straight into
 // its own column range and pool region, with its dimension buckets in
-// ascending order (per instance: iasc / ibucket / iopen); the others on D.
+// ascending order (per instance: iasc / ibucket / iopen); a request split
+// by dimension block (a lower-star image) as two instances side by side,
+// its D' part first and its D part from the D' part's second sweep on, the
+// lows merged when both have converged; the others on D.
 // Phase I visits only the unresolved columns: a list in column order,
 // compacted by every sweep, into which each admitted request's column range
 // is merged (k_srv_merge).  A retired request's columns leave the list in
-// the next sweep, and only then is its column range handed out again.  The reduction of a request is the
-// same whether it runs alone or in the mix: block-diagonal columns never add
-// into each other, and the lows of a reduced matrix are unique.
+// the next sweep, and only then is its column range handed out again.  The
+// bitmap tiers' chains stop after SERVE_CHAIN_CAP additions a sweep, so no
+// sweep of every request waits on one long chain.  The reduction of a
+// request is the same whether it runs alone or in the mix: block-diagonal
+// columns never add into each other, and the lows of a reduced matrix are
+// unique.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
