@@ -28,6 +28,12 @@
 //   * On the anti-transpose (dual.cu) Phase II takes the dimension buckets in
 //     ascending order, so that each bucket's pivots clear the next bucket's
 //     columns before they are reduced (twist's order).
+//   * Phase I visits a compacted list of the unresolved columns; the first
+//     holds only the columns with a low (k_list_*): a zero column never adds
+//     or repeats, and on the anti-transpose of a Rips complex the zero top
+//     dimension is almost all of the matrix.
+//   * Columns can arrive cleared (Work::preclear: the per-block form, where
+//     another part reduces them); Phase 0 skips those, Phase I zeroes them.
 //   * Convergence is tested on the device (the count of repeated lows from
 //     Phase I); kernels of a converged sweep return at once, so the host reads
 //     one status word per batch of sweeps, and the sweeps of a batch are
